@@ -1,0 +1,546 @@
+/* CPU restatement of metaLBM's fused collide-and-stream pull step.
+ *
+ * TEST INFRASTRUCTURE ONLY: the oracle the CUDA path is checked against and
+ * the "port" CPU baseline. Parity of this file with the reference is pinned
+ * bit-for-bit by tests/test_oracle_golden.py against vectors produced by the
+ * reference itself (oracle/_ref, tests/golden/make_golden.py).
+ *
+ * Every floating-point expression below keeps the reference's operation order
+ * (left-to-right C++ evaluation of the cited lines) and must be compiled with
+ * -ffp-contract=off, so each multiply and add is rounded separately as in the
+ * reference build.
+ */
+#include "mlbm_oracle.h"
+
+#include <math.h>
+#include <pthread.h>
+#include <stdlib.h>
+#include <string.h>
+
+#ifndef M_PI
+#define M_PI 3.14159265358979323846
+#endif
+
+/* ---- Lattice tables (Lattice.h:145-210, 535-612, 614-703) ---------------
+ * Velocity order: rest, the faceQ populations with c_x = -1, the faceQ with
+ * c_x = +1, then c_x = 0. Weights written as the reference's (T)a/(T)b. */
+static const int C_D2Q9[9][3] = {{0, 0, 0},  {-1, 1, 0}, {-1, 0, 0}, {-1, -1, 0}, {1, -1, 0},
+                                 {1, 0, 0},  {1, 1, 0},  {0, -1, 0}, {0, 1, 0}};
+static const int C_D3Q19[19][3] = {
+    {0, 0, 0},  {-1, 0, 0}, {-1, -1, 0}, {-1, 1, 0}, {-1, 0, -1}, {-1, 0, 1}, {1, 0, 0},
+    {1, 1, 0},  {1, -1, 0}, {1, 0, 1},   {1, 0, -1}, {0, -1, 0},  {0, 0, -1}, {0, -1, -1},
+    {0, -1, 1}, {0, 1, 0},  {0, 0, 1},   {0, 1, 1},  {0, 1, -1}};
+static const int C_D3Q27[27][3] = {
+    {0, 0, 0},   {-1, 0, 0},  {-1, -1, 0}, {-1, 1, 0}, {-1, 0, -1}, {-1, 0, 1},  {-1, -1, -1},
+    {-1, -1, 1}, {-1, 1, -1}, {-1, 1, 1},  {1, 0, 0},  {1, 1, 0},   {1, -1, 0},  {1, 0, 1},
+    {1, 0, -1},  {1, 1, 1},   {1, 1, -1},  {1, -1, 1}, {1, -1, -1}, {0, -1, 0},  {0, 0, -1},
+    {0, -1, -1}, {0, -1, 1},  {0, 1, 0},   {0, 0, 1},  {0, 1, 1},   {0, 1, -1}};
+
+static void weights(int lattice, double* w) {
+  if (lattice == ORACLE_D2Q9) {
+    const double a = 4.0 / 9.0, b = 1.0 / 36.0, c = 1.0 / 9.0;
+    const double t[9] = {a, b, c, b, b, c, b, c, c};
+    memcpy(w, t, sizeof t);
+  } else if (lattice == ORACLE_D3Q19) {
+    const double a = 1.0 / 3.0, b = 1.0 / 18.0, c = 1.0 / 36.0;
+    const double t[19] = {a, b, c, c, c, c, b, c, c, c, c, b, b, c, c, b, b, c, c};
+    memcpy(w, t, sizeof t);
+  } else {
+    const double a = 8.0 / 27.0, b = 2.0 / 27.0, c = 1.0 / 54.0, d = 1.0 / 216.0;
+    const double t[27] = {a, b, c, c, c, c, d, d, d, d, b, c, c, c,
+                          c, d, d, d, d, b, b, c, c, b, b, c, c};
+    memcpy(w, t, sizeof t);
+  }
+}
+
+int oracle_lattice_q(int lattice) {
+  return lattice == ORACLE_D2Q9 ? 9 : (lattice == ORACLE_D3Q19 ? 19 : 27);
+}
+int oracle_lattice_d(int lattice) { return lattice == ORACLE_D2Q9 ? 2 : 3; }
+
+static const int (*celerity(int lattice))[3] {
+  return lattice == ORACLE_D2Q9 ? C_D2Q9 : (lattice == ORACLE_D3Q19 ? C_D3Q19 : C_D3Q27);
+}
+
+void oracle_lattice_tables(int lattice, double* c, double* w) {
+  const int Q = oracle_lattice_q(lattice);
+  const int(*ci)[3] = celerity(lattice);
+  for (int q = 0; q < Q; ++q)
+    for (int d = 0; d < 3; ++d) c[q * 3 + d] = (double)ci[q][d];
+  weights(lattice, w);
+}
+
+#define QMAX 27
+
+typedef struct {
+  int D, Q;
+  double c[QMAX][3];
+  double w[QMAX];
+} lattice_t;
+
+static void lattice_init(lattice_t* L, int lattice) {
+  L->D = oracle_lattice_d(lattice);
+  L->Q = oracle_lattice_q(lattice);
+  const int(*ci)[3] = celerity(lattice);
+  for (int q = 0; q < L->Q; ++q)
+    for (int d = 0; d < 3; ++d) L->c[q][d] = (double)ci[q][d];
+  weights(lattice, L->w);
+}
+
+/* MathVector::dot (MathVector.h:45-53): a0*b0, then += ai*bi. */
+static inline double dotD(const double* a, const double* b, int D) {
+  double r = a[0] * b[0];
+  for (int d = 1; d < D; ++d) r += a[d] * b[d];
+  return r;
+}
+
+/* Equilibrium<TruncationMa3>::calculate (Equilibrium.h:14-33), inv_cs2 = 3,
+ * Power<T,n> = left-folded products (Helpers.h:93-113). */
+static inline double equilibrium(const lattice_t* L, double rho, const double* u, double u2,
+                                 int q) {
+  const double cu = dotD(L->c[q], u, L->D);
+  const double fEq = 1.0 + cu * 3.0 - 0.5 * u2 * 3.0 + 0.5 * 9.0 * cu * cu -
+                     0.5 * 9.0 * cu * u2 + (cu * cu * cu) * 27.0 / 6.0 +
+                     0.125 * u2 * u2 * 9.0 - 0.25 * cu * cu * u2 * 27.0 +
+                     (cu * cu * cu * cu) * 81.0 / 24.0;
+  return rho * L->w[q] * fEq;
+}
+
+double oracle_equilibrium(int lattice, double rho, const double* u, int q) {
+  lattice_t L;
+  lattice_init(&L, lattice);
+  return equilibrium(&L, rho, u, dotD(u, u, L.D), q);
+}
+
+struct oracle_state {
+  oracle_config cfg;
+  lattice_t L;
+  long V;
+  double beta;
+  double* prev;
+  double* next;
+  double* alpha; /* per node, persists across steps (Algorithm.h:103-106) */
+  double* rho;   /* stored fields (Algorithm.h:150-194) */
+  double* u;
+  double* force;
+  long long* newton_iterations;
+  long long* fallbacks;
+  long long* bisections;
+};
+
+/* ---- Forces (Force.h:137-292) ------------------------------------------
+ * Coordinates are node-local (Collision.h:86: iP - halo). Sinusoidal:
+ * F_d = A_d sin(x_d * 2 * pi / lambda_d) per axis (Force.h:208-215);
+ * Kolmogorov: F_x = A_x sin(y * 2 * pi / lambda_x), other components 0
+ * (Force.h:262-267). The unsigned coordinate times 2 is formed in integers
+ * before the double multiply, as in the reference expression. */
+static double sin_arg(unsigned coord, double lambda) {
+  return (double)(coord * 2u) * M_PI / lambda;
+}
+
+static void node_force(const oracle_state* s, const unsigned* pos, double* F) {
+  const oracle_config* c = &s->cfg;
+  const int D = s->L.D;
+  for (int d = 0; d < 3; ++d) F[d] = 0.0;
+  switch (c->force) {
+    case ORACLE_F_CONSTANT:
+      for (int d = 0; d < D; ++d) F[d] = c->amplitude[d];
+      break;
+    case ORACLE_F_SINUSOIDAL:
+      for (int d = 0; d < D; ++d) F[d] = c->amplitude[d] * sin(sin_arg(pos[d], c->wavelength[d]));
+      break;
+    case ORACLE_F_KOLMOGOROV: {
+      const int k = c->kolmogorov_component;
+      F[k] = c->amplitude[k] * sin(sin_arg(pos[c->kolmogorov_axis], c->wavelength[k]));
+      break;
+    }
+    default:
+      break;
+  }
+}
+
+/* ---- Forcing schemes (ForcingScheme.h:17-198) -------------------------- */
+static inline double collision_source(const oracle_state* s, const double* F, double rho,
+                                      const double* u, double eq_q, int q) {
+  const lattice_t* L = &s->L;
+  const int D = L->D;
+  switch (s->cfg.forcing) {
+    case ORACLE_FS_GUO: { /* ForcingScheme.h:100-117 */
+      const double cu = dotD(L->c[q], u, D);
+      double v[3] = {0.0, 0.0, 0.0};
+      for (int d = 0; d < D; ++d) v[d] = L->c[q][d] - u[d] + L->c[q][d] * (3.0 * cu);
+      const double R = dotD(v, F, D);
+      return (1.0 - 1.0 / (2.0 * s->cfg.tau)) * L->w[q] * 3.0 * R;
+    }
+    case ORACLE_FS_EDM: { /* ForcingScheme.h:183-197 */
+      const double inv = 1.0 / rho;
+      double v[3] = {0.0, 0.0, 0.0};
+      for (int d = 0; d < D; ++d) v[d] = u[d] + F[d] * inv;
+      return equilibrium(L, rho, v, dotD(v, v, D), q) - eq_q;
+    }
+    default: /* None (ForcingScheme.h:68-78), ShanChen (141-151) */
+      return 0.0;
+  }
+}
+
+/* ---- Entropic step (EntropicStep.h:15-63) ------------------------------ */
+typedef struct {
+  const double* f;    /* pulled populations */
+  const double* fneq; /* f - f_eq */
+  const double* w;
+  int Q;
+} hfun_t;
+
+static double h_function(const hfun_t* h, double alpha) {
+  double r = 0.0;
+  for (int q = 0; q < h->Q; ++q) {
+    const double f = h->f[q];
+    const double g = f - alpha * h->fneq[q];
+    r += f * log(f / h->w[q]) - g * log(g / h->w[q]);
+  }
+  return r;
+}
+
+static double h_derivative(const hfun_t* h, double alpha) {
+  double r = 0.0;
+  for (int q = 0; q < h->Q; ++q) {
+    const double g = h->f[q] - alpha * h->fneq[q];
+    r += h->fneq[q] * (1 + log(g / h->w[q]));
+  }
+  return r;
+}
+
+/* NewtonRaphsonSolver (EntropicStep.h:111-140). */
+static int newton(const hfun_t* h, double tol, int maxit, double* xR, double xMin, double xMax,
+                  long long* iters) {
+  double xStep = 0.0;
+  for (int it = 1; it <= maxit; ++it) {
+    *xR = *xR - xStep;
+    const double fe = h_function(h, *xR);
+    const double de = h_derivative(h, *xR);
+    ++*iters;
+    xStep = fe / de;
+    const double error = fabs(xStep);
+    if (error <= tol) return (*xR > xMin && *xR < xMax) ? 1 : 0;
+  }
+  return 0;
+}
+
+/* Residual-mode H-function: F = A - sum g ln(g/w) with A = sum f ln(f/w)
+ * precomputed, and F' = sum f_neq (1 + ln(g/w)) from the same logarithms.
+ * A population with g <= 0 (alpha at alpha_max) contributes its limit 0 to
+ * g ln g; alpha_max keeps every other g positive. */
+static void h_residual(const hfun_t* h, double A, double alpha, double* F, double* dF) {
+  double S = 0.0, Dv = 0.0;
+  for (int q = 0; q < h->Q; ++q) {
+    const double g = h->f[q] - alpha * h->fneq[q];
+    if (g > 0.0) {
+      const double l = log(g / h->w[q]);
+      S += g * l;
+      Dv += h->fneq[q] * (1 + l);
+    } else {
+      Dv += h->fneq[q] * (1 + log(4.9406564584124654e-324 / h->w[q]));
+    }
+  }
+  *F = A - S;
+  *dF = Dv;
+}
+
+/* Safeguarded bisection-Newton on [xMin, xMax], the update rule of
+ * Bisection_NewtonRaphsonSolver (EntropicStep.h:142-220) with |F| <= tol as
+ * the acceptance test. */
+static int bisection_newton_residual(const hfun_t* h, double A, double tol, int maxit,
+                                     double* xR, double xMin, double xMax, long long* iters) {
+  double fLow, fHigh, d;
+  h_residual(h, A, xMin, &fLow, &d);
+  h_residual(h, A, xMax, &fHigh, &d);
+  if ((fLow > 0.0 && fHigh > 0.0) || (fLow < 0.0 && fHigh < 0.0)) return 0;
+  if (fabs(fLow) <= tol) { *xR = xMin; return 1; }
+  if (fabs(fHigh) <= tol) { *xR = xMax; return 1; }
+  double xLow, xHigh;
+  if (fLow < 0.0) { xLow = xMin; xHigh = xMax; } else { xLow = xMax; xHigh = xMin; }
+  double x = 0.5 * (xMin + xMax);
+  double dxOld = fabs(xMax - xMin), dx = dxOld;
+  double fe, de;
+  h_residual(h, A, x, &fe, &de);
+  for (int it = 1; it <= maxit; ++it) {
+    if (fabs(fe) <= tol) { *xR = x; return 1; }
+    ++*iters;
+    if ((((x - xHigh) * de - fe) * ((x - xLow) * de - fe) > 0.0) ||
+        (fabs(2.0 * fe) > fabs(dxOld * de))) {
+      dxOld = dx;
+      dx = 0.5 * (xHigh - xLow);
+      x = xLow + dx;
+      if (xLow == x) { *xR = x; return 1; }
+    } else {
+      dxOld = dx;
+      dx = fe / de;
+      const double xTemp = x;
+      x -= dx;
+      if (xTemp == x) { *xR = x; return 1; }
+    }
+    h_residual(h, A, x, &fe, &de);
+    if (fe < 0.0) xLow = x; else xHigh = x;
+  }
+  *xR = x;
+  return fabs(fe) <= tol;
+}
+
+/* Residual-mode solve from a guess (see mlbm_oracle.h). */
+static double solve_residual(const hfun_t* h, double tol, int maxit, double guess, double xMax,
+                             long long* iters, long long* fallbacks, long long* bisections) {
+  double A = 0.0;
+  for (int q = 0; q < h->Q; ++q) A += h->f[q] * log(h->f[q] / h->w[q]);
+  double x = guess;
+  if (x > 1.0 && x < xMax) {
+    double fe, de;
+    h_residual(h, A, x, &fe, &de);
+    if (fabs(fe) <= tol) return x;
+    for (int it = 1; it <= maxit; ++it) {
+      ++*iters;
+      x -= fe / de;
+      if (!(x > 1.0 && x < xMax)) break;
+      h_residual(h, A, x, &fe, &de);
+      if (fabs(fe) <= tol) return x;
+    }
+  }
+  ++*bisections;
+  if (bisection_newton_residual(h, A, tol, maxit, &x, 1.0, xMax, iters)) return x;
+  ++*fallbacks;
+  return 2.0;
+}
+
+/* ELBM::calculateAlpha (Collision.h:351-375) with isDeviationSmall (284-303),
+ * calculateAlphaMax (305-326) and solveAlpha (328-349). */
+static double entropic_alpha(const oracle_state* s, const double* f, const double* fneq,
+                             double guess, long long* iters, long long* fallbacks,
+                             long long* bisections) {
+  const int Q = s->L.Q;
+  const oracle_config* c = &s->cfg;
+  int small = 1;
+  for (int q = 0; q < Q; ++q)
+    if (fabs(fneq[q]) / f[q] > c->deviation_threshold) small = 0;
+  if (small) return 2.0;
+  double alphaMax = 2.5;
+  for (int q = 0; q < Q; ++q) {
+    if (fneq[q] > 0) {
+      const double t = fabs(f[q]) / fneq[q];
+      if (t < alphaMax) alphaMax = t;
+    }
+  }
+  if (alphaMax < 2.) return 0.95 * alphaMax;
+  const hfun_t h = {f, fneq, s->L.w, Q};
+  if (c->guess_mode == ORACLE_GUESS_TWO) guess = 2.0;
+  if (c->alpha_mode == ORACLE_ALPHA_RESIDUAL)
+    return solve_residual(&h, c->newton_tolerance, c->newton_max_iterations, guess, alphaMax,
+                          iters, fallbacks, bisections);
+  double alpha = guess;
+  if (newton(&h, c->newton_tolerance, c->newton_max_iterations, &alpha, 1., alphaMax, iters))
+    return alpha;
+  ++*fallbacks;
+  return 2.0;
+}
+
+/* ---- One node of the fused pull step (Algorithm.h:97-126) -------------- */
+static void node_update(oracle_state* s, unsigned x, unsigned y, unsigned z, int store,
+                        long long* iters, long long* fallbacks, long long* bisections) {
+  const lattice_t* L = &s->L;
+  const oracle_config* c = &s->cfg;
+  const int Q = L->Q, D = L->D;
+  const unsigned lx = (unsigned)c->lx, ly = (unsigned)c->ly, lz = (unsigned)c->lz;
+  const long V = s->V;
+  const long idx = ((long)x * ly + y) * lz + z;
+
+  /* Pulled populations f_q(x - c_q): periodic wrap by modulo replaces the
+   * reference's halo planes (Communication.h:134-180, Boundary.h:50-100). */
+  double f[QMAX] = {0.0};
+  for (int q = 0; q < Q; ++q) {
+    const int* cq = celerity(c->lattice)[q];
+    const long sx = ((long)x - cq[0] + lx) % lx;
+    const long sy = ((long)y - cq[1] + ly) % ly;
+    const long sz = ((long)z - cq[2] + lz) % lz;
+    f[q] = s->prev[(long)q * V + (sx * ly + sy) * lz + sz];
+  }
+
+  /* Moment::calculateDensity / calculateVelocity (Moment.h:13-47). */
+  double rho = f[0];
+  for (int q = 1; q < Q; ++q) rho += f[q];
+  double u[3] = {0.0, 0.0, 0.0};
+  for (int d = 0; d < D; ++d) u[d] = L->c[0][d] * f[0];
+  for (int q = 1; q < Q; ++q)
+    for (int d = 0; d < D; ++d) u[d] += L->c[q][d] * f[q];
+  for (int d = 0; d < D; ++d) u[d] /= rho;
+  const double u2 = dotD(u, u, D);
+
+  /* Collision::setForce (Collision.h:81-88). */
+  const unsigned pos[3] = {x, y, z};
+  double F[3];
+  node_force(s, pos, F);
+
+  double* nxt = s->next;
+  double alpha;
+  if (c->collision == ORACLE_BGK) {
+    /* Collision<BGK>::collideAndStream (Collision.h:134-151). */
+    alpha = 2.0;
+    const double a = 1. - 2. * s->beta, b = 2. * s->beta;
+    for (int q = 0; q < Q; ++q) {
+      const double eq = equilibrium(L, rho, u, u2, q);
+      nxt[(long)q * V + idx] = a * f[q] + b * eq + collision_source(s, F, rho, u, eq, q);
+    }
+  } else {
+    /* Collision<ELBM>::calculateRelaxationTime (Collision.h:227-241) and
+     * collideAndStream (243-258). */
+    double fneq[QMAX];
+    for (int q = 0; q < Q; ++q) fneq[q] = f[q] - equilibrium(L, rho, u, u2, q);
+    alpha = entropic_alpha(s, f, fneq, s->alpha[idx], iters, fallbacks, bisections);
+    const double tauEff = 1.0 / (alpha * s->beta);
+    const double inv = 1.0 / tauEff;
+    for (int q = 0; q < Q; ++q) {
+      const double eq = f[q] - fneq[q];
+      nxt[(long)q * V + idx] = f[q] - inv * fneq[q] + collision_source(s, F, rho, u, eq, q);
+    }
+  }
+  s->alpha[idx] = alpha;
+
+  if (store) { /* Algorithm::storeFields (Algorithm.h:150-194) */
+    s->rho[idx] = rho;
+    for (int d = 0; d < D; ++d) {
+      /* ForcingScheme::calculateHydrodynamicVelocity: u + 0.5/rho F
+       * (ForcingScheme.h:27-33), unshifted for None (53-57). */
+      const double uh = (c->forcing == ORACLE_FS_NONE) ? u[d] : u[d] + F[d] * (0.5 / rho);
+      s->u[(long)d * V + idx] = uh;
+      s->force[(long)d * V + idx] = F[d];
+    }
+  }
+}
+
+oracle_state* oracle_create(const oracle_config* cfg) {
+  oracle_state* s = (oracle_state*)calloc(1, sizeof(oracle_state));
+  if (!s) return NULL;
+  s->cfg = *cfg;
+  if (s->cfg.threads < 1) s->cfg.threads = 1;
+  lattice_init(&s->L, cfg->lattice);
+  if (s->L.D == 2) s->cfg.lz = 1;
+  s->V = (long)s->cfg.lx * s->cfg.ly * s->cfg.lz;
+  s->beta = (double)1.0 / (2.0 * cfg->tau);
+  const long V = s->V, Q = s->L.Q, D = s->L.D;
+  s->prev = (double*)calloc((size_t)(Q * V), sizeof(double));
+  s->next = (double*)calloc((size_t)(Q * V), sizeof(double));
+  s->alpha = (double*)malloc(sizeof(double) * (size_t)V);
+  s->rho = (double*)calloc((size_t)V, sizeof(double));
+  s->u = (double*)calloc((size_t)(D * V), sizeof(double));
+  s->force = (double*)calloc((size_t)(D * V), sizeof(double));
+  s->newton_iterations = (long long*)calloc((size_t)s->cfg.threads, sizeof(long long));
+  s->fallbacks = (long long*)calloc((size_t)s->cfg.threads, sizeof(long long));
+  s->bisections = (long long*)calloc((size_t)s->cfg.threads, sizeof(long long));
+  if (!s->prev || !s->next || !s->alpha || !s->rho || !s->u || !s->force ||
+      !s->newton_iterations || !s->fallbacks || !s->bisections) {
+    oracle_destroy(s);
+    return NULL;
+  }
+  for (long i = 0; i < V; ++i) s->alpha[i] = 2.0;
+  return s;
+}
+
+void oracle_destroy(oracle_state* s) {
+  if (!s) return;
+  free(s->prev);
+  free(s->next);
+  free(s->alpha);
+  free(s->rho);
+  free(s->u);
+  free(s->force);
+  free(s->newton_iterations);
+  free(s->fallbacks);
+  free(s->bisections);
+  free(s);
+}
+
+void oracle_init_equilibrium(oracle_state* s, const double* rho, const double* u) {
+  const long V = s->V;
+  const int Q = s->L.Q, D = s->L.D;
+  for (long i = 0; i < V; ++i) {
+    double v[3] = {0, 0, 0};
+    for (int d = 0; d < D; ++d) v[d] = u[(long)d * V + i];
+    const double u2 = dotD(v, v, D);
+    for (int q = 0; q < Q; ++q) s->prev[(long)q * V + i] = equilibrium(&s->L, rho[i], v, u2, q);
+    s->alpha[i] = 2.0;
+  }
+}
+
+void oracle_set_populations(oracle_state* s, const double* f) {
+  memcpy(s->prev, f, sizeof(double) * (size_t)(s->L.Q * s->V));
+}
+
+void oracle_get_populations(const oracle_state* s, double* f) {
+  memcpy(f, s->prev, sizeof(double) * (size_t)(s->L.Q * s->V));
+}
+
+typedef struct {
+  oracle_state* s;
+  int tid, store;
+} sweep_arg;
+
+static void* sweep(void* p) {
+  sweep_arg* a = (sweep_arg*)p;
+  oracle_state* s = a->s;
+  const int T = s->cfg.threads;
+  const unsigned lx = (unsigned)s->cfg.lx, ly = (unsigned)s->cfg.ly, lz = (unsigned)s->cfg.lz;
+  /* X slabs, as the reference's 1-D MPI decomposition (Domain.h:22-24). */
+  const unsigned x0 = (unsigned)((long)lx * a->tid / T), x1 = (unsigned)((long)lx * (a->tid + 1) / T);
+  long long it = 0, fb = 0, bi = 0;
+  for (unsigned x = x0; x < x1; ++x)
+    for (unsigned y = 0; y < ly; ++y)
+      for (unsigned z = 0; z < lz; ++z) node_update(s, x, y, z, a->store, &it, &fb, &bi);
+  s->newton_iterations[a->tid] = it;
+  s->fallbacks[a->tid] = fb;
+  s->bisections[a->tid] = bi;
+  return NULL;
+}
+
+void oracle_step(oracle_state* s, int nsteps, int store_last) {
+  const int T = s->cfg.threads;
+  for (int it = 1; it <= nsteps; ++it) {
+    const int store = store_last && it == nsteps;
+    if (T == 1) {
+      sweep_arg a = {s, 0, store};
+      sweep(&a);
+    } else {
+      pthread_t th[256];
+      sweep_arg args[256];
+      const int n = T > 256 ? 256 : T;
+      for (int t = 0; t < n; ++t) {
+        args[t].s = s;
+        args[t].tid = t;
+        args[t].store = store;
+        pthread_create(&th[t], NULL, sweep, &args[t]);
+      }
+      for (int t = 0; t < n; ++t) pthread_join(th[t], NULL);
+    }
+    double* tmp = s->prev;
+    s->prev = s->next;
+    s->next = tmp;
+  }
+}
+
+void oracle_get_fields(const oracle_state* s, double* rho, double* u, double* alpha,
+                       double* force) {
+  const long V = s->V, D = s->L.D;
+  if (rho) memcpy(rho, s->rho, sizeof(double) * (size_t)V);
+  if (u) memcpy(u, s->u, sizeof(double) * (size_t)(D * V));
+  if (alpha) memcpy(alpha, s->alpha, sizeof(double) * (size_t)V);
+  if (force) memcpy(force, s->force, sizeof(double) * (size_t)(D * V));
+}
+
+void oracle_get_counters(const oracle_state* s, long long* newton_iterations,
+                         long long* fallbacks, long long* bisections) {
+  long long a = 0, b = 0, c = 0;
+  for (int t = 0; t < s->cfg.threads; ++t) {
+    a += s->newton_iterations[t];
+    b += s->fallbacks[t];
+    c += s->bisections[t];
+  }
+  if (newton_iterations) *newton_iterations = a;
+  if (fallbacks) *fallbacks = b;
+  if (bisections) *bisections = c;
+}
