@@ -1,0 +1,440 @@
+"""Benchmark of the fused collide-and-stream pull step on GB300.
+
+Default workload (the one the headline metric is quoted on): D3Q27 entropic
+SRT, FP32 population storage, 512^3 periodic lattice, beta = 0.9995, initial
+field = Taylor-Green vortex (U0 = 0.05) + random-phase solenoidal
+perturbation of amplitude 1e-3 on the shell 8 <= |k| <= 10 (seed 2). Every
+node solves for alpha in FP64 to |F(alpha)| <= 1e-12 (bisection-Newton
+fallback). Two arms run on the same GPU from the same state: the learned
+alpha guess (the committed MLP) and plain Newton from the previous alpha.
+`value` is the learned arm's MLUPS; the Newton arm is reported beside it.
+
+Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+       [--workload entropic_learned_512|bgk_d3q19_f64_256|bgk_d3q19_f32_256]
+Under torchrun (N > 1) every rank runs an independent replica of the workload
+on its own GPU (the path has no data exchange on one lattice per GPU); the
+timed region is bracketed by barriers and the max over ranks is used.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "D3Q27 entropic MLUPS, learned-α vs Newton-α on 1 GB300 at equal H-residual; %HBM"
+BETA = 0.9995
+TAU = 1.0 / (2.0 * BETA)
+
+
+def measured_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        return json.loads(p.read_text()), "measured"
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+# ---------------------------------------------------------------------------
+# workloads
+WORKLOADS = {
+    "entropic_learned_512": dict(latticeT="D3Q27", collisionT="ELBM", relaxationTime=TAU,
+                                 globalLength=(512, 512, 512), storage="f32",
+                                 alphaSolver="residual", newtonTolerance=1e-12,
+                                 deviationThreshold=0.0, bytes_per_node=2 * 27 * 4 + 8),
+    "bgk_d3q19_f64_256": dict(latticeT="D3Q19", collisionT="BGK", relaxationTime=0.55,
+                              forcingSchemeT="Guo", forceT="Kolmogorov",
+                              forceAmplitude=(1e-6, 0.0, 0.0), forceWaveLength=(128.0, 1.0, 1.0),
+                              kolmogorovAxis=2, globalLength=(256, 256, 256), storage="f64",
+                              bytes_per_node=2 * 19 * 8),
+    "bgk_d3q19_f32_256": dict(latticeT="D3Q19", collisionT="BGK", relaxationTime=0.55,
+                              forcingSchemeT="Guo", forceT="Kolmogorov",
+                              forceAmplitude=(1e-6, 0.0, 0.0), forceWaveLength=(128.0, 1.0, 1.0),
+                              kolmogorovAxis=2, globalLength=(256, 256, 256), storage="f32",
+                              bytes_per_node=2 * 19 * 4),
+}
+
+
+def initial_field(name: str, shape):
+    from metalbm_gb300 import fields
+    if name.startswith("entropic"):
+        rho, u = fields.taylor_green(shape, u0=0.05)
+        u = u + fields.solenoidal_shell(shape, 8.0, 10.0, 1e-3, seed=2)
+        return rho, u
+    return fields.perturbed_rest(shape, 3, 1e-4, seed=1)
+
+
+def deck_for(name: str, **over):
+    from metalbm_gb300 import InputDeck
+    w = {k: v for k, v in WORKLOADS[name].items() if k != "bytes_per_node"}
+    w.update(over)
+    return InputDeck(**w)
+
+
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines: list[str] = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.QUERY}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self) -> dict:
+        sm, smax, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = max(smax, float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": smax or None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+def time_steps(lat, steps: int, torch, dist=None):
+    """Time `steps` single-step calls with CUDA events on the handle's stream.
+    Returns (total ms, list of per-launch ms)."""
+    from metalbm_gb300.lattice import kernel_launch_count
+    stream = torch.cuda.ExternalStream(lat.stream)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(steps + 1)]
+    lat.sync()
+    if dist is not None:
+        dist.barrier()
+    torch.cuda.synchronize()
+    n0 = kernel_launch_count()
+    ev[0].record(stream)
+    for i in range(steps):
+        lat.step(1)
+        ev[i + 1].record(stream)
+    lat.sync()
+    torch.cuda.synchronize()
+    launches = kernel_launch_count() - n0
+    per = [ev[i].elapsed_time(ev[i + 1]) for i in range(steps)]
+    if dist is not None:
+        dist.barrier()
+    return ev[0].elapsed_time(ev[steps]), per, launches
+
+
+def load_or_train_model(deck, torch):
+    from metalbm_gb300 import alpha_model, fields
+    path = alpha_model.default_model_path(deck.latticeT)
+    if path.exists():
+        return alpha_model.load_model(path), str(path.relative_to(ROOT))
+    # no committed model: train a small one from a plain run (untimed setup)
+    shape = (64, 64, 64)
+    rho, u = fields.taylor_green(shape, u0=0.05)
+    small = deck_for("entropic_learned_512", globalLength=shape, alphaGuess="two")
+    X, y = alpha_model.collect_samples(small, rho, u, steps=100, every=25, n_per_log=100000)
+    model, _ = alpha_model.fit(X, y, small, epochs=20)
+    return model, "trained in bench setup (64^3, 100 steps)"
+
+
+def cpu_baseline_port(name: str, threads: int, seconds_budget: float = 20.0) -> dict:
+    """The oracle port (C restatement of the reference path) on the host
+    cores, on a bounded sample of the same workload."""
+    from oracle import ALPHA_REFERENCE, OracleConfig, OraclePort
+    w = WORKLOADS[name]
+    lat = w["latticeT"]
+    side = 64 if lat == "D3Q27" else 96
+    shape = (side, side, side)
+    rho, u = initial_field(name, shape)
+    cfg = OracleConfig(lattice=lat, collision="ELBM" if w["collisionT"] != "BGK" else "BGK",
+                       forcing=w.get("forcingSchemeT", "None"), force=w.get("forceT", "None"),
+                       tau=w["relaxationTime"], amplitude=w.get("forceAmplitude", (0, 0, 0)),
+                       wavelength=w.get("forceWaveLength", (1, 1, 1)),
+                       kolmogorov_axis=w.get("kolmogorovAxis", 1), size=shape,
+                       alpha_mode=ALPHA_REFERENCE, threads=threads)
+    port = OraclePort(cfg)
+    port.init_equilibrium(rho, u)
+    port.step(1, store_last=False)
+    steps, t0 = 0, time.perf_counter()
+    while True:
+        port.step(1, store_last=False)
+        steps += 1
+        dt = time.perf_counter() - t0
+        if dt > seconds_budget or steps >= 50:
+            break
+    V = int(np.prod(shape))
+    return {"value": V * steps / dt / 1e6, "unit": "MLUPS", "cores": threads, "kind": "port",
+            "sample": f"{lat} {w['collisionT']} FP64, reference alpha solver, {side}^3, "
+                      f"{steps} steps after 1 warm-up, {threads} threads"}
+
+
+# ---------------------------------------------------------------------------
+def run_ours(args):
+    import torch
+    import torch.distributed as dist_mod
+    from metalbm_gb300 import Lattice, build
+    from metalbm_gb300.lattice import kernel_launch_count
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        torch.cuda.set_device(local)
+        dist_mod.init_process_group("nccl", device_id=torch.device("cuda", local))
+        dist = dist_mod
+    if rank == 0:
+        build.build()
+    if dist is not None:
+        dist.barrier()
+    name = args.workload
+    w = WORKLOADS[name]
+    deck = deck_for(name, device=local)
+    shape = deck.shape
+    V = int(np.prod(shape))
+    rho, u = initial_field(name, shape)
+    entropic = w["collisionT"] != "BGK"
+    extra = {}
+
+    # --- arm 1: the learned guess (or the only arm for BGK workloads)
+    if entropic:
+        model, model_src = load_or_train_model(deck, torch)
+        deck_l = deck_for(name, device=local, alphaGuess="learned")
+    else:
+        deck_l = deck
+    lat = Lattice(deck_l)
+    if entropic:
+        lat.set_alpha_model(model)
+    lat.init_equilibrium(rho, u)
+    lat.step(args.warmup)
+    with ClockSampler(local) as clk:
+        total_ms, per, launches = time_steps(lat, args.steps, torch, dist)
+    lat.step(1, diagnostics=True)
+    dl = lat.diagnostics()
+    lat.close()
+    t = torch.tensor([total_ms], device=f"cuda:{local}")
+    if dist is not None:
+        dist.all_reduce(t, op=dist_mod.ReduceOp.MAX)
+    total_ms = float(t.item())
+
+    # --- arm 2: plain Newton from the previous alpha, same state, same GPU
+    if entropic:
+        lat = Lattice(deck_for(name, device=local, alphaGuess="previous"))
+        lat.init_equilibrium(rho, u)
+        lat.step(args.warmup)
+        nt_ms, nt_per, _ = time_steps(lat, args.steps, torch, dist)
+        lat.step(1, diagnostics=True)
+        dn = lat.diagnostics()
+        lat.close()
+        tn = torch.tensor([nt_ms], device=f"cuda:{local}")
+        if dist is not None:
+            dist.all_reduce(tn, op=dist_mod.ReduceOp.MAX)
+        nt_ms = float(tn.item())
+        newton_mlups = world * V * args.steps / (nt_ms * 1e-3) / 1e6
+        solved = max(dl["solved_nodes"], 1)
+        extra = {
+            "newton_alpha": {"value": newton_mlups, "unit": "MLUPS",
+                             "ms_per_step": nt_ms / args.steps,
+                             "newton_iterations_per_solved_node": dn["newton_iterations"] / max(dn["solved_nodes"], 1),
+                             "guess_hit_fraction": dn["guess_hits"] / max(dn["solved_nodes"], 1),
+                             "fallback_nodes": dn["fallback_nodes"]},
+            "learned_alpha": {"newton_iterations_per_solved_node": dl["newton_iterations"] / solved,
+                              "fallback_fraction": (dl["solved_nodes"] - dl["guess_hits"]) / solved,
+                              "alpha2_fallback_nodes": dl["fallback_nodes"],
+                              "model": model_src},
+            "speedup_learned_vs_newton": (V * args.steps / (total_ms * 1e-3) / 1e6 * world) / newton_mlups,
+            "newton_iterations_saved_per_solved_node":
+                dn["newton_iterations"] / max(dn["solved_nodes"], 1) - dl["newton_iterations"] / solved,
+            "residual_tolerance": deck.newtonTolerance,
+        }
+
+    value = world * V * args.steps / (total_ms * 1e-3) / 1e6
+    peaks, peak_src = measured_peaks()
+    bpn = w["bytes_per_node"]
+    avg_launch_ms = float(np.mean(per))
+    achieved = bpn * V / (avg_launch_ms * 1e-3) / 1e9
+    traffic = None
+    tfile = ROOT / "profiles" / "traffic.json"
+    if tfile.exists():
+        tr = json.loads(tfile.read_text()).get(name)
+        if tr:
+            traffic = tr.get("dram_bytes_per_launch")
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                "frac": achieved / peaks["hbm_gbs"], "traffic": traffic,
+                "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs, burst copy)"
+                if peak_src == "measured" else "fallback 6.8 TB/s",
+                "bytes_per_node": bpn, "kernel": "elbm_lowp_kernel" if entropic else
+                ("bgk_f64_kernel" if w["storage"] == "f64" else "bgk_lowp_kernel")}
+
+    # --- end to end through the C ABI with host buffers (rank 0 reports)
+    e2e = run_e2e(name, deck_l, rho, u, model if entropic else None, args.steps, torch, dist, world)
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        cpu = cpu_baseline_port(name, os.cpu_count() or 1)
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "MLUPS", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64" if entropic or w["storage"] == "f64" else "f32",
+            "data": "synthetic (Taylor-Green + seeded solenoidal perturbation)" if entropic
+                    else "synthetic (seeded uniform velocity perturbation)",
+            "config": {"workload": name, "lattice": deck.latticeT, "collision": deck.collisionT,
+                       "storage": deck.storage, "grid": list(shape), "beta": 1 / (2 * deck.relaxationTime),
+                       "alpha_solver": deck.alphaSolver if entropic else None,
+                       "parallelism": f"replicas x{world}",
+                       "l2": f"inputs {V * 27 * 4 * 2 / 1e9:.1f} GB > 129 MB L2, no flush needed"},
+            "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
+            "clocks": clk.summary(), **extra,
+        }
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def run_e2e(name, deck, rho, u, model, steps, torch, dist, world):
+    """Whole job through the public C ABI from pinned host memory: init from
+    host rho/u (H2D), then per step mlbm_step(STORE_FIELDS|DIAGNOSTICS),
+    mlbm_get_diagnostics and mlbm_get_fields(rho, u) into pinned host
+    buffers (D2H)."""
+    from metalbm_gb300 import Lattice
+    V = rho.size
+    D = u.shape[0]
+    pin = lambda shape: torch.empty(shape, dtype=torch.float64, pin_memory=True).numpy()  # noqa
+    h_rho, h_u = pin((V,)), pin((D, V))
+    h_rho[:] = rho
+    h_u[:] = u
+    o_rho, o_u = pin((V,)), pin((D, V))
+    lat = Lattice(deck)
+    if model is not None:
+        lat.set_alpha_model(model)
+    lat.sync()
+    if dist is not None:
+        dist.barrier()
+    t0 = time.perf_counter()
+    lat.init_equilibrium(h_rho, h_u)
+    for _ in range(steps):
+        lat.step(1, store=True, diagnostics=True)
+        lat.diagnostics()
+        lat._check(lat._lib.mlbm_get_fields(lat.handle, o_rho.ctypes.data_as(_dp()),
+                                            o_u.ctypes.data_as(_dp()), None, None, 0))
+    lat.sync()
+    dt = time.perf_counter() - t0
+    lat.close()
+    t = torch.tensor([dt], device="cuda")
+    if dist is not None:
+        dist.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    dt = float(t.item())
+    h2d = (1 + D) * V * 8
+    d2h_step = (1 + D) * V * 8 + 160
+    return {"value": world * V * steps / dt / 1e6, "unit": "MLUPS",
+            "h2d_bytes_per_step": h2d // steps, "d2h_bytes_per_step": d2h_step,
+            "what": "mlbm_init_equilibrium from pinned host rho/u, then per step mlbm_step"
+                    "(STORE_FIELDS|DIAGNOSTICS) + mlbm_get_diagnostics + mlbm_get_fields(rho,u)"}
+
+
+def _dp():
+    import ctypes
+    return ctypes.POINTER(ctypes.c_double)
+
+
+# ---------------------------------------------------------------------------
+def run_reference(args):
+    """The reference's CPU implementation of the path (the oracle port of
+    metaLBM's serial Algorithm loop, reference alpha solver), on the host
+    cores, same workload family and metric; rank 0 only."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    name = args.workload
+    w = WORKLOADS[name]
+    threads = os.cpu_count() or 1
+    from oracle import ALPHA_REFERENCE, OracleConfig, OraclePort
+    side = 96 if w["latticeT"] == "D3Q27" else 128
+    shape = (side, side, side)
+    rho, u = initial_field(name, shape)
+    cfg = OracleConfig(lattice=w["latticeT"], collision="ELBM" if w["collisionT"] != "BGK" else "BGK",
+                       forcing=w.get("forcingSchemeT", "None"), force=w.get("forceT", "None"),
+                       tau=w["relaxationTime"], amplitude=w.get("forceAmplitude", (0, 0, 0)),
+                       wavelength=w.get("forceWaveLength", (1, 1, 1)),
+                       kolmogorov_axis=w.get("kolmogorovAxis", 1), size=shape,
+                       alpha_mode=ALPHA_REFERENCE, threads=threads)
+    port = OraclePort(cfg)
+    port.init_equilibrium(rho, u)
+    port.step(args.warmup, store_last=False)
+    t0 = time.perf_counter()
+    port.step(args.steps, store_last=False)
+    dt = time.perf_counter() - t0
+    V = int(np.prod(shape))
+    value = V * args.steps / dt / 1e6
+    sample = (f"{w['latticeT']} {w['collisionT']} FP64 with the reference alpha solver on a "
+              f"{side}^3 sample of the workload's initial field, {threads} threads (x slabs)")
+    print(json.dumps({
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "MLUPS", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic", "config": {"workload": name, "grid": list(shape)},
+        "cpu_baseline": {"value": value, "unit": "MLUPS", "cores": threads, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": value, "unit": "MLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="entropic_learned_512", choices=sorted(WORKLOADS))
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        ap.error("--warmup must be >= 3")
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

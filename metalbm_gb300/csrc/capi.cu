@@ -1,0 +1,778 @@
+// C ABI of the fused collide-and-stream pull step (include/mlbm/mlbm.h).
+//
+// Host side of the drop-in: it owns the device buffers of one periodic
+// lattice (what Distribution and FieldList own in the reference,
+// Distribution.h:14-43, FieldList.h:22-86), converts host arrays between the
+// dense and the reference's padded layout, and enqueues the step kernels on
+// one CUDA stream. Errors are returned as status codes with a message; no
+// call aborts the process.
+
+#include <cuda_runtime.h>
+
+#include <atomic>
+#include <chrono>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <new>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "../../include/mlbm/mlbm.h"
+#include "kernels.h"
+#include "mlp_device.cuh"
+#include "mlp_train.h"
+
+using namespace mlbm;
+
+namespace {
+
+std::atomic<unsigned long long> g_launches{0};
+std::mutex g_create_error_mutex;
+std::string g_create_error;
+
+const int kQ[3] = {9, 19, 27};
+const int kD[3] = {2, 3, 3};
+const double kPi = 3.14159265358979323846;
+
+}  // namespace
+
+namespace mlbm {
+void count_launches(unsigned n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+}  // namespace mlbm
+
+struct mlbm_handle {
+  mlbm_config cfg{};
+  int Q = 0, D = 0;
+  long long V = 0;
+  uint32_t lx = 0, ly = 0, lz = 0;
+  int storage = 0;
+  size_t elem = 8;  // bytes per stored population value
+  void* f[2] = {nullptr, nullptr};
+  int cur = 0;      // f[cur] holds the current populations
+  double* rho = nullptr;
+  double* u = nullptr;
+  double* force = nullptr;
+  double* alpha = nullptr;      // FP64 storage
+  float* alpha32 = nullptr;     // low-precision storage
+  double* force_table[3] = {nullptr, nullptr, nullptr};
+  double* partials = nullptr;
+  int partial_blocks = 0;
+  double* diag_dev = nullptr;
+  unsigned long long* counters = nullptr;
+  unsigned* err_word = nullptr;
+  double* staging = nullptr;    // V doubles
+  MlpDev* mlp = nullptr;
+  bool have_model = false;
+  long long* sample_nodes = nullptr;
+  long long n_samples = 0;
+  double* sample_feat = nullptr;
+  double* sample_alpha = nullptr;
+  int* sample_solved = nullptr;
+  cudaStream_t own_stream = nullptr;
+  cudaStream_t stream = nullptr;
+  long long steps = 0;
+  bool diag_valid = false;
+  bool fields_valid = false;
+  StepParams base{};
+  std::string error;
+};
+
+static int fail(mlbm_handle* h, int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  std::vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  if (h) {
+    h->error = buf;
+  } else {
+    std::lock_guard<std::mutex> lk(g_create_error_mutex);
+    g_create_error = buf;
+  }
+  return code;
+}
+
+#define MLBM_CUDA(h, call)                                                              \
+  do {                                                                                  \
+    cudaError_t e_ = (call);                                                            \
+    if (e_ != cudaSuccess)                                                              \
+      return fail((h), MLBM_ERR_CUDA, "%s failed: %s", #call, cudaGetErrorString(e_));  \
+  } while (0)
+
+static int device_alloc(mlbm_handle* h, void** p, size_t bytes) {
+  if (bytes == 0) { *p = nullptr; return MLBM_OK; }
+  cudaError_t e = cudaMalloc(p, bytes);
+  if (e != cudaSuccess) {
+    *p = nullptr;
+    cudaGetLastError();
+    return fail(h, MLBM_ERR_ALLOC, "cudaMalloc of %zu bytes failed: %s", bytes,
+                cudaGetErrorString(e));
+  }
+  return MLBM_OK;
+}
+
+// ---- layouts -----------------------------------------------------------------
+// Reference layout (lSD, Domain.h:42-92 + FFTW padding): the last active
+// dimension padded to 2*(N/2+1); component stride = padded volume.
+struct RefLayout {
+  long long px, py, pz;  // padded extents
+  long long volume;
+};
+static RefLayout ref_layout(const mlbm_handle* h) {
+  RefLayout r;
+  r.px = h->lx;
+  if (h->D == 2) {
+    r.py = 2 * (h->ly / 2 + 1);
+    r.pz = 1;
+  } else {
+    r.py = h->ly;
+    r.pz = 2 * (h->lz / 2 + 1);
+  }
+  r.volume = r.px * r.py * r.pz;
+  return r;
+}
+
+// Copy ncomp components between dense [c][V] and reference [c][padded].
+static void dense_from_ref(const mlbm_handle* h, const double* ref, double* dense, int ncomp) {
+  const RefLayout r = ref_layout(h);
+  for (int c = 0; c < ncomp; ++c)
+    for (uint32_t x = 0; x < h->lx; ++x)
+      for (uint32_t y = 0; y < h->ly; ++y)
+        for (uint32_t z = 0; z < h->lz; ++z)
+          dense[(long long)c * h->V + ((long long)x * h->ly + y) * h->lz + z] =
+              ref[(long long)c * r.volume + (x * r.py + y) * r.pz + z];
+}
+static void ref_from_dense(const mlbm_handle* h, const double* dense, double* ref, int ncomp) {
+  const RefLayout r = ref_layout(h);
+  for (int c = 0; c < ncomp; ++c)
+    for (uint32_t x = 0; x < h->lx; ++x)
+      for (uint32_t y = 0; y < h->ly; ++y)
+        for (uint32_t z = 0; z < h->lz; ++z)
+          ref[(long long)c * r.volume + (x * r.py + y) * r.pz + z] =
+              dense[(long long)c * h->V + ((long long)x * h->ly + y) * h->lz + z];
+}
+
+// Upload ncomp host components (given layout) into device dense memory.
+static int upload(mlbm_handle* h, const double* host, double* dev, int ncomp, int layout) {
+  const size_t bytes = sizeof(double) * (size_t)h->V * ncomp;
+  if (layout == MLBM_LAYOUT_DENSE) {
+    MLBM_CUDA(h, cudaMemcpyAsync(dev, host, bytes, cudaMemcpyHostToDevice, h->stream));
+    MLBM_CUDA(h, cudaStreamSynchronize(h->stream));
+    return MLBM_OK;
+  }
+  std::vector<double> tmp;
+  try { tmp.resize((size_t)h->V * ncomp); } catch (...) {
+    return fail(h, MLBM_ERR_ALLOC, "host staging of %zu bytes failed", bytes);
+  }
+  dense_from_ref(h, host, tmp.data(), ncomp);
+  MLBM_CUDA(h, cudaMemcpyAsync(dev, tmp.data(), bytes, cudaMemcpyHostToDevice, h->stream));
+  MLBM_CUDA(h, cudaStreamSynchronize(h->stream));
+  return MLBM_OK;
+}
+
+static int download(mlbm_handle* h, const double* dev, double* host, int ncomp, int layout) {
+  const size_t bytes = sizeof(double) * (size_t)h->V * ncomp;
+  if (layout == MLBM_LAYOUT_DENSE) {
+    MLBM_CUDA(h, cudaMemcpyAsync(host, dev, bytes, cudaMemcpyDeviceToHost, h->stream));
+    MLBM_CUDA(h, cudaStreamSynchronize(h->stream));
+    return MLBM_OK;
+  }
+  std::vector<double> tmp;
+  try { tmp.resize((size_t)h->V * ncomp); } catch (...) {
+    return fail(h, MLBM_ERR_ALLOC, "host staging of %zu bytes failed", bytes);
+  }
+  MLBM_CUDA(h, cudaMemcpyAsync(tmp.data(), dev, bytes, cudaMemcpyDeviceToHost, h->stream));
+  MLBM_CUDA(h, cudaStreamSynchronize(h->stream));
+  ref_from_dense(h, tmp.data(), host, ncomp);
+  return MLBM_OK;
+}
+
+static bool valid_layout(int layout) {
+  return layout == MLBM_LAYOUT_DENSE || layout == MLBM_LAYOUT_REFERENCE;
+}
+
+// ---- API -----------------------------------------------------------------------
+extern "C" int mlbm_config_init(mlbm_config* c) {
+  if (!c) return MLBM_ERR_INVALID;
+  std::memset(c, 0, sizeof *c);
+  c->lattice = MLBM_D2Q9;
+  c->collision = MLBM_BGK;
+  c->forcing_scheme = MLBM_FORCING_NONE;
+  c->force = MLBM_FORCE_NONE;
+  c->relaxation_time = 0.7;
+  for (int d = 0; d < 3; ++d) c->force_wavelength[d] = 32.0;
+  c->kolmogorov_axis = 1;
+  c->kolmogorov_component = 0;
+  c->length[0] = c->length[1] = c->length[2] = 16;
+  c->storage = MLBM_STORAGE_F64;
+  c->alpha_mode = MLBM_ALPHA_REFERENCE;
+  c->alpha_guess = MLBM_GUESS_PREVIOUS;
+  c->newton_tolerance = 1e-8;
+  c->newton_max_iterations = 50;
+  c->deviation_threshold = 1e-3;
+  c->device = 0;
+  return MLBM_OK;
+}
+
+static void release(mlbm_handle* h) {
+  if (!h) return;
+  void* ptrs[] = {h->f[0], h->f[1], h->rho, h->u, h->force, h->alpha, h->alpha32,
+                  h->force_table[0], h->force_table[1], h->force_table[2], h->partials,
+                  h->diag_dev, h->counters, h->err_word, h->staging, h->mlp, h->sample_nodes,
+                  h->sample_feat, h->sample_alpha, h->sample_solved};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+  if (h->own_stream) cudaStreamDestroy(h->own_stream);
+  delete h;
+}
+
+static double host_sin_profile(double amplitude, unsigned i, double lambda) {
+  // Force.h:213, 266: amplitude * sin(iP * 2 * M_PI / waveLength), with the
+  // unsigned coordinate times 2 formed in integer arithmetic.
+  return amplitude * std::sin((double)(i * 2u) * kPi / lambda);
+}
+
+extern "C" int mlbm_create(const mlbm_config* cfg, mlbm_handle** out) {
+  if (!cfg || !out) return fail(nullptr, MLBM_ERR_INVALID, "null argument");
+  *out = nullptr;
+  const mlbm_config& c = *cfg;
+  if (c.lattice < 0 || c.lattice > 2) return fail(nullptr, MLBM_ERR_INVALID, "bad lattice %d", c.lattice);
+  if (c.collision < 0 || c.collision > 2)
+    return fail(nullptr, MLBM_ERR_INVALID, "bad collision %d", c.collision);
+  if (c.forcing_scheme < 0 || c.forcing_scheme > 3)
+    return fail(nullptr, MLBM_ERR_INVALID, "bad forcing scheme %d", c.forcing_scheme);
+  if (c.force < 0 || c.force > 3) return fail(nullptr, MLBM_ERR_INVALID, "bad force %d", c.force);
+  if (c.storage < 0 || c.storage > 2) return fail(nullptr, MLBM_ERR_INVALID, "bad storage %d", c.storage);
+  if (!(c.relaxation_time > 0.5) || !std::isfinite(c.relaxation_time))
+    return fail(nullptr, MLBM_ERR_INVALID, "relaxation time must be > 0.5 (got %g)", c.relaxation_time);
+  if (c.alpha_mode < 0 || c.alpha_mode > 1) return fail(nullptr, MLBM_ERR_INVALID, "bad alpha mode");
+  if (c.alpha_guess < 0 || c.alpha_guess > 2) return fail(nullptr, MLBM_ERR_INVALID, "bad alpha guess");
+  if (c.alpha_guess == MLBM_GUESS_LEARNED && c.storage == MLBM_STORAGE_F64)
+    return fail(nullptr, MLBM_ERR_INVALID, "the learned alpha guess runs with FP32/FP16 storage");
+  if (c.newton_max_iterations < 0 || !(c.newton_tolerance >= 0))
+    return fail(nullptr, MLBM_ERR_INVALID, "bad Newton parameters");
+  const int D = kD[c.lattice];
+  long long L[3] = {c.length[0], c.length[1], D == 2 ? 1 : c.length[2]};
+  for (int d = 0; d < 3; ++d)
+    if (L[d] < 1 || L[d] > 65536) return fail(nullptr, MLBM_ERR_INVALID, "bad length[%d] = %lld", d, L[d]);
+  const long long V = L[0] * L[1] * L[2];
+  if (V >= (1ll << 31)) return fail(nullptr, MLBM_ERR_INVALID, "lattice too large (%lld nodes)", V);
+  if (c.force == MLBM_FORCE_KOLMOGOROV &&
+      (c.kolmogorov_axis < 0 || c.kolmogorov_axis >= D || c.kolmogorov_component < 0 ||
+       c.kolmogorov_component >= D))
+    return fail(nullptr, MLBM_ERR_INVALID, "bad Kolmogorov axis/component");
+  if (c.force == MLBM_FORCE_SINUSOIDAL || c.force == MLBM_FORCE_KOLMOGOROV)
+    for (int d = 0; d < D; ++d)
+      if (c.force_wavelength[d] == 0.0) return fail(nullptr, MLBM_ERR_INVALID, "zero force wavelength");
+
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+    cudaGetLastError();
+    return fail(nullptr, MLBM_ERR_NO_DEVICE, "no CUDA device available");
+  }
+  if (c.device < 0 || c.device >= ndev) return fail(nullptr, MLBM_ERR_INVALID, "bad device %d", c.device);
+
+  mlbm_handle* h = new (std::nothrow) mlbm_handle();
+  if (!h) return fail(nullptr, MLBM_ERR_ALLOC, "host allocation failed");
+  h->cfg = c;
+  if (h->cfg.collision == MLBM_FORCED_BNR_ELBM) h->cfg.collision = MLBM_ELBM;
+  h->Q = kQ[c.lattice];
+  h->D = D;
+  h->lx = (uint32_t)L[0];
+  h->ly = (uint32_t)L[1];
+  h->lz = (uint32_t)L[2];
+  h->V = V;
+  h->storage = c.storage;
+  h->elem = c.storage == MLBM_STORAGE_F64 ? 8 : (c.storage == MLBM_STORAGE_F32 ? 4 : 2);
+
+  auto bail = [&](int code) {
+    std::string msg = h->error;
+    release(h);
+    return fail(nullptr, code, "%s", msg.c_str());
+  };
+  if (cudaSetDevice(c.device) != cudaSuccess) {
+    cudaGetLastError();
+    h->error = "cudaSetDevice failed";
+    return bail(MLBM_ERR_CUDA);
+  }
+  if (cudaStreamCreateWithFlags(&h->own_stream, cudaStreamNonBlocking) != cudaSuccess) {
+    h->error = "cudaStreamCreate failed";
+    return bail(MLBM_ERR_CUDA);
+  }
+  h->stream = h->own_stream;
+
+  const size_t popBytes = h->elem * (size_t)h->Q * (size_t)V;
+  int rc;
+  if ((rc = device_alloc(h, &h->f[0], popBytes)) || (rc = device_alloc(h, &h->f[1], popBytes)) ||
+      (rc = device_alloc(h, (void**)&h->rho, sizeof(double) * V)) ||
+      (rc = device_alloc(h, (void**)&h->u, sizeof(double) * V * D)) ||
+      (rc = device_alloc(h, (void**)&h->force, sizeof(double) * V * D)) ||
+      (rc = device_alloc(h, (void**)&h->staging, sizeof(double) * V)))
+    return bail(rc);
+  if (c.storage == MLBM_STORAGE_F64) {
+    if ((rc = device_alloc(h, (void**)&h->alpha, sizeof(double) * V))) return bail(rc);
+  } else {
+    if ((rc = device_alloc(h, (void**)&h->alpha32, sizeof(float) * V))) return bail(rc);
+  }
+  const int bs = 128;  // smallest block size of the step kernels
+  h->partial_blocks = (int)((V + bs - 1) / bs);
+  if ((rc = device_alloc(h, (void**)&h->partials, sizeof(double) * DIAG_FIELDS * h->partial_blocks)) ||
+      (rc = device_alloc(h, (void**)&h->diag_dev, sizeof(double) * DIAG_FIELDS)) ||
+      (rc = device_alloc(h, (void**)&h->counters, sizeof(unsigned long long) * CNT_COUNT)) ||
+      (rc = device_alloc(h, (void**)&h->err_word, sizeof(unsigned))) ||
+      (rc = device_alloc(h, (void**)&h->mlp, sizeof(MlpDev))))
+    return bail(rc);
+  cudaMemsetAsync(h->f[0], 0, popBytes, h->stream);
+  cudaMemsetAsync(h->f[1], 0, popBytes, h->stream);
+  cudaMemsetAsync(h->rho, 0, sizeof(double) * V, h->stream);
+  cudaMemsetAsync(h->u, 0, sizeof(double) * V * D, h->stream);
+  cudaMemsetAsync(h->force, 0, sizeof(double) * V * D, h->stream);
+  cudaMemsetAsync(h->counters, 0, sizeof(unsigned long long) * CNT_COUNT, h->stream);
+  cudaMemsetAsync(h->err_word, 0, sizeof(unsigned), h->stream);
+  cudaMemsetAsync(h->mlp, 0, sizeof(MlpDev), h->stream);
+
+  // Force profiles tabulated on the host (Force.h:208-215, 262-267).
+  if (c.force == MLBM_FORCE_SINUSOIDAL || c.force == MLBM_FORCE_KOLMOGOROV) {
+    const int ntab = c.force == MLBM_FORCE_SINUSOIDAL ? D : 1;
+    for (int t = 0; t < ntab; ++t) {
+      const int axis = c.force == MLBM_FORCE_SINUSOIDAL ? t : c.kolmogorov_axis;
+      const int comp = c.force == MLBM_FORCE_SINUSOIDAL ? t : c.kolmogorov_component;
+      const long long n = L[axis];
+      std::vector<double> tab(n);
+      for (long long i = 0; i < n; ++i)
+        tab[i] = host_sin_profile(c.force_amplitude[comp], (unsigned)i, c.force_wavelength[comp]);
+      if ((rc = device_alloc(h, (void**)&h->force_table[t], sizeof(double) * n))) return bail(rc);
+      if (cudaMemcpy(h->force_table[t], tab.data(), sizeof(double) * n, cudaMemcpyHostToDevice) !=
+          cudaSuccess) {
+        h->error = "force table upload failed";
+        return bail(MLBM_ERR_CUDA);
+      }
+    }
+  }
+
+  StepParams& p = h->base;
+  p.V = V;
+  p.lx = h->lx; p.ly = h->ly; p.lz = h->lz;
+  p.div_lz.init(h->lz);
+  p.div_ly.init(h->ly);
+  p.tau = c.relaxation_time;
+  p.beta = (double)1.0 / (2.0 * c.relaxation_time);     // Collision.h:122
+  p.bgk_a = 1. - 2. * p.beta;                            // Collision.h:145
+  p.bgk_b = 2. * p.beta;                                 // Collision.h:147
+  {
+    double w[27];
+    const double* wl = nullptr;
+    static const double w9[9] = {4.0 / 9.0, 1.0 / 36.0, 1.0 / 9.0, 1.0 / 36.0, 1.0 / 36.0,
+                                 1.0 / 9.0, 1.0 / 36.0, 1.0 / 9.0, 1.0 / 9.0};
+    static const double w19[19] = {1.0 / 3.0,  1.0 / 18.0, 1.0 / 36.0, 1.0 / 36.0, 1.0 / 36.0,
+                                   1.0 / 36.0, 1.0 / 18.0, 1.0 / 36.0, 1.0 / 36.0, 1.0 / 36.0,
+                                   1.0 / 36.0, 1.0 / 18.0, 1.0 / 18.0, 1.0 / 36.0, 1.0 / 36.0,
+                                   1.0 / 18.0, 1.0 / 18.0, 1.0 / 36.0, 1.0 / 36.0};
+    for (int q = 0; q < 27; ++q) {
+      const int cls = (q == 0) ? 0 : ((q == 1 || q == 10 || q == 19 || q == 20 || q == 23 || q == 24) ? 1
+                        : ((q >= 6 && q <= 9) || (q >= 15 && q <= 18)) ? 3 : 2);
+      const double v[4] = {8.0 / 27.0, 2.0 / 27.0, 1.0 / 54.0, 1.0 / 216.0};
+      w[q] = v[cls];
+    }
+    wl = c.lattice == MLBM_D2Q9 ? w9 : (c.lattice == MLBM_D3Q19 ? w19 : w);
+    for (int q = 0; q < h->Q; ++q)  // ForcingScheme.h:115-116
+      p.guo_k[q] = (1.0 - 1.0 / (2.0 * c.relaxation_time)) * wl[q] * 3.0;
+  }
+  p.force_type = c.force;
+  p.kol_axis = c.kolmogorov_axis;
+  p.kol_comp = c.kolmogorov_component;
+  for (int d = 0; d < 3; ++d) p.amp[d] = d < D ? c.force_amplitude[d] : 0.0;
+  for (int t = 0; t < 3; ++t) p.force_table[t] = h->force_table[t];
+  p.alpha_mode = c.alpha_mode;
+  p.guess_mode = c.alpha_guess;
+  p.newton_tol = c.newton_tolerance;
+  p.newton_maxit = c.newton_max_iterations;
+  p.deviation_threshold = c.deviation_threshold;
+  p.rho_out = h->rho;
+  p.u_out = h->u;
+  p.force_out = h->force;
+  p.alpha_field = h->alpha;
+  p.alpha_field_f32 = h->alpha32;
+  p.diag_partials = h->partials;
+  p.counters = h->counters;
+  p.err_word = h->err_word;
+  p.mlp = h->mlp;
+
+  if (cudaStreamSynchronize(h->stream) != cudaSuccess) {
+    h->error = std::string("device initialisation failed: ") + cudaGetErrorString(cudaGetLastError());
+    return bail(MLBM_ERR_CUDA);
+  }
+  *out = h;
+  return MLBM_OK;
+}
+
+extern "C" int mlbm_destroy(mlbm_handle* h) {
+  if (!h) return MLBM_ERR_INVALID;
+  cudaSetDevice(h->cfg.device);
+  cudaStreamSynchronize(h->stream);
+  release(h);
+  return MLBM_OK;
+}
+
+static int fill_alpha(mlbm_handle* h, double value) {
+  std::vector<double> a64;
+  std::vector<float> a32;
+  if (h->alpha) {
+    a64.assign((size_t)h->V, value);
+    MLBM_CUDA(h, cudaMemcpy(h->alpha, a64.data(), sizeof(double) * h->V, cudaMemcpyHostToDevice));
+  } else {
+    a32.assign((size_t)h->V, (float)value);
+    MLBM_CUDA(h, cudaMemcpy(h->alpha32, a32.data(), sizeof(float) * h->V, cudaMemcpyHostToDevice));
+  }
+  return MLBM_OK;
+}
+
+extern "C" int mlbm_init_equilibrium(mlbm_handle* h, const double* rho, const double* u, int layout) {
+  if (!h) return MLBM_ERR_INVALID;
+  if (!rho || !u || !valid_layout(layout)) return fail(h, MLBM_ERR_INVALID, "bad arguments");
+  MLBM_CUDA(h, cudaSetDevice(h->cfg.device));
+  int rc;
+  // rho and u go through the field buffers (overwritten by the next store).
+  if ((rc = upload(h, rho, h->rho, 1, layout))) return rc;
+  if ((rc = upload(h, u, h->u, h->D, layout))) return rc;
+  cudaError_t e = h->storage == MLBM_STORAGE_F64
+                      ? init_f64(h->cfg.lattice, h->rho, h->u, (double*)h->f[h->cur], h->V, h->stream)
+                      : init_lowp(h->cfg.lattice, h->storage, h->rho, h->u, h->f[h->cur], h->V, h->stream);
+  count_launches(1);
+  if (e != cudaSuccess) return fail(h, MLBM_ERR_CUDA, "init kernel: %s", cudaGetErrorString(e));
+  if ((rc = fill_alpha(h, 2.0))) return rc;  // Initialize.h:82-89
+  MLBM_CUDA(h, cudaStreamSynchronize(h->stream));
+  h->fields_valid = false;
+  return MLBM_OK;
+}
+
+extern "C" int mlbm_set_populations(mlbm_handle* h, const double* f, int layout) {
+  if (!h) return MLBM_ERR_INVALID;
+  if (!f || !valid_layout(layout)) return fail(h, MLBM_ERR_INVALID, "bad arguments");
+  MLBM_CUDA(h, cudaSetDevice(h->cfg.device));
+  const RefLayout r = ref_layout(h);
+  const long long stride = layout == MLBM_LAYOUT_DENSE ? h->V : r.volume;
+  int rc;
+  for (int q = 0; q < h->Q; ++q) {
+    double* dst = h->storage == MLBM_STORAGE_F64 ? (double*)h->f[h->cur] + (long long)q * h->V
+                                                 : h->staging;
+    if ((rc = upload(h, f + (long long)q * stride, dst, 1, layout))) return rc;
+    if (h->storage != MLBM_STORAGE_F64) {
+      cudaError_t e = f64_to_lowp(h->cfg.lattice, h->storage, h->staging, q, h->f[h->cur], h->V,
+                                  h->stream);
+      count_launches(1);
+      if (e != cudaSuccess) return fail(h, MLBM_ERR_CUDA, "encode: %s", cudaGetErrorString(e));
+      MLBM_CUDA(h, cudaStreamSynchronize(h->stream));
+    }
+  }
+  h->fields_valid = false;
+  return MLBM_OK;
+}
+
+extern "C" int mlbm_get_populations(mlbm_handle* h, double* f, int layout) {
+  if (!h) return MLBM_ERR_INVALID;
+  if (!f || !valid_layout(layout)) return fail(h, MLBM_ERR_INVALID, "bad arguments");
+  MLBM_CUDA(h, cudaSetDevice(h->cfg.device));
+  const RefLayout r = ref_layout(h);
+  const long long stride = layout == MLBM_LAYOUT_DENSE ? h->V : r.volume;
+  int rc;
+  for (int q = 0; q < h->Q; ++q) {
+    const double* src = (const double*)h->f[h->cur] + (long long)q * h->V;
+    if (h->storage != MLBM_STORAGE_F64) {
+      cudaError_t e = lowp_to_f64(h->cfg.lattice, h->storage, h->f[h->cur], q, h->staging, h->V,
+                                  h->stream);
+      count_launches(1);
+      if (e != cudaSuccess) return fail(h, MLBM_ERR_CUDA, "decode: %s", cudaGetErrorString(e));
+      src = h->staging;
+    }
+    if ((rc = download(h, src, f + (long long)q * stride, 1, layout))) return rc;
+  }
+  return MLBM_OK;
+}
+
+extern "C" int mlbm_step(mlbm_handle* h, int nsteps, unsigned int flags) {
+  if (!h) return MLBM_ERR_INVALID;
+  if (nsteps < 0) return fail(h, MLBM_ERR_INVALID, "negative step count");
+  if (nsteps == 0) return MLBM_OK;
+  if ((flags & MLBM_STEP_LOG_SAMPLES) && h->n_samples == 0)
+    return fail(h, MLBM_ERR_STATE, "LOG_SAMPLES without sample nodes (mlbm_set_sample_nodes)");
+  if (h->cfg.alpha_guess == MLBM_GUESS_LEARNED && h->cfg.collision != MLBM_BGK && !h->have_model)
+    return fail(h, MLBM_ERR_STATE, "learned alpha guess without a model (mlbm_set_alpha_model)");
+  MLBM_CUDA(h, cudaSetDevice(h->cfg.device));
+  MLBM_CUDA(h, cudaMemsetAsync(h->counters, 0, sizeof(unsigned long long) * CNT_COUNT, h->stream));
+  const int collision = h->cfg.collision == MLBM_BGK ? 0 : 1;
+  for (int s = 0; s < nsteps; ++s) {
+    const bool last = s == nsteps - 1;
+    StepParams p = h->base;
+    p.store = last && (flags & MLBM_STEP_STORE_FIELDS) ? 1 : 0;
+    p.diag = last && (flags & MLBM_STEP_DIAGNOSTICS) ? 1 : 0;
+    const void* prev = h->f[h->cur];
+    void* next = h->f[1 - h->cur];
+    cudaError_t e = h->storage == MLBM_STORAGE_F64
+                        ? step_f64(h->cfg.lattice, collision, h->cfg.forcing_scheme,
+                                   (const double*)prev, (double*)next, p, h->stream)
+                        : step_lowp(h->cfg.lattice, collision, h->cfg.forcing_scheme, h->storage,
+                                    prev, next, p, h->stream);
+    count_launches(1);
+    if (e != cudaSuccess) return fail(h, MLBM_ERR_CUDA, "step kernel: %s", cudaGetErrorString(e));
+    if (p.diag) {
+      const int bs = (h->storage == MLBM_STORAGE_F64 ? (collision ? 128 : 256) : (collision ? 128 : 256));
+      const int nb = (int)((h->V + bs - 1) / bs);
+      e = finalize_diag(h->partials, nb, h->diag_dev, h->stream);
+      count_launches(1);
+      if (e != cudaSuccess) return fail(h, MLBM_ERR_CUDA, "diagnostics: %s", cudaGetErrorString(e));
+    }
+    if (last && (flags & MLBM_STEP_LOG_SAMPLES)) {
+      e = log_samples(h->cfg.lattice, h->storage, prev, p, h->sample_nodes, h->n_samples,
+                      h->sample_feat, h->sample_alpha, h->sample_solved, h->stream);
+      count_launches(1);
+      if (e != cudaSuccess) return fail(h, MLBM_ERR_CUDA, "samples: %s", cudaGetErrorString(e));
+    }
+    h->cur = 1 - h->cur;  // std::swap(prev, next), Algorithm.h:336
+    ++h->steps;
+    if (p.store) h->fields_valid = true;
+    if (p.diag) h->diag_valid = true;
+  }
+  return MLBM_OK;
+}
+
+extern "C" int mlbm_sync(mlbm_handle* h, int timeout_ms) {
+  if (!h) return MLBM_ERR_INVALID;
+  MLBM_CUDA(h, cudaSetDevice(h->cfg.device));
+  const auto t0 = std::chrono::steady_clock::now();
+  for (;;) {
+    cudaError_t e = cudaStreamQuery(h->stream);
+    if (e == cudaSuccess) break;
+    if (e != cudaErrorNotReady) return fail(h, MLBM_ERR_CUDA, "stream error: %s", cudaGetErrorString(e));
+    if (timeout_ms >= 0) {
+      const auto ms = std::chrono::duration_cast<std::chrono::milliseconds>(
+                          std::chrono::steady_clock::now() - t0).count();
+      if (ms >= timeout_ms) return fail(h, MLBM_ERR_TIMEOUT, "device work not finished after %d ms", timeout_ms);
+    }
+    std::this_thread::sleep_for(std::chrono::microseconds(50));
+  }
+  unsigned err = 0;
+  MLBM_CUDA(h, cudaMemcpy(&err, h->err_word, sizeof err, cudaMemcpyDeviceToHost));
+  if (err) return fail(h, MLBM_ERR_NUMERIC, "device error word 0x%x (non-finite or non-positive density)", err);
+  return MLBM_OK;
+}
+
+extern "C" int mlbm_get_fields(mlbm_handle* h, double* rho, double* u, double* alpha, double* force,
+                               int layout) {
+  if (!h) return MLBM_ERR_INVALID;
+  if (!valid_layout(layout)) return fail(h, MLBM_ERR_INVALID, "bad layout");
+  if (!h->fields_valid) return fail(h, MLBM_ERR_STATE, "no stored fields (use MLBM_STEP_STORE_FIELDS)");
+  MLBM_CUDA(h, cudaSetDevice(h->cfg.device));
+  int rc;
+  if (rho && (rc = download(h, h->rho, rho, 1, layout))) return rc;
+  if (u && (rc = download(h, h->u, u, h->D, layout))) return rc;
+  if (force && (rc = download(h, h->force, force, h->D, layout))) return rc;
+  if (alpha) {
+    if (h->alpha) {
+      if ((rc = download(h, h->alpha, alpha, 1, layout))) return rc;
+    } else {
+      std::vector<float> a((size_t)h->V);
+      std::vector<double> ad((size_t)h->V);
+      MLBM_CUDA(h, cudaMemcpy(a.data(), h->alpha32, sizeof(float) * h->V, cudaMemcpyDeviceToHost));
+      for (long long i = 0; i < h->V; ++i) ad[i] = a[i];
+      if (layout == MLBM_LAYOUT_DENSE) std::memcpy(alpha, ad.data(), sizeof(double) * h->V);
+      else ref_from_dense(h, ad.data(), alpha, 1);
+    }
+  }
+  return MLBM_OK;
+}
+
+extern "C" int mlbm_get_diagnostics(mlbm_handle* h, mlbm_diag* out) {
+  if (!h || !out) return MLBM_ERR_INVALID;
+  MLBM_CUDA(h, cudaSetDevice(h->cfg.device));
+  MLBM_CUDA(h, cudaStreamSynchronize(h->stream));
+  std::memset(out, 0, sizeof *out);
+  out->step = h->steps;
+  double d[DIAG_FIELDS] = {0, 0, 0, 0, 0};
+  if (h->diag_valid) MLBM_CUDA(h, cudaMemcpy(d, h->diag_dev, sizeof d, cudaMemcpyDeviceToHost));
+  unsigned long long c[CNT_COUNT];
+  MLBM_CUDA(h, cudaMemcpy(c, h->counters, sizeof c, cudaMemcpyDeviceToHost));
+  unsigned err = 0;
+  MLBM_CUDA(h, cudaMemcpy(&err, h->err_word, sizeof err, cudaMemcpyDeviceToHost));
+  out->mass = d[0];
+  out->energy = d[1] / (double)h->V;  // AnalysisScalar::normalize, Analysis.h:29
+  out->max_mach = d[2];
+  out->alpha_min = d[3];
+  out->alpha_max = d[4];
+  out->solved_nodes = (long long)c[CNT_SOLVED];
+  out->newton_iterations = (long long)c[CNT_ITER];
+  out->guess_hits = (long long)c[CNT_HITS];
+  out->bisection_nodes = (long long)c[CNT_BISECT];
+  out->fallback_nodes = (long long)c[CNT_FALLBACK];
+  out->limited_nodes = (long long)c[CNT_LIMITED];
+  out->shortcut_nodes = (long long)c[CNT_SHORTCUT];
+  out->error_word = err;
+  return MLBM_OK;
+}
+
+extern "C" int mlbm_get_stream(mlbm_handle* h, void** stream) {
+  if (!h || !stream) return MLBM_ERR_INVALID;
+  *stream = (void*)h->stream;
+  return MLBM_OK;
+}
+
+extern "C" int mlbm_set_stream(mlbm_handle* h, void* stream) {
+  if (!h) return MLBM_ERR_INVALID;
+  MLBM_CUDA(h, cudaStreamSynchronize(h->stream));
+  h->stream = stream ? (cudaStream_t)stream : h->own_stream;
+  return MLBM_OK;
+}
+
+extern "C" int mlbm_set_sample_nodes(mlbm_handle* h, const long long* nodes, long long n) {
+  if (!h) return MLBM_ERR_INVALID;
+  if (n < 0 || (n > 0 && !nodes)) return fail(h, MLBM_ERR_INVALID, "bad sample list");
+  for (long long i = 0; i < n; ++i)
+    if (nodes[i] < 0 || nodes[i] >= h->V) return fail(h, MLBM_ERR_INVALID, "sample node %lld out of range", nodes[i]);
+  MLBM_CUDA(h, cudaSetDevice(h->cfg.device));
+  MLBM_CUDA(h, cudaStreamSynchronize(h->stream));
+  void* ptrs[] = {h->sample_nodes, h->sample_feat, h->sample_alpha, h->sample_solved};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+  h->sample_nodes = nullptr; h->sample_feat = nullptr; h->sample_alpha = nullptr; h->sample_solved = nullptr;
+  h->n_samples = 0;
+  if (n == 0) return MLBM_OK;
+  int rc;
+  if ((rc = device_alloc(h, (void**)&h->sample_nodes, sizeof(long long) * n)) ||
+      (rc = device_alloc(h, (void**)&h->sample_feat, sizeof(double) * n * h->Q)) ||
+      (rc = device_alloc(h, (void**)&h->sample_alpha, sizeof(double) * n)) ||
+      (rc = device_alloc(h, (void**)&h->sample_solved, sizeof(int) * n)))
+    return rc;
+  MLBM_CUDA(h, cudaMemcpy(h->sample_nodes, nodes, sizeof(long long) * n, cudaMemcpyHostToDevice));
+  h->n_samples = n;
+  return MLBM_OK;
+}
+
+extern "C" int mlbm_get_samples(mlbm_handle* h, double* features, double* alpha, int* solved) {
+  if (!h) return MLBM_ERR_INVALID;
+  if (h->n_samples == 0) return fail(h, MLBM_ERR_STATE, "no sample nodes");
+  MLBM_CUDA(h, cudaSetDevice(h->cfg.device));
+  MLBM_CUDA(h, cudaStreamSynchronize(h->stream));
+  if (features)
+    MLBM_CUDA(h, cudaMemcpy(features, h->sample_feat, sizeof(double) * h->n_samples * h->Q, cudaMemcpyDeviceToHost));
+  if (alpha)
+    MLBM_CUDA(h, cudaMemcpy(alpha, h->sample_alpha, sizeof(double) * h->n_samples, cudaMemcpyDeviceToHost));
+  if (solved)
+    MLBM_CUDA(h, cudaMemcpy(solved, h->sample_solved, sizeof(int) * h->n_samples, cudaMemcpyDeviceToHost));
+  return MLBM_OK;
+}
+
+// Host model -> device inference layout (BF16 weights, zero-padded inputs).
+static int upload_model(mlbm_handle* h, const mlbm_mlp* m, MlpDev* dst) {
+  if (m->n_in != h->Q || m->n_hidden != MLBM_MLP_HIDDEN)
+    return fail(h, MLBM_ERR_INVALID, "model shape %d->%d does not match Q=%d, hidden=%d", m->n_in,
+                m->n_hidden, h->Q, MLBM_MLP_HIDDEN);
+  MlpDev d;
+  std::memset(&d, 0, sizeof d);
+  for (int j = 0; j < MLP_H; ++j) {
+    for (int i = 0; i < 32; ++i)
+      d.w1[j * 32 + i] = __float2bfloat16(i < m->n_in ? m->w1[j * m->n_in + i] : 0.0f);
+    for (int i = 0; i < MLP_H; ++i) d.w2[j * MLP_H + i] = __float2bfloat16(m->w2[j * MLP_H + i]);
+    d.b1[j] = m->b1[j];
+    d.b2[j] = m->b2[j];
+    d.w3[j] = m->w3[j];
+  }
+  for (int i = 0; i < 32; ++i) d.in_scale[i] = i < m->n_in ? m->input_scale[i] : 0.0f;
+  d.b3 = m->b3;
+  d.out_scale = m->output_scale;
+  d.n_in = m->n_in;
+  MLBM_CUDA(h, cudaMemcpy(dst, &d, sizeof d, cudaMemcpyHostToDevice));
+  return MLBM_OK;
+}
+
+extern "C" int mlbm_set_alpha_model(mlbm_handle* h, const mlbm_mlp* m) {
+  if (!h || !m) return MLBM_ERR_INVALID;
+  MLBM_CUDA(h, cudaSetDevice(h->cfg.device));
+  MLBM_CUDA(h, cudaStreamSynchronize(h->stream));
+  int rc = upload_model(h, m, h->mlp);
+  if (rc) return rc;
+  h->have_model = true;
+  return MLBM_OK;
+}
+
+extern "C" int mlbm_alpha_model_predict(mlbm_handle* h, const mlbm_mlp* m, const float* X, long long n,
+                                        float* alpha) {
+  if (!h || !m || !X || !alpha || n <= 0) return MLBM_ERR_INVALID;
+  MLBM_CUDA(h, cudaSetDevice(h->cfg.device));
+  MlpDev* dm = nullptr;
+  float *dX = nullptr, *dA = nullptr;
+  int rc;
+  if ((rc = device_alloc(h, (void**)&dm, sizeof(MlpDev)))) return rc;
+  if ((rc = device_alloc(h, (void**)&dX, sizeof(float) * n * m->n_in)) ||
+      (rc = device_alloc(h, (void**)&dA, sizeof(float) * n))) {
+    cudaFree(dm); cudaFree(dX);
+    return rc;
+  }
+  rc = upload_model(h, m, dm);
+  if (!rc) {
+    cudaMemcpy(dX, X, sizeof(float) * n * m->n_in, cudaMemcpyHostToDevice);
+    cudaError_t e = mlp_predict(dm, m->n_in, dX, n, dA, h->stream);
+    count_launches(1);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    if (e == cudaSuccess) e = cudaMemcpy(alpha, dA, sizeof(float) * n, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) rc = fail(h, MLBM_ERR_CUDA, "predict: %s", cudaGetErrorString(e));
+  }
+  cudaFree(dm); cudaFree(dX); cudaFree(dA);
+  return rc;
+}
+
+extern "C" int mlbm_alpha_model_gradient(mlbm_handle* h, const mlbm_mlp* m, const float* X,
+                                         const float* y, long long n, float* loss, mlbm_mlp* grad) {
+  if (!h || !m || !X || !y || !loss || !grad || n <= 0) return MLBM_ERR_INVALID;
+  if (m->n_in < 1 || m->n_in > MLBM_MLP_MAX_IN || m->n_hidden != MLBM_MLP_HIDDEN)
+    return fail(h, MLBM_ERR_INVALID, "bad model shape");
+  MLBM_CUDA(h, cudaSetDevice(h->cfg.device));
+  MlpTrainer tr;
+  cudaError_t e = tr.init(m->n_in, n, h->stream);
+  if (e == cudaSuccess) e = tr.set_data(X, y, n);
+  if (e == cudaSuccess) e = tr.set_model(*m);
+  float l = 0.0f;
+  if (e == cudaSuccess) e = tr.gradient(n, &l);
+  if (e == cudaSuccess) e = tr.get_gradient(grad);
+  count_launches(tr.launches);
+  tr.release();
+  if (e != cudaSuccess) return fail(h, MLBM_ERR_CUDA, "gradient: %s", cudaGetErrorString(e));
+  *loss = l;
+  return MLBM_OK;
+}
+
+extern "C" int mlbm_train_alpha_model(mlbm_handle* h, const float* X, const float* y, long long n,
+                                      mlbm_train_cfg* cfg, mlbm_mlp* m) {
+  if (!h || !X || !y || !cfg || !m || n <= 0) return MLBM_ERR_INVALID;
+  if (m->n_in < 1 || m->n_in > MLBM_MLP_MAX_IN || m->n_hidden != MLBM_MLP_HIDDEN)
+    return fail(h, MLBM_ERR_INVALID, "bad model shape");
+  if (cfg->epochs < 1 || cfg->batch < 1) return fail(h, MLBM_ERR_INVALID, "bad training configuration");
+  MLBM_CUDA(h, cudaSetDevice(h->cfg.device));
+  MlpTrainer tr;
+  cudaError_t e = tr.init(m->n_in, cfg->batch, h->stream);
+  if (e == cudaSuccess) e = tr.set_data(X, y, n);
+  if (e == cudaSuccess) e = tr.set_model(*m);
+  float last = 0.0f;
+  if (e == cudaSuccess) e = tr.train(*cfg, &last);
+  if (e == cudaSuccess) e = tr.get_model(m);
+  count_launches(tr.launches);
+  tr.release();
+  if (e != cudaSuccess) return fail(h, MLBM_ERR_CUDA, "training: %s", cudaGetErrorString(e));
+  cfg->final_loss = last;
+  return MLBM_OK;
+}
+
+extern "C" const char* mlbm_last_error(const mlbm_handle* h) {
+  if (h) return h->error.c_str();
+  std::lock_guard<std::mutex> lk(g_create_error_mutex);
+  static thread_local std::string copy;
+  copy = g_create_error;
+  return copy.c_str();
+}
+
+extern "C" unsigned long long mlbm_kernel_launch_count(void) {
+  return g_launches.load(std::memory_order_relaxed);
+}

@@ -1,0 +1,188 @@
+// Shared device-side definitions of the mlbm kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "lattice.cuh"
+
+namespace mlbm {
+
+enum : int { FS_NONE = 0, FS_GUO = 1, FS_SHANCHEN = 2, FS_EDM = 3 };
+enum : int { FORCE_NONE = 0, FORCE_CONSTANT = 1, FORCE_SINUSOIDAL = 2, FORCE_KOLMOGOROV = 3 };
+enum : int { ALPHA_REFERENCE = 0, ALPHA_RESIDUAL = 1 };
+enum : int { GUESS_PREVIOUS = 0, GUESS_TWO = 1, GUESS_LEARNED = 2 };
+
+enum : unsigned { ERR_NONFINITE = 1u, ERR_DENSITY = 2u };
+
+// Unsigned division by a runtime constant with a multiply-high
+// (Granlund & Montgomery, "Division by invariant integers using
+// multiplication", PLDI 1994): q = (umulhi(n, m) + n) >> s for n < 2^31.
+struct FastDiv {
+  uint32_t d, m, s;
+  __host__ void init(uint32_t divisor) {
+    d = divisor;
+    s = 0;
+    while ((1u << s) < divisor) ++s;
+    const uint64_t one = 1;
+    m = (uint32_t)(((one << 32) * ((one << s) - divisor)) / divisor + 1);
+    if (divisor == 1) { m = 0; s = 0; }
+  }
+  __device__ __forceinline__ uint32_t div(uint32_t n) const {
+    return (__umulhi(n, m) + n) >> s;
+  }
+};
+
+// Per-step parameters, passed by value to every step kernel.
+struct StepParams {
+  long long V;               // nodes
+  uint32_t lx, ly, lz;
+  FastDiv div_lz, div_ly;    // node index -> (x, y, z)
+  // relaxation
+  double tau, beta;
+  double bgk_a, bgk_b;       // (1 - 2 beta), 2 beta  (Collision.h:145-149)
+  double guo_k[27];          // ((1 - 1/(2 tau)) w_q) 3  (ForcingScheme.h:115-116)
+  // force
+  int force_type;
+  int kol_axis, kol_comp;
+  double amp[3];
+  const double* force_table[3];  // per-axis host-computed sin profiles (device)
+  // entropic solver
+  int alpha_mode, guess_mode;
+  double newton_tol;
+  int newton_maxit;
+  double deviation_threshold;
+  // optional outputs on this step
+  int store;                 // write rho, u_hydro, alpha(, force) fields
+  int diag;                  // fused diagnostics reduction
+  double* rho_out;
+  double* u_out;             // [D][V]
+  double* force_out;         // [D][V]
+  double* alpha_field;       // FP64 storage: per-node alpha (read guess, write result)
+  float* alpha_field_f32;    // FP32 storage: per-node alpha
+  double* diag_partials;     // per block: mass, energy, max_mach, alpha_min, alpha_max
+  unsigned long long* counters;  // solver counters (see CNT_*)
+  unsigned* err_word;
+  const void* mlp;           // device MlpDev* (learned guess)
+};
+
+enum : int {
+  CNT_SOLVED = 0, CNT_ITER = 1, CNT_HITS = 2, CNT_BISECT = 3, CNT_FALLBACK = 4,
+  CNT_LIMITED = 5, CNT_SHORTCUT = 6, CNT_COUNT = 8
+};
+constexpr int DIAG_FIELDS = 5;
+
+// Source node of the pulled population with velocity (cx, cy, cz): periodic
+// neighbour offsets along each axis, formed once per node.
+struct PullOffsets {
+  long long ox[3];  // index 0: c = -1 (reads x+1), 1: c = 0, 2: c = +1 (reads x-1)
+  long long oy[3];
+  long long oz[3];
+  __device__ __forceinline__ long long at(int cx, int cy, int cz) const {
+    return ox[cx + 1] + oy[cy + 1] + oz[cz + 1];
+  }
+};
+
+__device__ __forceinline__ void node_coords(const StepParams& p, long long idx, uint32_t& x,
+                                            uint32_t& y, uint32_t& z) {
+  const uint32_t i = (uint32_t)idx;
+  const uint32_t t = p.div_lz.div(i);
+  z = i - t * p.lz;
+  x = p.div_ly.div(t);
+  y = t - x * p.ly;
+}
+
+__device__ __forceinline__ PullOffsets pull_offsets(const StepParams& p, uint32_t x, uint32_t y,
+                                                    uint32_t z) {
+  PullOffsets o;
+  const long long sx = (long long)p.ly * p.lz;
+  const uint32_t xp = (x + 1 == p.lx) ? 0 : x + 1, xm = (x == 0) ? p.lx - 1 : x - 1;
+  const uint32_t yp = (y + 1 == p.ly) ? 0 : y + 1, ym = (y == 0) ? p.ly - 1 : y - 1;
+  const uint32_t zp = (z + 1 == p.lz) ? 0 : z + 1, zm = (z == 0) ? p.lz - 1 : z - 1;
+  o.ox[0] = xp * sx; o.ox[1] = x * sx; o.ox[2] = xm * sx;
+  o.oy[0] = (long long)yp * p.lz; o.oy[1] = (long long)y * p.lz; o.oy[2] = (long long)ym * p.lz;
+  o.oz[0] = zp; o.oz[1] = z; o.oz[2] = zm;
+  return o;
+}
+
+// Per-node body force (Force.h:137-292). The sine profiles are tabulated on
+// the host with the reference's expression amplitude * sin(i*2*pi/lambda)
+// (Force.h:213, 266), so the device reads the very same doubles.
+template <int D>
+__device__ __forceinline__ void node_force(const StepParams& p, uint32_t x, uint32_t y,
+                                           uint32_t z, double F[3]) {
+  F[0] = 0.0; F[1] = 0.0; F[2] = 0.0;
+  switch (p.force_type) {
+    case FORCE_CONSTANT:
+#pragma unroll
+      for (int d = 0; d < D; ++d) F[d] = p.amp[d];
+      break;
+    case FORCE_SINUSOIDAL:
+      F[0] = __ldg(p.force_table[0] + x);
+      F[1] = __ldg(p.force_table[1] + y);
+      if (D == 3) F[2] = __ldg(p.force_table[2] + z);
+      break;
+    case FORCE_KOLMOGOROV: {
+      const uint32_t c = p.kol_axis == 0 ? x : (p.kol_axis == 1 ? y : z);
+      const double v = __ldg(p.force_table[0] + c);
+      F[0] = p.kol_comp == 0 ? v : 0.0;
+      F[1] = p.kol_comp == 1 ? v : 0.0;
+      F[2] = p.kol_comp == 2 ? v : 0.0;
+      break;
+    }
+    default:
+      break;
+  }
+}
+
+// Warp + block reduction of the diagnostics, written to partials[blockIdx.x].
+__device__ __forceinline__ void block_reduce_diag(double mass, double energy, double mach,
+                                                  double amin, double amax, double* partials) {
+  __shared__ double sh[DIAG_FIELDS][32];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    mass += __shfl_down_sync(0xffffffffu, mass, o);
+    energy += __shfl_down_sync(0xffffffffu, energy, o);
+    mach = fmax(mach, __shfl_down_sync(0xffffffffu, mach, o));
+    amin = fmin(amin, __shfl_down_sync(0xffffffffu, amin, o));
+    amax = fmax(amax, __shfl_down_sync(0xffffffffu, amax, o));
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  if (lane == 0) {
+    sh[0][warp] = mass; sh[1][warp] = energy; sh[2][warp] = mach;
+    sh[3][warp] = amin; sh[4][warp] = amax;
+  }
+  __syncthreads();
+  if (warp == 0) {
+    mass = lane < nw ? sh[0][lane] : 0.0;
+    energy = lane < nw ? sh[1][lane] : 0.0;
+    mach = lane < nw ? sh[2][lane] : 0.0;
+    amin = lane < nw ? sh[3][lane] : 1e300;
+    amax = lane < nw ? sh[4][lane] : -1e300;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      mass += __shfl_down_sync(0xffffffffu, mass, o);
+      energy += __shfl_down_sync(0xffffffffu, energy, o);
+      mach = fmax(mach, __shfl_down_sync(0xffffffffu, mach, o));
+      amin = fmin(amin, __shfl_down_sync(0xffffffffu, amin, o));
+      amax = fmax(amax, __shfl_down_sync(0xffffffffu, amax, o));
+    }
+    if (lane == 0) {
+      double* o = partials + (size_t)blockIdx.x * DIAG_FIELDS;
+      o[0] = mass; o[1] = energy; o[2] = mach; o[3] = amin; o[4] = amax;
+    }
+  }
+}
+
+// Warp-aggregated add of the solver counters.
+__device__ __forceinline__ void add_counters(unsigned long long* counters, const unsigned c[CNT_COUNT]) {
+#pragma unroll
+  for (int k = 0; k < 7; ++k) {
+    unsigned v = c[k];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0 && v) atomicAdd(counters + k, (unsigned long long)v);
+  }
+}
+
+}  // namespace mlbm

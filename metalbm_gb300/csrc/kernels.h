@@ -1,0 +1,83 @@
+// Host-callable launchers of the mlbm kernels (plain C++ signatures).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "common.cuh"
+
+namespace mlbm {
+
+// FP64 storage, reference arithmetic (step_f64.cu).
+cudaError_t step_f64(int lattice, int collision, int forcing, const double* prev, double* next,
+                     const StepParams& p, cudaStream_t s);
+cudaError_t init_f64(int lattice, const double* rho, const double* u, double* f, long long V,
+                     cudaStream_t s);
+
+// FP32 / FP16-shifted storage, FP32 collision (step_lowp.cu).
+cudaError_t step_lowp(int lattice, int collision, int forcing, int storage, const void* prev,
+                      void* next, const StepParams& p, cudaStream_t s);
+cudaError_t init_lowp(int lattice, int storage, const double* rho, const double* u, void* f,
+                      long long V, cudaStream_t s);
+// Population q between storage and FP64 (staging buffers of V doubles).
+cudaError_t lowp_to_f64(int lattice, int storage, const void* f, int q, double* out, long long V,
+                        cudaStream_t s);
+cudaError_t f64_to_lowp(int lattice, int storage, const double* in, int q, void* f, long long V,
+                        cudaStream_t s);
+
+// Diagnostics: sum the per-block partials in a fixed order (deterministic).
+cudaError_t finalize_diag(const double* partials, int nblocks, double* out, cudaStream_t s);
+
+// Sample logger: (f_neq/rho [Q], alpha) at the given nodes, from the
+// pre-collision populations `prev` and the alpha field of the step just run.
+cudaError_t log_samples_f64(int lattice, const double* prev, const StepParams& p,
+                            const long long* nodes, long long n, double* features, double* alpha,
+                            int* solved, cudaStream_t s);
+cudaError_t log_samples_lowp(int lattice, int storage, const void* prev, const StepParams& p,
+                             const long long* nodes, long long n, double* features, double* alpha,
+                             int* solved, cudaStream_t s);
+cudaError_t log_samples(int lattice, int storage, const void* prev, const StepParams& p,
+                        const long long* nodes, long long n, double* features, double* alpha,
+                        int* solved, cudaStream_t s);
+
+// Per-lattice (and per-storage) entry points, one translation unit each.
+cudaError_t step_f64_L0(int collision, int forcing, const double* prev, double* next, const StepParams& p, cudaStream_t s);
+cudaError_t init_f64_L0(const double* rho, const double* u, double* f, long long V, cudaStream_t s);
+cudaError_t log_samples_f64_L0(const double* prev, const StepParams& p, const long long* nodes, long long n, double* features, double* alpha, int* solved, cudaStream_t s);
+cudaError_t step_lowp_L0_S1(int collision, int fs, const void* prev, void* next, const StepParams& p, cudaStream_t s);
+cudaError_t init_lowp_L0_S1(const double* rho, const double* u, void* f, long long V, cudaStream_t s);
+cudaError_t lowp_to_f64_L0_S1(const void* f, int q, double* out, long long V, cudaStream_t s);
+cudaError_t f64_to_lowp_L0_S1(const double* in, int q, void* f, long long V, cudaStream_t s);
+cudaError_t log_samples_lowp_L0_S1(const void* prev, const StepParams& p, const long long* nodes, long long n, double* features, double* alpha, int* solved, cudaStream_t s);
+cudaError_t step_lowp_L0_S2(int collision, int fs, const void* prev, void* next, const StepParams& p, cudaStream_t s);
+cudaError_t init_lowp_L0_S2(const double* rho, const double* u, void* f, long long V, cudaStream_t s);
+cudaError_t lowp_to_f64_L0_S2(const void* f, int q, double* out, long long V, cudaStream_t s);
+cudaError_t f64_to_lowp_L0_S2(const double* in, int q, void* f, long long V, cudaStream_t s);
+cudaError_t log_samples_lowp_L0_S2(const void* prev, const StepParams& p, const long long* nodes, long long n, double* features, double* alpha, int* solved, cudaStream_t s);
+cudaError_t step_f64_L1(int collision, int forcing, const double* prev, double* next, const StepParams& p, cudaStream_t s);
+cudaError_t init_f64_L1(const double* rho, const double* u, double* f, long long V, cudaStream_t s);
+cudaError_t log_samples_f64_L1(const double* prev, const StepParams& p, const long long* nodes, long long n, double* features, double* alpha, int* solved, cudaStream_t s);
+cudaError_t step_lowp_L1_S1(int collision, int fs, const void* prev, void* next, const StepParams& p, cudaStream_t s);
+cudaError_t init_lowp_L1_S1(const double* rho, const double* u, void* f, long long V, cudaStream_t s);
+cudaError_t lowp_to_f64_L1_S1(const void* f, int q, double* out, long long V, cudaStream_t s);
+cudaError_t f64_to_lowp_L1_S1(const double* in, int q, void* f, long long V, cudaStream_t s);
+cudaError_t log_samples_lowp_L1_S1(const void* prev, const StepParams& p, const long long* nodes, long long n, double* features, double* alpha, int* solved, cudaStream_t s);
+cudaError_t step_lowp_L1_S2(int collision, int fs, const void* prev, void* next, const StepParams& p, cudaStream_t s);
+cudaError_t init_lowp_L1_S2(const double* rho, const double* u, void* f, long long V, cudaStream_t s);
+cudaError_t lowp_to_f64_L1_S2(const void* f, int q, double* out, long long V, cudaStream_t s);
+cudaError_t f64_to_lowp_L1_S2(const double* in, int q, void* f, long long V, cudaStream_t s);
+cudaError_t log_samples_lowp_L1_S2(const void* prev, const StepParams& p, const long long* nodes, long long n, double* features, double* alpha, int* solved, cudaStream_t s);
+cudaError_t step_f64_L2(int collision, int forcing, const double* prev, double* next, const StepParams& p, cudaStream_t s);
+cudaError_t init_f64_L2(const double* rho, const double* u, double* f, long long V, cudaStream_t s);
+cudaError_t log_samples_f64_L2(const double* prev, const StepParams& p, const long long* nodes, long long n, double* features, double* alpha, int* solved, cudaStream_t s);
+cudaError_t step_lowp_L2_S1(int collision, int fs, const void* prev, void* next, const StepParams& p, cudaStream_t s);
+cudaError_t init_lowp_L2_S1(const double* rho, const double* u, void* f, long long V, cudaStream_t s);
+cudaError_t lowp_to_f64_L2_S1(const void* f, int q, double* out, long long V, cudaStream_t s);
+cudaError_t f64_to_lowp_L2_S1(const double* in, int q, void* f, long long V, cudaStream_t s);
+cudaError_t log_samples_lowp_L2_S1(const void* prev, const StepParams& p, const long long* nodes, long long n, double* features, double* alpha, int* solved, cudaStream_t s);
+cudaError_t step_lowp_L2_S2(int collision, int fs, const void* prev, void* next, const StepParams& p, cudaStream_t s);
+cudaError_t init_lowp_L2_S2(const double* rho, const double* u, void* f, long long V, cudaStream_t s);
+cudaError_t lowp_to_f64_L2_S2(const void* f, int q, double* out, long long V, cudaStream_t s);
+cudaError_t f64_to_lowp_L2_S2(const double* in, int q, void* f, long long V, cudaStream_t s);
+cudaError_t log_samples_lowp_L2_S2(const void* prev, const StepParams& p, const long long* nodes, long long n, double* features, double* alpha, int* solved, cudaStream_t s);
+
+}  // namespace mlbm

@@ -1,0 +1,100 @@
+// Small kernels shared by every storage format: the fixed-order reduction of
+// the per-block diagnostics partials, and the sample-logger dispatch.
+
+#include "common.cuh"
+#include "kernels.h"
+
+namespace mlbm {
+
+// One block of 256 threads: each thread folds a strided subset of the
+// partials in index order, then a fixed tree; the result does not depend on
+// scheduling, so a diagnostics value is reproducible run to run.
+__global__ void finalize_diag_kernel(const double* __restrict__ partials, int nblocks,
+                                     double* __restrict__ out) {
+  __shared__ double sh[DIAG_FIELDS][256];
+  double m = 0.0, e = 0.0, mach = 0.0, amin = 1e300, amax = -1e300;
+  for (int b = threadIdx.x; b < nblocks; b += blockDim.x) {
+    const double* p = partials + (size_t)b * DIAG_FIELDS;
+    m += p[0];
+    e += p[1];
+    mach = fmax(mach, p[2]);
+    amin = fmin(amin, p[3]);
+    amax = fmax(amax, p[4]);
+  }
+  sh[0][threadIdx.x] = m; sh[1][threadIdx.x] = e; sh[2][threadIdx.x] = mach;
+  sh[3][threadIdx.x] = amin; sh[4][threadIdx.x] = amax;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) {
+      sh[0][threadIdx.x] += sh[0][threadIdx.x + w];
+      sh[1][threadIdx.x] += sh[1][threadIdx.x + w];
+      sh[2][threadIdx.x] = fmax(sh[2][threadIdx.x], sh[2][threadIdx.x + w]);
+      sh[3][threadIdx.x] = fmin(sh[3][threadIdx.x], sh[3][threadIdx.x + w]);
+      sh[4][threadIdx.x] = fmax(sh[4][threadIdx.x], sh[4][threadIdx.x + w]);
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0)
+    for (int k = 0; k < DIAG_FIELDS; ++k) out[k] = sh[k][0];
+}
+
+cudaError_t finalize_diag(const double* partials, int nblocks, double* out, cudaStream_t s) {
+  finalize_diag_kernel<<<1, 256, 0, s>>>(partials, nblocks, out);
+  return cudaGetLastError();
+}
+
+#define MLBM_BY_LAT(L, CALL0, CALL1, CALL2) \
+  switch (L) { case 0: return CALL0; case 1: return CALL1; case 2: return CALL2; } \
+  return cudaErrorInvalidValue;
+#define MLBM_BY_LAT_ST(L, S, F, ARGS) \
+  if (S == 1) { MLBM_BY_LAT(L, F##_L0_S1 ARGS, F##_L1_S1 ARGS, F##_L2_S1 ARGS) } \
+  if (S == 2) { MLBM_BY_LAT(L, F##_L0_S2 ARGS, F##_L1_S2 ARGS, F##_L2_S2 ARGS) } \
+  return cudaErrorInvalidValue;
+
+cudaError_t step_f64(int lattice, int collision, int forcing, const double* prev, double* next,
+                     const StepParams& p, cudaStream_t s) {
+  MLBM_BY_LAT(lattice, step_f64_L0(collision, forcing, prev, next, p, s),
+              step_f64_L1(collision, forcing, prev, next, p, s),
+              step_f64_L2(collision, forcing, prev, next, p, s))
+}
+
+cudaError_t init_f64(int lattice, const double* rho, const double* u, double* f, long long V,
+                     cudaStream_t s) {
+  MLBM_BY_LAT(lattice, init_f64_L0(rho, u, f, V, s), init_f64_L1(rho, u, f, V, s),
+              init_f64_L2(rho, u, f, V, s))
+}
+
+cudaError_t step_lowp(int lattice, int collision, int forcing, int storage, const void* prev,
+                      void* next, const StepParams& p, cudaStream_t s) {
+  MLBM_BY_LAT_ST(lattice, storage, step_lowp, (collision, forcing, prev, next, p, s))
+}
+
+cudaError_t init_lowp(int lattice, int storage, const double* rho, const double* u, void* f,
+                      long long V, cudaStream_t s) {
+  MLBM_BY_LAT_ST(lattice, storage, init_lowp, (rho, u, f, V, s))
+}
+
+cudaError_t lowp_to_f64(int lattice, int storage, const void* f, int q, double* out, long long V,
+                        cudaStream_t s) {
+  MLBM_BY_LAT_ST(lattice, storage, lowp_to_f64, (f, q, out, V, s))
+}
+
+cudaError_t f64_to_lowp(int lattice, int storage, const double* in, int q, void* f, long long V,
+                        cudaStream_t s) {
+  MLBM_BY_LAT_ST(lattice, storage, f64_to_lowp, (in, q, f, V, s))
+}
+
+cudaError_t log_samples(int lattice, int storage, const void* prev, const StepParams& p,
+                        const long long* nodes, long long n, double* features, double* alpha,
+                        int* solved, cudaStream_t s) {
+  if (storage == 0) {
+    MLBM_BY_LAT(lattice,
+                log_samples_f64_L0((const double*)prev, p, nodes, n, features, alpha, solved, s),
+                log_samples_f64_L1((const double*)prev, p, nodes, n, features, alpha, solved, s),
+                log_samples_f64_L2((const double*)prev, p, nodes, n, features, alpha, solved, s))
+  }
+  MLBM_BY_LAT_ST(lattice, storage, log_samples_lowp,
+                 (prev, p, nodes, n, features, alpha, solved, s))
+}
+
+}  // namespace mlbm

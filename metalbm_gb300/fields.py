@@ -58,45 +58,58 @@ def taylor_green(shape, u0: float = 0.05, rho0: float = 1.0):
 
     u = U0 sin x cos y cos z, v = -U0 cos x sin y cos z, w = 0,
     p = rho0 U0^2 / 16 (cos 2x + cos 2y)(cos 2z + 2), rho = rho0 + 3 p.
+    Built by broadcasting separable factors (no full-size coordinate grids).
     """
     lx, ly, lz = shape
     x = 2 * np.pi * np.arange(lx) / lx
     y = 2 * np.pi * np.arange(ly) / ly
     z = 2 * np.pi * np.arange(lz) / lz
-    X, Y, Z = np.meshgrid(x, y, z, indexing="ij")
-    ux = u0 * np.sin(X) * np.cos(Y) * np.cos(Z)
-    uy = -u0 * np.cos(X) * np.sin(Y) * np.cos(Z)
-    uz = np.zeros_like(ux)
-    p = rho0 * u0 * u0 / 16.0 * (np.cos(2 * X) + np.cos(2 * Y)) * (np.cos(2 * Z) + 2.0)
-    rho = rho0 + 3.0 * p
-    return rho.reshape(-1), np.stack([ux.reshape(-1), uy.reshape(-1), uz.reshape(-1)])
+    sx, cx = np.sin(x)[:, None, None], np.cos(x)[:, None, None]
+    sy, cy = np.sin(y)[None, :, None], np.cos(y)[None, :, None]
+    cz = np.cos(z)[None, None, :]
+    u = np.empty((3, lx, ly, lz))
+    u[0] = u0 * (sx * cy) * cz
+    u[1] = -u0 * (cx * sy) * cz
+    u[2] = 0.0
+    c2 = (np.cos(2 * x)[:, None, None] + np.cos(2 * y)[None, :, None])
+    rho = rho0 + 3.0 * (rho0 * u0 * u0 / 16.0) * c2 * (np.cos(2 * z)[None, None, :] + 2.0)
+    return rho.reshape(-1), u.reshape(3, -1)
 
 
 def solenoidal_shell(shape, kmin: float, kmax: float, amplitude: float, seed: int):
     """Random-phase divergence-free velocity on the wavenumber shell kmin<=|k|<=kmax.
 
     Each Fourier mode in the shell gets a random complex vector (counter-based
-    draws keyed by the mode's index), projected orthogonal to k; the field is
-    the real inverse FFT, scaled so that the largest |u| equals ``amplitude``.
-    Returns u [3, V] in reference node order.
+    draws keyed by the mode's index in the half-spectrum array), projected
+    orthogonal to k; the field is the real inverse FFT, scaled so that the
+    largest |u| equals ``amplitude``. Returns u [3, V] in reference node order.
     """
     lx, ly, lz = shape
     kx = np.fft.fftfreq(lx, 1.0 / lx)
     ky = np.fft.fftfreq(ly, 1.0 / ly)
     kz = np.fft.rfftfreq(lz, 1.0 / lz)
-    KX, KY, KZ = np.meshgrid(kx, ky, kz, indexing="ij")
+    nz = kz.size
+    # shell modes only: |k| <= kmax bounds every component
+    sel = [np.nonzero(np.abs(k) <= kmax)[0] for k in (kx, ky, kz)]
+    I, J, K = np.meshgrid(*sel, indexing="ij")
+    I, J, K = I.ravel(), J.ravel(), K.ravel()
+    KX, KY, KZ = kx[I], ky[J], kz[K]
     k2 = KX ** 2 + KY ** 2 + KZ ** 2
-    shell = (k2 >= kmin * kmin) & (k2 <= kmax * kmax)
-    idx = np.arange(KX.size, dtype=np.uint64).reshape(KX.shape)
-    uh = []
+    m = (k2 >= kmin * kmin) & (k2 <= kmax * kmax)
+    I, J, K, KX, KY, KZ, k2 = I[m], J[m], K[m], KX[m], KY[m], KZ[m], k2[m]
+    idx = ((I.astype(np.int64) * ly + J) * nz + K).astype(np.uint64)
+    c = []
     for d in range(3):
         re = 2.0 * uniform(seed, 10 + 2 * d, idx) - 1.0
         im = 2.0 * uniform(seed, 11 + 2 * d, idx) - 1.0
-        uh.append(np.where(shell, re + 1j * im, 0.0))
-    kk = np.where(k2 == 0, 1.0, k2)
-    kdotu = (KX * uh[0] + KY * uh[1] + KZ * uh[2]) / kk
-    uh = [uh[0] - KX * kdotu, uh[1] - KY * kdotu, uh[2] - KZ * kdotu]
-    u = np.stack([np.fft.irfftn(c, s=(lx, ly, lz)) for c in uh])
+        c.append(re + 1j * im)
+    kdotu = (KX * c[0] + KY * c[1] + KZ * c[2]) / k2
+    c = [c[0] - KX * kdotu, c[1] - KY * kdotu, c[2] - KZ * kdotu]
+    u = np.empty((3, lx, ly, lz))
+    for d in range(3):
+        spec = np.zeros((lx, ly, nz), np.complex128)
+        spec[I, J, K] = c[d]
+        u[d] = np.fft.irfftn(spec, s=(lx, ly, lz))
     peak = np.sqrt((u ** 2).sum(axis=0)).max()
     if peak > 0:
         u *= amplitude / peak

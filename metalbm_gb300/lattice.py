@@ -1,0 +1,310 @@
+"""Python host side of the drop-in: InputDeck, Lattice (one handle), Algorithm."""
+from __future__ import annotations
+
+import ctypes as ct
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import capi
+from .capi import MlbmError
+
+_LATTICES = {"D2Q9": capi.D2Q9, "D3Q19": capi.D3Q19, "D3Q27": capi.D3Q27}
+_COLLISIONS = {"BGK": capi.BGK, "ELBM": capi.ELBM, "ForcedBNR_ELBM": capi.FORCED_BNR_ELBM}
+_FORCINGS = {"None": capi.FORCING_NONE, "Guo": capi.FORCING_GUO,
+             "ShanChen": capi.FORCING_SHAN_CHEN,
+             "ExactDifferenceMethod": capi.FORCING_EXACT_DIFFERENCE}
+_FORCES = {"None": capi.FORCE_NONE, "Constant": capi.FORCE_CONSTANT,
+           "Sinusoidal": capi.FORCE_SINUSOIDAL, "Kolmogorov": capi.FORCE_KOLMOGOROV}
+_STORAGES = {"f64": capi.STORAGE_F64, "f32": capi.STORAGE_F32,
+             "f16_shifted": capi.STORAGE_F16_SHIFTED}
+_ALPHA = {"reference": capi.ALPHA_REFERENCE, "residual": capi.ALPHA_RESIDUAL}
+_GUESS = {"previous": capi.GUESS_PREVIOUS, "two": capi.GUESS_TWO, "learned": capi.GUESS_LEARNED}
+Q_OF = {"D2Q9": 9, "D3Q19": 19, "D3Q27": 27}
+D_OF = {"D2Q9": 2, "D3Q19": 3, "D3Q27": 3}
+
+
+@dataclass
+class InputDeck:
+    """The Input.in parameters of the hot path (src/Input_prod.in:16-53),
+    as a runtime configuration. Names follow the reference deck."""
+    latticeT: str = "D2Q9"
+    collisionT: str = "BGK"
+    forcingSchemeT: str = "None"
+    forceT: str = "None"
+    relaxationTime: float = 0.7
+    forceAmplitude: tuple = (0.0, 0.0, 0.0)
+    forceWaveLength: tuple = (32.0, 32.0, 32.0)
+    globalLength: tuple = (16, 16, 16)
+    # Kolmogorov force: F[component] = A sin(2 pi x[axis] / lambda); the
+    # reference is axis = 1 (y), component = 0 (x), Force.h:262-267.
+    kolmogorovAxis: int = 1
+    kolmogorovComponent: int = 0
+    # GB300 build options
+    storage: str = "f64"
+    alphaSolver: str = "reference"
+    alphaGuess: str = "previous"
+    newtonTolerance: float = 1e-8
+    newtonMaxIterations: int = 50
+    deviationThreshold: float = 1e-3
+    device: int = 0
+
+    @property
+    def Q(self) -> int:
+        return Q_OF[self.latticeT]
+
+    @property
+    def D(self) -> int:
+        return D_OF[self.latticeT]
+
+    @property
+    def shape(self) -> tuple[int, int, int]:
+        lx, ly, lz = self.globalLength
+        return (lx, ly, 1 if self.D == 2 else lz)
+
+    def to_c(self) -> capi.Config:
+        c = capi.Config()
+        capi.load().mlbm_config_init(ct.byref(c))
+        c.lattice = _LATTICES[self.latticeT]
+        c.collision = _COLLISIONS[self.collisionT]
+        c.forcing_scheme = _FORCINGS[self.forcingSchemeT]
+        c.force = _FORCES[self.forceT]
+        c.relaxation_time = float(self.relaxationTime)
+        for d in range(3):
+            c.force_amplitude[d] = float(self.forceAmplitude[d])
+            c.force_wavelength[d] = float(self.forceWaveLength[d])
+            c.length[d] = int(self.globalLength[d])
+        c.kolmogorov_axis = int(self.kolmogorovAxis)
+        c.kolmogorov_component = int(self.kolmogorovComponent)
+        c.storage = _STORAGES[self.storage]
+        c.alpha_mode = _ALPHA[self.alphaSolver]
+        c.alpha_guess = _GUESS[self.alphaGuess]
+        c.newton_tolerance = float(self.newtonTolerance)
+        c.newton_max_iterations = int(self.newtonMaxIterations)
+        c.deviation_threshold = float(self.deviationThreshold)
+        c.device = int(self.device)
+        return c
+
+
+@dataclass
+class MlpModel:
+    """Weights of the alpha-guess MLP (n_in -> 32 -> 32 -> 1, tanh)."""
+    n_in: int
+    input_scale: np.ndarray
+    w1: np.ndarray  # [32, n_in]
+    b1: np.ndarray
+    w2: np.ndarray  # [32, 32]
+    b2: np.ndarray
+    w3: np.ndarray  # [32]
+    b3: float
+    output_scale: float
+
+    @staticmethod
+    def init(n_in: int, input_scale, output_scale: float, seed: int = 0) -> "MlpModel":
+        rng = np.random.default_rng(seed)
+        h = capi.MLP_HIDDEN
+        return MlpModel(n_in, np.asarray(input_scale, np.float32),
+                        (rng.standard_normal((h, n_in)) / np.sqrt(n_in)).astype(np.float32),
+                        np.zeros(h, np.float32),
+                        (rng.standard_normal((h, h)) / np.sqrt(h)).astype(np.float32),
+                        np.zeros(h, np.float32),
+                        (rng.standard_normal(h) / np.sqrt(h)).astype(np.float32), 0.0,
+                        float(output_scale))
+
+    def to_c(self) -> capi.Mlp:
+        m = capi.Mlp()
+        m.n_in, m.n_hidden = self.n_in, capi.MLP_HIDDEN
+        ct.memmove(m.input_scale, np.ascontiguousarray(self.input_scale, np.float32).ctypes.data,
+                   4 * self.n_in)
+        ct.memmove(m.w1, np.ascontiguousarray(self.w1, np.float32).ctypes.data, 4 * 32 * self.n_in)
+        for name in ("b1", "b2", "w3"):
+            ct.memmove(getattr(m, name), np.ascontiguousarray(getattr(self, name), np.float32)
+                       .ctypes.data, 4 * 32)
+        ct.memmove(m.w2, np.ascontiguousarray(self.w2, np.float32).ctypes.data, 4 * 32 * 32)
+        m.b3 = float(self.b3)
+        m.output_scale = float(self.output_scale)
+        return m
+
+    @staticmethod
+    def from_c(m: capi.Mlp) -> "MlpModel":
+        n = m.n_in
+        arr = lambda a, k: np.ctypeslib.as_array(a)[:k].astype(np.float32).copy()  # noqa: E731
+        return MlpModel(n, arr(m.input_scale, n), arr(m.w1, 32 * n).reshape(32, n),
+                        arr(m.b1, 32), arr(m.w2, 1024).reshape(32, 32), arr(m.b2, 32),
+                        arr(m.w3, 32), float(m.b3), float(m.output_scale))
+
+
+def _dptr(a: np.ndarray):
+    return a.ctypes.data_as(ct.POINTER(ct.c_double))
+
+
+def _fptr(a: np.ndarray):
+    return a.ctypes.data_as(ct.POINTER(ct.c_float))
+
+
+class Lattice:
+    """One periodic lattice on one GPU, driven through the C ABI."""
+
+    def __init__(self, deck: InputDeck):
+        self.deck = deck
+        self._lib = capi.load()
+        self.Q, self.D = deck.Q, deck.D
+        self.shape = deck.shape
+        self.V = int(np.prod(self.shape))
+        cfg = deck.to_c()
+        h = ct.c_void_p()
+        rc = self._lib.mlbm_create(ct.byref(cfg), ct.byref(h))
+        if rc != capi.OK:
+            raise MlbmError(rc, self._lib.mlbm_last_error(None).decode())
+        self._h = h
+
+    # --- plumbing
+    def _check(self, rc: int):
+        if rc != capi.OK:
+            raise MlbmError(rc, self._lib.mlbm_last_error(self._h).decode())
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.mlbm_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    @property
+    def handle(self):
+        return self._h
+
+    @property
+    def stream(self) -> int:
+        s = ct.c_void_p()
+        self._check(self._lib.mlbm_get_stream(self._h, ct.byref(s)))
+        return s.value or 0
+
+    def set_stream(self, stream_ptr: int | None):
+        self._check(self._lib.mlbm_set_stream(self._h, ct.c_void_p(stream_ptr or 0)))
+
+    # --- state
+    def init_equilibrium(self, rho: np.ndarray, u: np.ndarray, layout: int = capi.LAYOUT_DENSE):
+        rho = np.ascontiguousarray(rho, np.float64)
+        u = np.ascontiguousarray(u, np.float64)
+        self._check(self._lib.mlbm_init_equilibrium(self._h, _dptr(rho), _dptr(u), layout))
+
+    def set_populations(self, f: np.ndarray, layout: int = capi.LAYOUT_DENSE):
+        f = np.ascontiguousarray(f, np.float64)
+        self._check(self._lib.mlbm_set_populations(self._h, _dptr(f), layout))
+
+    def populations(self) -> np.ndarray:
+        f = np.empty((self.Q, self.V))
+        self._check(self._lib.mlbm_get_populations(self._h, _dptr(f), capi.LAYOUT_DENSE))
+        return f
+
+    def step(self, n: int = 1, store: bool = False, diagnostics: bool = False,
+             samples: bool = False):
+        flags = (capi.STEP_STORE_FIELDS if store else 0) | \
+                (capi.STEP_DIAGNOSTICS if diagnostics else 0) | \
+                (capi.STEP_LOG_SAMPLES if samples else 0)
+        self._check(self._lib.mlbm_step(self._h, int(n), flags))
+
+    def sync(self, timeout_ms: int = -1):
+        self._check(self._lib.mlbm_sync(self._h, int(timeout_ms)))
+
+    def fields(self) -> dict[str, np.ndarray]:
+        rho = np.empty(self.V)
+        u = np.empty((self.D, self.V))
+        alpha = np.empty(self.V)
+        force = np.empty((self.D, self.V))
+        self._check(self._lib.mlbm_get_fields(self._h, _dptr(rho), _dptr(u), _dptr(alpha),
+                                              _dptr(force), capi.LAYOUT_DENSE))
+        return {"rho": rho, "u": u, "alpha": alpha, "force": force}
+
+    def diagnostics(self) -> dict:
+        d = capi.Diag()
+        self._check(self._lib.mlbm_get_diagnostics(self._h, ct.byref(d)))
+        return d.as_dict()
+
+    # --- sample logger and learned alpha
+    def set_sample_nodes(self, nodes: np.ndarray):
+        nodes = np.ascontiguousarray(nodes, np.int64)
+        self._n_samples = len(nodes)
+        self._check(self._lib.mlbm_set_sample_nodes(
+            self._h, nodes.ctypes.data_as(ct.POINTER(ct.c_longlong)), len(nodes)))
+
+    def samples(self) -> tuple[np.ndarray, np.ndarray, np.ndarray]:
+        n = self._n_samples
+        feat = np.empty((n, self.Q))
+        alpha = np.empty(n)
+        solved = np.empty(n, np.int32)
+        self._check(self._lib.mlbm_get_samples(self._h, _dptr(feat), _dptr(alpha),
+                                               solved.ctypes.data_as(ct.POINTER(ct.c_int))))
+        return feat, alpha, solved
+
+    def set_alpha_model(self, model: MlpModel):
+        m = model.to_c()
+        self._check(self._lib.mlbm_set_alpha_model(self._h, ct.byref(m)))
+
+    def train_alpha_model(self, X: np.ndarray, y: np.ndarray, model: MlpModel, epochs: int = 10,
+                          batch: int = 4096, lr: float = 1e-3, seed: int = 0) -> tuple[MlpModel, float]:
+        X = np.ascontiguousarray(X, np.float32)
+        y = np.ascontiguousarray(y, np.float32)
+        cfg = capi.TrainCfg(epochs, batch, lr, 0.9, 0.999, 1e-8, seed, 0.0)
+        m = model.to_c()
+        self._check(self._lib.mlbm_train_alpha_model(self._h, _fptr(X), _fptr(y), len(y),
+                                                     ct.byref(cfg), ct.byref(m)))
+        return MlpModel.from_c(m), cfg.final_loss
+
+    def alpha_model_gradient(self, model: MlpModel, X: np.ndarray, y: np.ndarray):
+        X = np.ascontiguousarray(X, np.float32)
+        y = np.ascontiguousarray(y, np.float32)
+        m = model.to_c()
+        g = capi.Mlp()
+        loss = ct.c_float()
+        self._check(self._lib.mlbm_alpha_model_gradient(self._h, ct.byref(m), _fptr(X), _fptr(y),
+                                                        len(y), ct.byref(loss), ct.byref(g)))
+        return float(loss.value), MlpModel.from_c(g)
+
+    def alpha_model_predict(self, model: MlpModel, X: np.ndarray) -> np.ndarray:
+        X = np.ascontiguousarray(X, np.float32)
+        out = np.empty(len(X), np.float32)
+        m = model.to_c()
+        self._check(self._lib.mlbm_alpha_model_predict(self._h, ct.byref(m), _fptr(X), len(X),
+                                                       _fptr(out)))
+        return out
+
+
+def kernel_launch_count() -> int:
+    return int(capi.load().mlbm_kernel_launch_count())
+
+
+class Algorithm:
+    """metaLBM's Algorithm surface on the GPU lattice (Algorithm.h:23-29).
+
+    ``iterate(iteration)`` runs one fused pull step (Algorithm.h:326-358);
+    ``isStored`` makes that step store rho, u, alpha and F (Algorithm.h:67,
+    150-194); ``unpack(local)`` / ``pack()`` move the populations in and out
+    in the reference's padded local layout (Algorithm.h:132-147).
+    """
+
+    def __init__(self, lattice: Lattice):
+        self.lattice = lattice
+        self.isStored = False
+        self._iteration = 0
+
+    def iterate(self, iteration: int):
+        self.lattice.step(1, store=self.isStored)
+        self._iteration = iteration
+
+    def unpack(self, local: np.ndarray):
+        self.lattice.set_populations(local, capi.LAYOUT_REFERENCE)
+
+    def pack(self, local: np.ndarray):
+        f = np.ascontiguousarray(local, np.float64)
+        self.lattice._check(self.lattice._lib.mlbm_get_populations(
+            self.lattice.handle, _dptr(f), capi.LAYOUT_REFERENCE))
+        local[...] = f

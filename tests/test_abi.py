@@ -1,0 +1,71 @@
+"""The C-ABI library builds, loads and exports every entry point that
+include/mlbm/mlbm.h declares. No GPU compute here: only calls that are valid
+without a device (config defaults, error reporting)."""
+import ctypes as ct
+import re
+
+import pytest
+
+from conftest import ROOT
+
+
+def header_functions():
+    text = (ROOT / "include" / "mlbm" / "mlbm.h").read_text()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(mlbm_[a-z_0-9]+)\s*\(", text)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from metalbm_gb300 import build, capi
+    build.build()
+    return capi.load()
+
+
+def test_header_declares_the_boundary():
+    names = header_functions()
+    for n in ["mlbm_create", "mlbm_destroy", "mlbm_init_equilibrium", "mlbm_set_populations",
+              "mlbm_get_populations", "mlbm_step", "mlbm_get_fields", "mlbm_get_diagnostics",
+              "mlbm_set_alpha_model", "mlbm_train_alpha_model", "mlbm_last_error", "mlbm_sync"]:
+        assert n in names
+
+
+def test_library_exports_every_declared_symbol(lib):
+    from metalbm_gb300 import capi
+    missing = [n for n in header_functions() if not hasattr(lib, n)]
+    assert not missing, missing
+    assert sorted(capi.EXPORTS) == header_functions()
+
+
+def test_config_defaults_are_the_reference_deck(lib):
+    from metalbm_gb300 import capi
+    c = capi.Config()
+    assert lib.mlbm_config_init(ct.byref(c)) == capi.OK
+    assert c.newton_tolerance == 1e-8 and c.newton_max_iterations == 50
+    assert c.deviation_threshold == 1e-3 and c.kolmogorov_axis == 1
+
+
+def test_struct_sizes_match_header(lib):
+    """ctypes mirrors of the C structs have the C sizes (checked against a
+    tiny C program compiled with the header)."""
+    import subprocess, tempfile, pathlib
+    from metalbm_gb300 import capi
+    src = '#include <stdio.h>\n#include "mlbm/mlbm.h"\nint main(){printf("%zu %zu %zu %zu\\n", sizeof(mlbm_config), sizeof(mlbm_diag), sizeof(mlbm_mlp), sizeof(mlbm_train_cfg));return 0;}\n'
+    with tempfile.TemporaryDirectory() as td:
+        p = pathlib.Path(td)
+        (p / "s.c").write_text(src)
+        subprocess.run(["gcc", "-I", str(ROOT / "include"), str(p / "s.c"), "-o", str(p / "s")], check=True)
+        out = subprocess.run([str(p / "s")], capture_output=True, text=True, check=True).stdout.split()
+    assert [int(x) for x in out] == [ct.sizeof(capi.Config), ct.sizeof(capi.Diag),
+                                     ct.sizeof(capi.Mlp), ct.sizeof(capi.TrainCfg)]
+
+
+def test_create_reports_errors_without_aborting(lib):
+    from metalbm_gb300 import capi
+    c = capi.Config()
+    lib.mlbm_config_init(ct.byref(c))
+    c.relaxation_time = 0.4  # invalid: tau must exceed 1/2
+    h = ct.c_void_p()
+    assert lib.mlbm_create(ct.byref(c), ct.byref(h)) == capi.ERR_INVALID
+    assert b"relaxation time" in lib.mlbm_last_error(None)
+    assert lib.mlbm_create(None, ct.byref(h)) == capi.ERR_INVALID

@@ -1,0 +1,131 @@
+"""The learned alpha guess: GPU training kernels against the CPU oracle, the
+fused BF16 tensor-core inference against its restatement, and what the guess
+changes in the entropic step."""
+import numpy as np
+import pytest
+
+from oracle import mlp as mlp_oracle
+
+
+def synthetic(n_in=27, n=3000, seed=0):
+    rng = np.random.default_rng(seed)
+    X = (rng.standard_normal((n, n_in)) * 1e-3).astype(np.float32)
+    y = (2.0 + 0.05 * np.tanh(X[:, :5].sum(1) * 300.0)).astype(np.float32)
+    return X, y
+
+
+def model_for(X, y, seed=1):
+    from metalbm_gb300 import MlpModel
+    std = X.std(0)
+    return MlpModel.init(X.shape[1], (1.0 / std).astype(np.float32), float(np.std(y - 2)), seed)
+
+
+@pytest.fixture(scope="module")
+def lat():
+    from metalbm_gb300 import InputDeck, Lattice, build
+    build.build()
+    with Lattice(InputDeck(latticeT="D3Q27", globalLength=(4, 4, 4))) as L:
+        yield L
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("n_in", [9, 19, 27])
+def test_gradient_matches_cpu_oracle(lat, n_in):
+    X, y = synthetic(n_in, 2000)
+    m = model_for(X, y)
+    loss, g = lat.alpha_model_gradient(m, X, y)
+    ref_loss, ref = mlp_oracle.loss_and_grad(m, X, y)
+    assert abs(loss - ref_loss) <= 1e-5 * ref_loss
+    for k in ("w1", "b1", "w2", "b2", "w3"):
+        a, b = getattr(g, k), ref[k]
+        assert np.abs(a - b).max() <= 2e-4 * np.abs(b).max() + 1e-9, k
+    assert abs(g.b3 - ref["b3"]) <= 2e-4 * abs(ref["b3"]) + 1e-9
+
+
+@pytest.mark.gpu
+def test_gradient_matches_finite_differences(lat):
+    X, y = synthetic(27, 500, seed=3)
+    m = model_for(X, y, seed=4)
+    _, g = lat.alpha_model_gradient(m, X, y)
+    rng = np.random.default_rng(0)
+    for name in ("w1", "w2", "w3", "b1"):
+        arr = getattr(m, name)
+        for _ in range(4):
+            idx = tuple(rng.integers(0, s) for s in arr.shape)
+            h = 1e-3 * max(1.0, abs(float(arr[idx])))
+            old = float(arr[idx])
+            arr[idx] = old + h
+            lp = mlp_oracle.loss_only(m, X, y.astype(np.float64))
+            arr[idx] = old - h
+            lm = mlp_oracle.loss_only(m, X, y.astype(np.float64))
+            arr[idx] = old
+            fd = (lp - lm) / (2 * h)
+            assert abs(getattr(g, name)[idx] - fd) <= 1e-3 * abs(fd) + 1e-7
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("n_in", [9, 19, 27])
+def test_tensor_core_inference_matches_bf16_restatement(lat, n_in):
+    X, y = synthetic(n_in, 1000, seed=5)
+    m = model_for(X, y, seed=6)
+    got = lat.alpha_model_predict(m, X)
+    ref = mlp_oracle.predict_bf16(m, X)
+    assert np.abs(got - ref).max() <= 1e-4 * m.output_scale
+
+
+@pytest.mark.gpu
+def test_training_reduces_loss(lat):
+    X, y = synthetic(27, 20000, seed=7)
+    m0 = model_for(X, y, seed=8)
+    l0 = mlp_oracle.loss_only(m0, X, y.astype(np.float64))
+    m1, last = lat.train_alpha_model(X, y, m0, epochs=20, batch=2048, lr=3e-3)
+    l1 = mlp_oracle.loss_only(m1, X, y.astype(np.float64))
+    assert l1 < 0.2 * l0, (l0, l1, last)
+
+
+def _entropic_run(guess, model=None, steps=6, shape=(16, 12, 10)):
+    from metalbm_gb300 import InputDeck, Lattice, fields
+    rho, u = fields.taylor_green(shape, u0=0.08)
+    deck = InputDeck(latticeT="D3Q27", collisionT="ELBM", relaxationTime=0.50025,
+                     globalLength=shape, storage="f32", alphaSolver="residual",
+                     alphaGuess=guess, newtonTolerance=1e-12, deviationThreshold=0.0)
+    with Lattice(deck) as L:
+        if model is not None:
+            L.set_alpha_model(model)
+        L.init_equilibrium(rho, u)
+        L.step(steps, store=True)
+        return L.fields(), L.diagnostics()
+
+
+@pytest.mark.gpu
+def test_zero_model_equals_constant_two_guess():
+    """A model with zero weights outputs exactly 2: the fused inference path
+    then reproduces the constant-2 guess bit for bit."""
+    from metalbm_gb300 import MlpModel
+    z = MlpModel.init(27, np.ones(27, np.float32), 0.05, seed=0)
+    z.w1[:] = 0; z.w2[:] = 0; z.w3[:] = 0; z.b3 = 0.0
+    a, da = _entropic_run("learned", z)
+    b, db = _entropic_run("two")
+    assert np.array_equal(a["alpha"], b["alpha"]) and np.array_equal(a["u"], b["u"])
+    assert da["newton_iterations"] == db["newton_iterations"]
+
+
+@pytest.mark.gpu
+def test_learned_guess_saves_newton_iterations_at_equal_residual():
+    """Train on samples of a plain run, then run with the learned guess: the
+    residual test |F| <= 1e-12 holds for both, u agrees to 1e-6, and the
+    learned guess needs fewer Newton iterations than the constant-2 guess."""
+    from metalbm_gb300 import InputDeck, fields
+    from metalbm_gb300 import alpha_model
+    shape = (16, 12, 10)
+    rho, u = fields.taylor_green(shape, u0=0.08)
+    deck = InputDeck(latticeT="D3Q27", collisionT="ELBM", relaxationTime=0.50025,
+                     globalLength=shape, storage="f32", alphaSolver="residual",
+                     alphaGuess="two", newtonTolerance=1e-12, deviationThreshold=0.0)
+    X, y = alpha_model.collect_samples(deck, rho, u, steps=12, every=2, n_per_log=1500)
+    model, loss = alpha_model.fit(X, y, deck, epochs=60, batch=1024, lr=3e-3)
+    a, da = _entropic_run("learned", model)
+    b, db = _entropic_run("two")
+    assert da["fallback_nodes"] == 0 and db["fallback_nodes"] == 0
+    assert np.abs(a["u"] - b["u"]).max() <= 1e-6
+    assert da["newton_iterations"] < db["newton_iterations"], (da, db)

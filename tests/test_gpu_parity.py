@@ -1,0 +1,235 @@
+"""GPU parity of the fused pull step against the reference and the oracle.
+
+* FP64 BGK: bit-identical to the reference CPU build (golden vectors made by
+  the reference itself) for every lattice / forcing scheme / force case.
+* FP64 entropic (reference solver): within 1e-12 (max |a-b| / max |b|) of
+  the reference in f, rho and u; the only difference is CUDA's log against
+  the host libm's.
+* The C ABI calls below go through libmlbm.so; there is no CPU path.
+"""
+import json
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+
+CASES = sorted(p.stem for p in GOLDEN.glob("*.npz"))
+TOL_F64 = 1e-12
+
+
+def load(case):
+    z = np.load(GOLDEN / f"{case}.npz")
+    return {k: z[k] for k in z.files if k != "meta"}, json.loads(str(z["meta"]))
+
+
+def deck_for(meta, **kw):
+    from metalbm_gb300 import InputDeck
+    return InputDeck(latticeT=meta["lattice"], collisionT=meta["collision"],
+                     forcingSchemeT=meta["forcing"], forceT=meta["force"],
+                     relaxationTime=meta["tau"], forceAmplitude=tuple(meta["amp"]),
+                     forceWaveLength=tuple(meta["wavelength"]), globalLength=tuple(meta["size"]),
+                     **kw)
+
+
+def rel(a, b):
+    return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300))
+
+
+@pytest.fixture(scope="module", autouse=True)
+def built():
+    from metalbm_gb300 import build
+    build.build()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", CASES)
+def test_f64_matches_reference(case):
+    from metalbm_gb300 import Lattice
+    g, meta = load(case)
+    with Lattice(deck_for(meta)) as lat:
+        lat.init_equilibrium(g["rho0"], g["u0"])
+        lat.step(meta["steps"], store=True)
+        lat.sync(60000)
+        f = lat.populations()
+        fl = lat.fields()
+    if meta["collision"] == "BGK":
+        assert np.array_equal(f, g["f"]), rel(f, g["f"])
+        assert np.array_equal(fl["rho"], g["rho"])
+        assert np.array_equal(fl["u"], g["u"])
+        assert np.array_equal(fl["force"], g["force"])
+        assert np.array_equal(fl["alpha"], g["alpha"])
+    else:
+        assert rel(f, g["f"]) <= TOL_F64
+        assert rel(fl["rho"], g["rho"]) <= TOL_F64
+        assert rel(fl["u"], g["u"]) <= TOL_F64
+        assert np.array_equal(fl["force"], g["force"])
+        assert np.abs(fl["alpha"] - g["alpha"]).max() <= 1e-7
+
+
+@pytest.mark.gpu
+def test_reference_layout_roundtrip_and_algorithm_surface():
+    """unpack/pack in the reference's padded layout (Algorithm.h:132-147)
+    and iterate with isStored, against the oracle port."""
+    from metalbm_gb300 import Algorithm, InputDeck, Lattice
+    from oracle import OracleConfig, OraclePort
+    from metalbm_gb300 import fields
+    shape = (6, 5, 7)
+    rho, u = fields.perturbed_rest(shape, 3, 0.03, seed=3, rho_amplitude=0.01)
+    deck = InputDeck(latticeT="D3Q19", forcingSchemeT="Guo", forceT="Kolmogorov",
+                     relaxationTime=0.7, forceAmplitude=(1e-3, 0, 0),
+                     forceWaveLength=(5.0, 1, 1), globalLength=shape)
+    port = OraclePort(OracleConfig(lattice="D3Q19", forcing="Guo", force="Kolmogorov", tau=0.7,
+                                   amplitude=(1e-3, 0, 0), wavelength=(5.0, 1, 1), size=shape))
+    port.init_equilibrium(rho, u)
+    f0 = port.populations()
+    pz = 2 * (shape[2] // 2 + 1)
+    local = np.full((19, shape[0], shape[1], pz), -7.0)
+    local[..., :shape[2]] = f0.reshape(19, *shape)
+    with Lattice(deck) as lat:
+        alg = Algorithm(lat)
+        alg.unpack(local.reshape(19, -1))
+        for it in range(1, 4):
+            alg.isStored = it == 3
+            alg.iterate(it)
+        out = np.zeros_like(local).reshape(19, -1)
+        alg.pack(out)
+    port.step(3)
+    out = out.reshape(local.shape)
+    assert np.array_equal(out[..., :shape[2]].reshape(19, -1), port.populations())
+    assert (out[..., shape[2]:] == 0.0).all()  # padding untouched
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("lattice", ["D2Q9", "D3Q19", "D3Q27"])
+def test_kolmogorov_axis_parameter_matches_port(lattice):
+    """F_x(z) (force along the contiguous axis), not expressible in the
+    reference, against the port with the same axis parameter."""
+    from metalbm_gb300 import InputDeck, Lattice, fields
+    from oracle import OracleConfig, OraclePort
+    D = 2 if lattice == "D2Q9" else 3
+    shape = (8, 6, 10) if D == 3 else (8, 10, 1)
+    axis = D - 1
+    rho, u = fields.perturbed_rest(shape, D, 0.02, seed=5, rho_amplitude=0.01)
+    kw = dict(forceAmplitude=(1e-3, 0, 0), forceWaveLength=(5.0, 1, 1), globalLength=shape)
+    with Lattice(InputDeck(latticeT=lattice, forcingSchemeT="Guo", forceT="Kolmogorov",
+                           relaxationTime=0.6, kolmogorovAxis=axis, **kw)) as lat:
+        lat.init_equilibrium(rho, u)
+        lat.step(7, store=True)
+        f = lat.populations()
+    port = OraclePort(OracleConfig(lattice=lattice, forcing="Guo", force="Kolmogorov", tau=0.6,
+                                   amplitude=(1e-3, 0, 0), wavelength=(5.0, 1, 1), size=shape,
+                                   kolmogorov_axis=axis))
+    port.init_equilibrium(rho, u)
+    port.step(7)
+    assert np.array_equal(f, port.populations())
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("lattice,guess", [("D3Q27", "previous"), ("D3Q27", "two"),
+                                           ("D2Q9", "previous"), ("D3Q19", "two")])
+def test_residual_solver_matches_port(lattice, guess):
+    """The bracketed FP64 solver (|F| <= 1e-12, Newton + bisection-Newton)
+    against its restatement in the oracle."""
+    from metalbm_gb300 import InputDeck, Lattice, fields
+    from oracle import ALPHA_RESIDUAL, GUESS_PREVIOUS, GUESS_TWO, OracleConfig, OraclePort
+    D = 2 if lattice == "D2Q9" else 3
+    shape = (10, 8, 6) if D == 3 else (16, 12, 1)
+    rho, u = fields.perturbed_rest(shape, D, 0.06, seed=11, rho_amplitude=0.03)
+    kw = dict(tau=0.5005, size=shape)
+    with Lattice(InputDeck(latticeT=lattice, collisionT="ELBM", relaxationTime=0.5005,
+                           globalLength=shape, alphaSolver="residual", alphaGuess=guess,
+                           newtonTolerance=1e-12, deviationThreshold=0.0)) as lat:
+        lat.init_equilibrium(rho, u)
+        lat.step(6, store=True)
+        f = lat.populations()
+        fl = lat.fields()
+        d = lat.diagnostics()
+    port = OraclePort(OracleConfig(lattice=lattice, collision="ELBM", alpha_mode=ALPHA_RESIDUAL,
+                                   guess_mode=GUESS_TWO if guess == "two" else GUESS_PREVIOUS,
+                                   newton_tolerance=1e-12, deviation_threshold=0.0, **kw))
+    port.init_equilibrium(rho, u)
+    port.step(6)
+    assert rel(f, port.populations()) <= 1e-12
+    assert np.abs(fl["alpha"] - port.fields()["alpha"]).max() <= 1e-6
+    assert d["fallback_nodes"] == 0 and d["solved_nodes"] > 0
+
+
+@pytest.mark.gpu
+def test_diagnostics_match_fields():
+    from metalbm_gb300 import InputDeck, Lattice, fields
+    shape = (12, 10, 8)
+    rho, u = fields.perturbed_rest(shape, 3, 0.02, seed=2, rho_amplitude=0.01)
+    with Lattice(InputDeck(latticeT="D3Q19", forcingSchemeT="Guo", forceT="Kolmogorov",
+                           relaxationTime=0.6, forceAmplitude=(1e-3, 0, 0),
+                           forceWaveLength=(5.0, 1, 1), globalLength=shape)) as lat:
+        lat.init_equilibrium(rho, u)
+        lat.step(5, store=True, diagnostics=True)
+        fl = lat.fields()
+        d = lat.diagnostics()
+    e = (0.5 * fl["rho"] * (fl["u"] ** 2).sum(0)).sum() / fl["rho"].size
+    assert abs(d["energy"] - e) <= 1e-13 * e
+    assert abs(d["mass"] - fl["rho"].sum()) <= 1e-12 * fl["rho"].sum()
+    mach = np.sqrt(3 * (fl["u"] ** 2).sum(0)).max()
+    assert abs(d["max_mach"] - mach) <= 1e-14
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("storage,tol", [("f32", 2e-4), ("f16_shifted", 5e-3)])
+@pytest.mark.parametrize("lattice", ["D2Q9", "D3Q19", "D3Q27"])
+def test_low_precision_storage_tracks_f64(storage, tol, lattice):
+    """FP32 / FP16-shifted storage with FP32 collision against the FP64
+    kernel: the stored-population rounding bounds the error of u."""
+    from metalbm_gb300 import InputDeck, Lattice, fields
+    D = 2 if lattice == "D2Q9" else 3
+    shape = (16, 12, 10) if D == 3 else (32, 24, 1)
+    rho, u = fields.perturbed_rest(shape, D, 0.02, seed=4, rho_amplitude=0.005)
+    out = {}
+    for st in ("f64", storage):
+        with Lattice(InputDeck(latticeT=lattice, forcingSchemeT="Guo", forceT="Kolmogorov",
+                               relaxationTime=0.6, forceAmplitude=(1e-4, 0, 0),
+                               forceWaveLength=(8.0, 1, 1), globalLength=shape, storage=st)) as lat:
+            lat.init_equilibrium(rho, u)
+            lat.step(20, store=True)
+            out[st] = lat.fields()
+    assert rel(out[storage]["u"], out["f64"]["u"]) <= tol
+    assert rel(out[storage]["rho"], out["f64"]["rho"]) <= tol * 1e-2
+
+
+@pytest.mark.gpu
+def test_mixed_entropic_tracks_f64():
+    """FP32-storage entropic step (FP64 alpha solve) against the FP64 one."""
+    from metalbm_gb300 import InputDeck, Lattice, fields
+    shape = (16, 12, 10)
+    rho, u = fields.taylor_green(shape, u0=0.05)
+    out = {}
+    for st in ("f64", "f32"):
+        with Lattice(InputDeck(latticeT="D3Q27", collisionT="ELBM", relaxationTime=0.50025,
+                               globalLength=shape, storage=st, alphaSolver="residual",
+                               newtonTolerance=1e-12, deviationThreshold=0.0)) as lat:
+            lat.init_equilibrium(rho, u)
+            lat.step(10, store=True)
+            out[st] = lat.fields()
+            out[st + "_d"] = lat.diagnostics()
+    assert rel(out["f32"]["u"], out["f64"]["u"]) <= 1e-4
+    assert out["f32_d"]["fallback_nodes"] == 0
+
+
+@pytest.mark.gpu
+def test_error_word_and_timeout_paths():
+    """A NaN population sets the device error word (no trap); mlbm_sync
+    reports it as MLBM_ERR_NUMERIC and the context stays usable."""
+    from metalbm_gb300 import InputDeck, Lattice, MlbmError, capi
+    shape = (4, 4, 4)
+    with Lattice(InputDeck(latticeT="D3Q19", globalLength=shape)) as lat:
+        f = np.full((19, 64), 1.0 / 19)
+        f[3, 5] = np.nan
+        lat.set_populations(f)
+        lat.step(1)
+        with pytest.raises(MlbmError) as e:
+            lat.sync(10000)
+        assert e.value.code == capi.ERR_NUMERIC
+    with Lattice(InputDeck(latticeT="D3Q19", globalLength=shape)) as lat:
+        lat.set_populations(np.full((19, 64), 1.0 / 19))
+        lat.step(2)
+        lat.sync(10000)
