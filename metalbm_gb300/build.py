@@ -20,6 +20,7 @@ PKG = Path(__file__).resolve().parent
 CSRC = PKG / "csrc"
 BUILD = PKG / "_build"
 LIB = PKG / "libmlbm.so"
+ROUTINE = PKG / "routine_gpu"   # C++ Routine-shaped driver on include/mlbm/Algorithm_gpu.h
 INCLUDE = PKG.parent / "include"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -57,14 +58,26 @@ def _sources():
 
 def _deps():
     return sorted(CSRC.glob("*.cu")) + sorted(CSRC.glob("*.cuh")) + sorted(CSRC.glob("*.h")) + \
-        sorted(INCLUDE.glob("mlbm/*.h")) + [Path(__file__)]
+        sorted(INCLUDE.glob("mlbm/*.h")) + sorted((PKG / "cpp").glob("*.cpp")) + [Path(__file__)]
 
 
 def up_to_date() -> bool:
-    if not LIB.exists():
+    if not LIB.exists() or not ROUTINE.exists():
         return False
-    t = LIB.stat().st_mtime
+    t = min(LIB.stat().st_mtime, ROUTINE.stat().st_mtime)
     return all(p.stat().st_mtime < t for p in _deps())
+
+
+def build_routine() -> Path:
+    """The C++ host driver, linked against libmlbm.so (rpath $ORIGIN)."""
+    tmp = ROUTINE.with_name(f"routine_gpu.{os.getpid()}.tmp")
+    cmd = ["g++", "-O2", "-std=c++17", f"-I{INCLUDE}", str(PKG / "cpp" / "routine_gpu.cpp"),
+           f"-L{PKG}", "-lmlbm", "-Wl,-rpath,$ORIGIN", "-o", str(tmp)]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"building routine_gpu failed:\n{r.stderr[-4000:]}")
+    os.replace(tmp, ROUTINE)
+    return ROUTINE
 
 
 def _compile(unit) -> tuple[Path, str]:
@@ -94,6 +107,7 @@ def build(force: bool = False, verbose: bool = False) -> Path:
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stderr[-4000:]}")
     os.replace(tmp, LIB)
+    build_routine()
     if verbose:
         print(f"built {LIB}")
     return LIB

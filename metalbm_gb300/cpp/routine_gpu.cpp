@@ -1,0 +1,96 @@
+// Routine-shaped C++ host loop on mlbm::AlgorithmGPU (include/mlbm/Algorithm_gpu.h).
+//
+// The same driving sequence as metaLBM's Routine::compute (Routine.h:90-153)
+// with the GPU Algorithm dropped in: initial density and velocity in the
+// reference's padded FieldList layout, f = f_eq(rho, u), `steps` iterations
+// with isStored on the last one, then pack and storeFields.
+//
+// Usage: routine_gpu <in.bin> <out.bin> <steps> <lattice 0|1|2> <collision 0|1|2>
+//                    <forcing 0..3> <force 0..3> <tau> <ax> <ay> <az> <lx> <ly> <lz>
+//                    <Lx> <Ly> <Lz>
+//   in.bin : float64 rho[V], u[D][V] dense (index (x*Ly+y)*Lz+z)
+//   out.bin: float64 f[Q][V], rho[V], u[D][V], alpha[V], force[D][V], seconds
+#include <cstdio>
+#include <cstdlib>
+#include <vector>
+
+#include "mlbm/Algorithm_gpu.h"
+
+int main(int argc, char** argv) {
+  if (argc != 18) {
+    std::fprintf(stderr, "usage: see the header of routine_gpu.cpp\n");
+    return 2;
+  }
+  mlbm_config cfg;
+  mlbm_config_init(&cfg);
+  const int steps = std::atoi(argv[3]);
+  cfg.lattice = std::atoi(argv[4]);
+  cfg.collision = std::atoi(argv[5]);
+  cfg.forcing_scheme = std::atoi(argv[6]);
+  cfg.force = std::atoi(argv[7]);
+  cfg.relaxation_time = std::atof(argv[8]);
+  for (int d = 0; d < 3; ++d) {
+    cfg.force_amplitude[d] = std::atof(argv[9 + d]);
+    cfg.force_wavelength[d] = std::atof(argv[12 + d]);
+    cfg.length[d] = std::atoi(argv[15 + d]);
+  }
+  const int Q = cfg.lattice == MLBM_D2Q9 ? 9 : (cfg.lattice == MLBM_D3Q19 ? 19 : 27);
+  const int D = cfg.lattice == MLBM_D2Q9 ? 2 : 3;
+  const long lx = cfg.length[0], ly = cfg.length[1], lz = D == 2 ? 1 : cfg.length[2];
+  const long V = lx * ly * lz;
+  // reference local layout: last active dimension padded to 2*(N/2+1)
+  const long py = D == 2 ? 2 * (ly / 2 + 1) : ly, pz = D == 2 ? 1 : 2 * (lz / 2 + 1);
+  const long n = lx * py * pz;  // numberElements
+  auto ref = [&](long x, long y, long z) { return (x * py + y) * pz + z; };
+  auto dense = [&](long x, long y, long z) { return (x * ly + y) * lz + z; };
+
+  std::vector<double> in((size_t)(1 + D) * V);
+  FILE* fi = std::fopen(argv[1], "rb");
+  if (!fi || std::fread(in.data(), sizeof(double), in.size(), fi) != in.size()) return 3;
+  std::fclose(fi);
+  std::vector<double> density(n, 0.0), velocity((size_t)D * n, 0.0);
+  for (long x = 0; x < lx; ++x)
+    for (long y = 0; y < ly; ++y)
+      for (long z = 0; z < lz; ++z) {
+        density[ref(x, y, z)] = in[dense(x, y, z)];
+        for (int c = 0; c < D; ++c) velocity[c * n + ref(x, y, z)] = in[(1 + c) * V + dense(x, y, z)];
+      }
+
+  try {
+    mlbm::AlgorithmGPU algorithm(cfg);
+    algorithm.initialize(density.data(), velocity.data());
+    double seconds = 0.0;
+    for (int it = 1; it <= steps; ++it) {
+      algorithm.isStored = (it == steps);
+      algorithm.iterate(it);
+      seconds += algorithm.getComputationTime();
+    }
+    std::vector<double> distribution((size_t)Q * n, 0.0), alpha(n), force((size_t)D * n);
+    algorithm.pack(distribution.data());
+    algorithm.storeFields(density.data(), velocity.data(), alpha.data(), force.data());
+
+    std::vector<double> out((size_t)(Q + 1 + D + 1 + D) * V + 1);
+    for (long x = 0; x < lx; ++x)
+      for (long y = 0; y < ly; ++y)
+        for (long z = 0; z < lz; ++z) {
+          const long k = dense(x, y, z), r = ref(x, y, z);
+          for (int q = 0; q < Q; ++q) out[q * V + k] = distribution[q * n + r];
+          long o = (long)Q * V;
+          out[o + k] = density[r];
+          o += V;
+          for (int c = 0; c < D; ++c) out[o + c * V + k] = velocity[c * n + r];
+          o += (long)D * V;
+          out[o + k] = alpha[r];
+          o += V;
+          for (int c = 0; c < D; ++c) out[o + c * V + k] = force[c * n + r];
+        }
+    out.back() = seconds;
+    FILE* fo = std::fopen(argv[2], "wb");
+    if (!fo || std::fwrite(out.data(), sizeof(double), out.size(), fo) != out.size()) return 4;
+    std::fclose(fo);
+  } catch (const mlbm::Error& e) {
+    std::fprintf(stderr, "mlbm error %d: %s\n", e.code, e.what());
+    return 5;
+  }
+  return 0;
+}

@@ -201,6 +201,7 @@ cudaError_t MlpTrainer::set_data(const float* hX, const float* hy, long long nn)
   if ((e = dalloc((void**)&X, sizeof(float) * n * n_in)) || (e = dalloc((void**)&y, sizeof(float) * n)) ||
       (e = dalloc((void**)&perm, sizeof(long long) * n)))
     return e;
+  if ((e = cudaStreamSynchronize(s))) return e;
   if ((e = cudaMemcpy(X, hX, sizeof(float) * n * n_in, cudaMemcpyHostToDevice))) return e;
   return cudaMemcpy(y, hy, sizeof(float) * n, cudaMemcpyHostToDevice);
 }
@@ -250,7 +251,9 @@ cudaError_t MlpTrainer::gradient(long long nb, float* loss_out) {
   launches += 3;
   cudaError_t e = cudaGetLastError();
   if (e) return e;
-  return cudaMemcpy(loss_out, loss, sizeof(float), cudaMemcpyDeviceToHost);
+  // the kernels run on the handle's (non-blocking) stream
+  if ((e = cudaMemcpyAsync(loss_out, loss, sizeof(float), cudaMemcpyDeviceToHost, s))) return e;
+  return cudaStreamSynchronize(s);
 }
 
 cudaError_t MlpTrainer::train(const mlbm_train_cfg& cfg, float* last_loss) {
@@ -295,7 +298,9 @@ cudaError_t MlpTrainer::train(const mlbm_train_cfg& cfg, float* last_loss) {
 
 cudaError_t MlpTrainer::get_model(mlbm_mlp* out) {
   std::vector<float> th(mlp_param_count(n_in));
-  cudaError_t e = cudaMemcpy(th.data(), theta, sizeof(float) * th.size(), cudaMemcpyDeviceToHost);
+  cudaError_t e = cudaStreamSynchronize(s);
+  if (e) return e;
+  e = cudaMemcpy(th.data(), theta, sizeof(float) * th.size(), cudaMemcpyDeviceToHost);
   if (e) return e;
   *out = model;
   unpack(th, n_in, out);
@@ -304,7 +309,9 @@ cudaError_t MlpTrainer::get_model(mlbm_mlp* out) {
 
 cudaError_t MlpTrainer::get_gradient(mlbm_mlp* out) {
   std::vector<float> th(mlp_param_count(n_in));
-  cudaError_t e = cudaMemcpy(th.data(), grad, sizeof(float) * th.size(), cudaMemcpyDeviceToHost);
+  cudaError_t e = cudaStreamSynchronize(s);
+  if (e) return e;
+  e = cudaMemcpy(th.data(), grad, sizeof(float) * th.size(), cudaMemcpyDeviceToHost);
   if (e) return e;
   std::memset(out, 0, sizeof *out);
   out->n_in = n_in;
