@@ -236,6 +236,30 @@ const char* mlbm_last_error(const mlbm_handle* h);
 /* Number of CUDA kernels this library has launched in this process. */
 unsigned long long mlbm_kernel_launch_count(void);
 
+/* Allocation-free FP64 BGK step with fused diagnostics. No counterpart in the
+ * reference: it exists for callers that cannot allocate device memory (a host
+ * framework that owns every device allocation through its own pool, a step
+ * replayed where cudaMalloc is not allowed, an embedded fixed memory budget).
+ * It allocates nothing: f_in and f_out ([Q][V], dense, distinct) and
+ * force_profile are the caller's device buffers; the diagnostics scratch (one
+ * slot per 256-node block) is a static device array of 65,536 slots (2.5 MiB)
+ * that every GPU loading the library holds until the process exits, so
+ * lattices are limited to 16,777,216 nodes (256^3); larger ones return
+ * MLBM_ERR_INVALID. cfg must be BGK with FP64 storage. force_profile: the
+ * Kolmogorov profile A sin(2 pi i / lambda) over length[kolmogorov_axis]
+ * nodes, or for Sinusoidal the three per-axis profiles concatenated (x, y, z);
+ * NULL for None / Constant. Writes device diag_out[5] = {sum rho,
+ * sum 1/2 rho |u|^2 (divide by V for mlbm_diag.energy), max Mach, 2, 2} and,
+ * if non-NULL, the device error word to *error_word_out. Enqueued on
+ * `stream` (a cudaStream_t; NULL = legacy default stream) on the current
+ * device; returns before the work completes. The first call on a device looks
+ * up the scratch's device address (cudaGetSymbolAddress), so make it before
+ * any stream capture. Every call shares the scratch: calls that overlap on
+ * the GPU race. Errors: mlbm_last_error(NULL). */
+int mlbm_step_f64_noalloc(const mlbm_config* cfg, const double* f_in, double* f_out,
+                          const double* force_profile, double* diag_out,
+                          unsigned int* error_word_out, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

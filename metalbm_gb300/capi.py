@@ -31,7 +31,7 @@ EXPORTS = [
     "mlbm_get_diagnostics", "mlbm_sync", "mlbm_get_stream", "mlbm_set_stream",
     "mlbm_set_sample_nodes", "mlbm_get_samples", "mlbm_set_alpha_model",
     "mlbm_train_alpha_model", "mlbm_alpha_model_gradient", "mlbm_alpha_model_predict",
-    "mlbm_last_error", "mlbm_kernel_launch_count",
+    "mlbm_last_error", "mlbm_kernel_launch_count", "mlbm_step_f64_noalloc",
 ]
 
 
@@ -110,6 +110,7 @@ def load(path: Path | str | None = None):
         "mlbm_alpha_model_predict": ([vp, ct.POINTER(Mlp), fp, ct.c_longlong, fp], ct.c_int),
         "mlbm_last_error": ([vp], ct.c_char_p),
         "mlbm_kernel_launch_count": ([], ct.c_ulonglong),
+        "mlbm_step_f64_noalloc": ([ct.POINTER(Config), vp, vp, vp, vp, vp, vp], ct.c_int),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)

@@ -42,6 +42,11 @@ const double kPi = 3.14159265358979323846;
 
 namespace mlbm {
 void count_launches(unsigned n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+// Error message of a call made without a handle (mlbm_last_error(NULL)).
+void set_global_error(const char* message) {
+  std::lock_guard<std::mutex> lk(g_create_error_mutex);
+  g_create_error = message;
+}
 }  // namespace mlbm
 
 struct mlbm_handle {
