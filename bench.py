@@ -136,6 +136,24 @@ class ClockSampler:
 
 
 # ---------------------------------------------------------------------------
+def max_over_ranks(value: float, dist=None, device=None) -> float:
+    """The slowest rank's time: the timed region of every replica is
+    bracketed by barriers, and the job's time is the max over ranks."""
+    if dist is None:
+        return float(value)
+    import torch
+    t = torch.tensor([float(value)], dtype=torch.float64,
+                     device=device if device is not None else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_value(nodes_per_rank: int, steps: int, world: int, max_ms: float) -> float:
+    """Whole-job MLUPS: every rank advances its own replica of `nodes_per_rank`
+    nodes by `steps` steps; the job takes the slowest rank's time."""
+    return world * nodes_per_rank * steps / (max_ms * 1e-3) / 1e6
+
+
 def time_steps(lat, steps: int, torch, dist=None):
     """Time `steps` single-step calls with CUDA events on the handle's stream.
     Returns (total ms, list of per-launch ms)."""
@@ -249,10 +267,7 @@ def run_ours(args):
     lat.step(1, diagnostics=True)
     dl = lat.diagnostics()
     lat.close()
-    t = torch.tensor([total_ms], device=f"cuda:{local}")
-    if dist is not None:
-        dist.all_reduce(t, op=dist_mod.ReduceOp.MAX)
-    total_ms = float(t.item())
+    total_ms = max_over_ranks(total_ms, dist, f"cuda:{local}")
 
     # --- arm 2: plain Newton from the previous alpha, same state, same GPU
     if entropic:
@@ -263,11 +278,8 @@ def run_ours(args):
         lat.step(1, diagnostics=True)
         dn = lat.diagnostics()
         lat.close()
-        tn = torch.tensor([nt_ms], device=f"cuda:{local}")
-        if dist is not None:
-            dist.all_reduce(tn, op=dist_mod.ReduceOp.MAX)
-        nt_ms = float(tn.item())
-        newton_mlups = world * V * args.steps / (nt_ms * 1e-3) / 1e6
+        nt_ms = max_over_ranks(nt_ms, dist, f"cuda:{local}")
+        newton_mlups = job_value(V, args.steps, world, nt_ms)
         solved = max(dl["solved_nodes"], 1)
         extra = {
             "newton_alpha": {"value": newton_mlups, "unit": "MLUPS",
@@ -279,13 +291,13 @@ def run_ours(args):
                               "fallback_fraction": (dl["solved_nodes"] - dl["guess_hits"]) / solved,
                               "alpha2_fallback_nodes": dl["fallback_nodes"],
                               "model": model_src},
-            "speedup_learned_vs_newton": (V * args.steps / (total_ms * 1e-3) / 1e6 * world) / newton_mlups,
+            "speedup_learned_vs_newton": job_value(V, args.steps, world, total_ms) / newton_mlups,
             "newton_iterations_saved_per_solved_node":
                 dn["newton_iterations"] / max(dn["solved_nodes"], 1) - dl["newton_iterations"] / solved,
             "residual_tolerance": deck.newtonTolerance,
         }
 
-    value = world * V * args.steps / (total_ms * 1e-3) / 1e6
+    value = job_value(V, args.steps, world, total_ms)
     peaks, peak_src = measured_peaks()
     bpn = w["bytes_per_node"]
     avg_launch_ms = float(np.mean(per))
@@ -360,10 +372,7 @@ def run_e2e(name, deck, rho, u, model, steps, torch, dist, world):
     lat.sync()
     dt = time.perf_counter() - t0
     lat.close()
-    t = torch.tensor([dt], device="cuda")
-    if dist is not None:
-        dist.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-    dt = float(t.item())
+    dt = max_over_ranks(dt, dist, torch.device("cuda", torch.cuda.current_device()))
     h2d = (1 + D) * V * 8
     d2h_step = (1 + D) * V * 8 + 160
     return {"value": world * V * steps / dt / 1e6, "unit": "MLUPS",

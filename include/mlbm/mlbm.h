@@ -189,6 +189,13 @@ int mlbm_step(mlbm_handle* h, int nsteps, unsigned int flags);
 int mlbm_get_fields(mlbm_handle* h, double* rho, double* u, double* alpha, double* force,
                     int layout);
 
+/* The per-node alpha field [V] (FP64 on the host; FP32 on the device for
+ * FP32/FP16 storage): the guess the next entropic step starts from
+ * (Algorithm.h:103-106). For checkpoint / restart; the reference's restart
+ * re-initialises alpha to 2 (Initialize.h:82-89, 118-145). Synchronize. */
+int mlbm_get_alpha(mlbm_handle* h, double* alpha, int layout);
+int mlbm_set_alpha(mlbm_handle* h, const double* alpha, int layout);
+
 /* Diagnostics and solver counters of the last mlbm_step call. Synchronizes. */
 int mlbm_get_diagnostics(mlbm_handle* h, mlbm_diag* out);
 

@@ -24,7 +24,8 @@ ROUTINE = PKG / "routine_gpu"   # C++ Routine-shaped driver on include/mlbm/Algo
 INCLUDE = PKG.parent / "include"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
+COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
+          "--expt-relaxed-constexpr",
           "-Xptxas", "-v", f"-I{INCLUDE}", f"-I{CSRC}"]
 PER_FILE = {"step_f64.cu": ["-fmad=false"]}
 

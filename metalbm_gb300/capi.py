@@ -32,7 +32,9 @@ EXPORTS = [
     "mlbm_set_sample_nodes", "mlbm_get_samples", "mlbm_set_alpha_model",
     "mlbm_train_alpha_model", "mlbm_alpha_model_gradient", "mlbm_alpha_model_predict",
     "mlbm_last_error", "mlbm_kernel_launch_count", "mlbm_step_f64_noalloc",
+    "mlbm_get_alpha", "mlbm_set_alpha",
 ]
+TESTING_EXPORTS = ["mlbm_testing_fast_log"]
 
 
 class Config(ct.Structure):
@@ -97,6 +99,8 @@ def load(path: Path | str | None = None):
         "mlbm_step": ([vp, ct.c_int, ct.c_uint], ct.c_int),
         "mlbm_get_fields": ([vp, dp, dp, dp, dp, ct.c_int], ct.c_int),
         "mlbm_get_diagnostics": ([vp, ct.POINTER(Diag)], ct.c_int),
+        "mlbm_get_alpha": ([vp, dp, ct.c_int], ct.c_int),
+        "mlbm_set_alpha": ([vp, dp, ct.c_int], ct.c_int),
         "mlbm_sync": ([vp, ct.c_int], ct.c_int),
         "mlbm_get_stream": ([vp, ct.POINTER(vp)], ct.c_int),
         "mlbm_set_stream": ([vp, vp], ct.c_int),
@@ -111,6 +115,7 @@ def load(path: Path | str | None = None):
         "mlbm_last_error": ([vp], ct.c_char_p),
         "mlbm_kernel_launch_count": ([], ct.c_ulonglong),
         "mlbm_step_f64_noalloc": ([ct.POINTER(Config), vp, vp, vp, vp, vp, vp], ct.c_int),
+        "mlbm_testing_fast_log": ([dp, dp, ct.c_longlong], ct.c_int),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)

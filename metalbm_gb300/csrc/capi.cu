@@ -22,7 +22,9 @@
 #include <vector>
 
 #include "../../include/mlbm/mlbm.h"
+#include "../../include/mlbm/mlbm_testing.h"
 #include "kernels.h"
+#include "fastlog.cuh"
 #include "mlp_device.cuh"
 #include "mlp_train.h"
 
@@ -64,6 +66,7 @@ struct mlbm_handle {
   double* alpha = nullptr;      // FP64 storage
   float* alpha32 = nullptr;     // low-precision storage
   double* force_table[3] = {nullptr, nullptr, nullptr};
+  float* force_table_f[3] = {nullptr, nullptr, nullptr};
   double* partials = nullptr;
   int partial_blocks = 0;
   double* diag_dev = nullptr;
@@ -71,6 +74,7 @@ struct mlbm_handle {
   unsigned* err_word = nullptr;
   double* staging = nullptr;    // V doubles
   MlpDev* mlp = nullptr;
+  LogEntry* log_table = nullptr;
   bool have_model = false;
   long long* sample_nodes = nullptr;
   long long n_samples = 0;
@@ -226,8 +230,10 @@ extern "C" int mlbm_config_init(mlbm_config* c) {
 static void release(mlbm_handle* h) {
   if (!h) return;
   void* ptrs[] = {h->f[0], h->f[1], h->rho, h->u, h->force, h->alpha, h->alpha32,
-                  h->force_table[0], h->force_table[1], h->force_table[2], h->partials,
-                  h->diag_dev, h->counters, h->err_word, h->staging, h->mlp, h->sample_nodes,
+                  h->force_table[0], h->force_table[1], h->force_table[2], h->force_table_f[0],
+                  h->force_table_f[1], h->force_table_f[2], h->partials,
+                  h->diag_dev, h->counters, h->err_word, h->staging, h->mlp, h->log_table,
+                  h->sample_nodes,
                   h->sample_feat, h->sample_alpha, h->sample_solved};
   for (void* p : ptrs)
     if (p) cudaFree(p);
@@ -235,10 +241,38 @@ static void release(mlbm_handle* h) {
   delete h;
 }
 
+// Table of the FP64 logarithm (fastlog.cuh): for the centre c_j of each of
+// the 128 mantissa intervals, inv_j = RN(1/c_j) and -ln(inv_j) split into a
+// double-double, evaluated in the host's extended precision.
+static void make_log_table(LogEntry* t) {
+  for (int j = 0; j < LOG_TABLE; ++j) {
+    const double c = 1.0 + (j + 0.5) / (double)LOG_TABLE;
+    const double inv = 1.0 / c;
+    const long double L = -std::log((long double)inv);
+    const double hi = (double)L;
+    t[j].inv = inv;
+    t[j].hi = hi;
+    t[j].lo = (double)(L - (long double)hi);
+  }
+}
+
 static double host_sin_profile(double amplitude, unsigned i, double lambda) {
   // Force.h:213, 266: amplitude * sin(iP * 2 * M_PI / waveLength), with the
   // unsigned coordinate times 2 formed in integer arithmetic.
   return amplitude * std::sin((double)(i * 2u) * kPi / lambda);
+}
+
+static int fill_alpha(mlbm_handle* h, double value) {
+  std::vector<double> a64;
+  std::vector<float> a32;
+  if (h->alpha) {
+    a64.assign((size_t)h->V, value);
+    MLBM_CUDA(h, cudaMemcpy(h->alpha, a64.data(), sizeof(double) * h->V, cudaMemcpyHostToDevice));
+  } else {
+    a32.assign((size_t)h->V, (float)value);
+    MLBM_CUDA(h, cudaMemcpy(h->alpha32, a32.data(), sizeof(float) * h->V, cudaMemcpyHostToDevice));
+  }
+  return MLBM_OK;
 }
 
 extern "C" int mlbm_create(const mlbm_config* cfg, mlbm_handle** out) {
@@ -329,8 +363,17 @@ extern "C" int mlbm_create(const mlbm_config* cfg, mlbm_handle** out) {
       (rc = device_alloc(h, (void**)&h->diag_dev, sizeof(double) * DIAG_FIELDS)) ||
       (rc = device_alloc(h, (void**)&h->counters, sizeof(unsigned long long) * CNT_COUNT)) ||
       (rc = device_alloc(h, (void**)&h->err_word, sizeof(unsigned))) ||
-      (rc = device_alloc(h, (void**)&h->mlp, sizeof(MlpDev))))
+      (rc = device_alloc(h, (void**)&h->mlp, sizeof(MlpDev))) ||
+      (rc = device_alloc(h, (void**)&h->log_table, sizeof(LogEntry) * LOG_TABLE)))
     return bail(rc);
+  {
+    LogEntry tab[LOG_TABLE];
+    make_log_table(tab);
+    if (cudaMemcpy(h->log_table, tab, sizeof tab, cudaMemcpyHostToDevice) != cudaSuccess) {
+      h->error = "log table upload failed";
+      return bail(MLBM_ERR_CUDA);
+    }
+  }
   cudaMemsetAsync(h->f[0], 0, popBytes, h->stream);
   cudaMemsetAsync(h->f[1], 0, popBytes, h->stream);
   cudaMemsetAsync(h->rho, 0, sizeof(double) * V, h->stream);
@@ -350,9 +393,14 @@ extern "C" int mlbm_create(const mlbm_config* cfg, mlbm_handle** out) {
       std::vector<double> tab(n);
       for (long long i = 0; i < n; ++i)
         tab[i] = host_sin_profile(c.force_amplitude[comp], (unsigned)i, c.force_wavelength[comp]);
-      if ((rc = device_alloc(h, (void**)&h->force_table[t], sizeof(double) * n))) return bail(rc);
+      std::vector<float> tabf(tab.begin(), tab.end());
+      if ((rc = device_alloc(h, (void**)&h->force_table[t], sizeof(double) * n)) ||
+          (rc = device_alloc(h, (void**)&h->force_table_f[t], sizeof(float) * n)))
+        return bail(rc);
       if (cudaMemcpy(h->force_table[t], tab.data(), sizeof(double) * n, cudaMemcpyHostToDevice) !=
-          cudaSuccess) {
+              cudaSuccess ||
+          cudaMemcpy(h->force_table_f[t], tabf.data(), sizeof(float) * n, cudaMemcpyHostToDevice) !=
+              cudaSuccess) {
         h->error = "force table upload failed";
         return bail(MLBM_ERR_CUDA);
       }
@@ -391,7 +439,13 @@ extern "C" int mlbm_create(const mlbm_config* cfg, mlbm_handle** out) {
   p.kol_axis = c.kolmogorov_axis;
   p.kol_comp = c.kolmogorov_component;
   for (int d = 0; d < 3; ++d) p.amp[d] = d < D ? c.force_amplitude[d] : 0.0;
-  for (int t = 0; t < 3; ++t) p.force_table[t] = h->force_table[t];
+  for (int t = 0; t < 3; ++t) {
+    p.force_table[t] = h->force_table[t];
+    p.force_table_f[t] = h->force_table_f[t];
+    p.amp_f[t] = (float)p.amp[t];
+  }
+  p.bgk_b_f = (float)p.bgk_b;
+  p.guo_kt_f = (float)((1.0 - 1.0 / (2.0 * c.relaxation_time)) * 3.0);
   p.alpha_mode = c.alpha_mode;
   p.guess_mode = c.alpha_guess;
   p.newton_tol = c.newton_tolerance;
@@ -406,11 +460,15 @@ extern "C" int mlbm_create(const mlbm_config* cfg, mlbm_handle** out) {
   p.counters = h->counters;
   p.err_word = h->err_word;
   p.mlp = h->mlp;
+  p.log_table = h->log_table;
 
   if (cudaStreamSynchronize(h->stream) != cudaSuccess) {
     h->error = std::string("device initialisation failed: ") + cudaGetErrorString(cudaGetLastError());
     return bail(MLBM_ERR_CUDA);
   }
+  // alpha = 2 from construction on (initAlpha, Initialize.h:82-89), so a
+  // handle filled with mlbm_set_populations starts as the reference does
+  if ((rc = fill_alpha(h, 2.0))) return bail(rc);
   *out = h;
   return MLBM_OK;
 }
@@ -420,19 +478,6 @@ extern "C" int mlbm_destroy(mlbm_handle* h) {
   cudaSetDevice(h->cfg.device);
   cudaStreamSynchronize(h->stream);
   release(h);
-  return MLBM_OK;
-}
-
-static int fill_alpha(mlbm_handle* h, double value) {
-  std::vector<double> a64;
-  std::vector<float> a32;
-  if (h->alpha) {
-    a64.assign((size_t)h->V, value);
-    MLBM_CUDA(h, cudaMemcpy(h->alpha, a64.data(), sizeof(double) * h->V, cudaMemcpyHostToDevice));
-  } else {
-    a32.assign((size_t)h->V, (float)value);
-    MLBM_CUDA(h, cudaMemcpy(h->alpha32, a32.data(), sizeof(float) * h->V, cudaMemcpyHostToDevice));
-  }
   return MLBM_OK;
 }
 
@@ -619,6 +664,35 @@ extern "C" int mlbm_get_diagnostics(mlbm_handle* h, mlbm_diag* out) {
   return MLBM_OK;
 }
 
+extern "C" int mlbm_get_alpha(mlbm_handle* h, double* alpha, int layout) {
+  if (!h) return MLBM_ERR_INVALID;
+  if (!alpha || !valid_layout(layout)) return fail(h, MLBM_ERR_INVALID, "bad arguments");
+  MLBM_CUDA(h, cudaSetDevice(h->cfg.device));
+  MLBM_CUDA(h, cudaStreamSynchronize(h->stream));
+  if (h->alpha) return download(h, h->alpha, alpha, 1, layout);
+  std::vector<float> a((size_t)h->V);
+  std::vector<double> ad((size_t)h->V);
+  MLBM_CUDA(h, cudaMemcpy(a.data(), h->alpha32, sizeof(float) * h->V, cudaMemcpyDeviceToHost));
+  for (long long i = 0; i < h->V; ++i) ad[i] = a[i];
+  if (layout == MLBM_LAYOUT_DENSE) std::memcpy(alpha, ad.data(), sizeof(double) * h->V);
+  else ref_from_dense(h, ad.data(), alpha, 1);
+  return MLBM_OK;
+}
+
+extern "C" int mlbm_set_alpha(mlbm_handle* h, const double* alpha, int layout) {
+  if (!h) return MLBM_ERR_INVALID;
+  if (!alpha || !valid_layout(layout)) return fail(h, MLBM_ERR_INVALID, "bad arguments");
+  MLBM_CUDA(h, cudaSetDevice(h->cfg.device));
+  MLBM_CUDA(h, cudaStreamSynchronize(h->stream));
+  if (h->alpha) return upload(h, alpha, h->alpha, 1, layout);
+  std::vector<double> ad((size_t)h->V);
+  if (layout == MLBM_LAYOUT_DENSE) std::memcpy(ad.data(), alpha, sizeof(double) * h->V);
+  else dense_from_ref(h, alpha, ad.data(), 1);
+  std::vector<float> a(ad.begin(), ad.end());
+  MLBM_CUDA(h, cudaMemcpy(h->alpha32, a.data(), sizeof(float) * h->V, cudaMemcpyHostToDevice));
+  return MLBM_OK;
+}
+
 extern "C" int mlbm_get_stream(mlbm_handle* h, void** stream) {
   if (!h || !stream) return MLBM_ERR_INVALID;
   *stream = (void*)h->stream;
@@ -671,8 +745,9 @@ extern "C" int mlbm_get_samples(mlbm_handle* h, double* features, double* alpha,
 }
 
 // Host model -> device inference layout (BF16 weights, zero-padded inputs).
-static int upload_model(mlbm_handle* h, const mlbm_mlp* m, MlpDev* dst) {
-  if (m->n_in != h->Q || m->n_hidden != MLBM_MLP_HIDDEN)
+static int upload_model(mlbm_handle* h, const mlbm_mlp* m, MlpDev* dst, bool any_q = false) {
+  const bool q_ok = any_q ? (m->n_in == 9 || m->n_in == 19 || m->n_in == 27) : m->n_in == h->Q;
+  if (!q_ok || m->n_hidden != MLBM_MLP_HIDDEN)
     return fail(h, MLBM_ERR_INVALID, "model shape %d->%d does not match Q=%d, hidden=%d", m->n_in,
                 m->n_hidden, h->Q, MLBM_MLP_HIDDEN);
   MlpDev d;
@@ -716,7 +791,7 @@ extern "C" int mlbm_alpha_model_predict(mlbm_handle* h, const mlbm_mlp* m, const
     cudaFree(dm); cudaFree(dX);
     return rc;
   }
-  rc = upload_model(h, m, dm);
+  rc = upload_model(h, m, dm, true);
   if (!rc) {
     cudaMemcpy(dX, X, sizeof(float) * n * m->n_in, cudaMemcpyHostToDevice);
     cudaError_t e = mlp_predict(dm, m->n_in, dX, n, dA, h->stream);
@@ -780,4 +855,27 @@ extern "C" const char* mlbm_last_error(const mlbm_handle* h) {
 
 extern "C" unsigned long long mlbm_kernel_launch_count(void) {
   return g_launches.load(std::memory_order_relaxed);
+}
+
+extern "C" int mlbm_testing_fast_log(const double* x, double* out, long long n) {
+  if (!x || !out || n <= 0) return MLBM_ERR_INVALID;
+  LogEntry tab[LOG_TABLE];
+  make_log_table(tab);
+  void *dx = nullptr, *dout = nullptr, *dtab = nullptr;
+  if (cudaMalloc(&dx, sizeof(double) * n) != cudaSuccess ||
+      cudaMalloc(&dout, sizeof(double) * n) != cudaSuccess ||
+      cudaMalloc(&dtab, sizeof tab) != cudaSuccess) {
+    cudaFree(dx); cudaFree(dout); cudaFree(dtab);
+    cudaGetLastError();
+    return fail(nullptr, MLBM_ERR_ALLOC, "testing buffers");
+  }
+  cudaError_t e = cudaMemcpy(dx, x, sizeof(double) * n, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(dtab, tab, sizeof tab, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = fast_log_eval((const double*)dx, (double*)dout, n, dtab, 0);
+  count_launches(1);
+  if (e == cudaSuccess) e = cudaDeviceSynchronize();
+  if (e == cudaSuccess) e = cudaMemcpy(out, dout, sizeof(double) * n, cudaMemcpyDeviceToHost);
+  cudaFree(dx); cudaFree(dout); cudaFree(dtab);
+  if (e != cudaSuccess) return fail(nullptr, MLBM_ERR_CUDA, "fast log: %s", cudaGetErrorString(e));
+  return MLBM_OK;
 }

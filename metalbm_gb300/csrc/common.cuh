@@ -47,6 +47,13 @@ struct StepParams {
   int kol_axis, kol_comp;
   double amp[3];
   const double* force_table[3];  // per-axis host-computed sin profiles (device)
+  // float copies for the low-precision kernels, which execute no FP64
+  // instruction on their common path (a double->float conversion runs on
+  // GB300's narrow FP64 pipe)
+  const float* force_table_f[3];
+  float amp_f[3];
+  float bgk_b_f;             // 2 beta
+  float guo_kt_f;            // (1 - 1/(2 tau)) 3; S_q = kt w_q [...]
   // entropic solver
   int alpha_mode, guess_mode;
   double newton_tol;
@@ -64,6 +71,7 @@ struct StepParams {
   unsigned long long* counters;  // solver counters (see CNT_*)
   unsigned* err_word;
   const void* mlp;           // device MlpDev* (learned guess)
+  const void* log_table;     // device LogEntry[LOG_TABLE] (fastlog.cuh)
 };
 
 enum : int {

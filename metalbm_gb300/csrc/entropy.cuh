@@ -1,0 +1,61 @@
+// The entropy-balance function of the residual-mode alpha solve, shared by
+// the FP64-storage and FP32/FP16-storage entropic kernels.
+#pragma once
+
+#include "fastlog.cuh"
+#include "lattice.cuh"
+
+namespace mlbm {
+
+// Entropy-balance function in log1p form. With r_q = f_neq_q / f_q and
+// t_q = -x r_q (so g_q = f_q (1 + t_q)), ln(g_q/w_q) = L_q + log1p(t_q) where
+// L_q = ln(f_q/w_q), and F(x) = sum f ln(f/w) - sum g ln(g/w) of
+// EntropicStep.h:31-45 becomes
+//   F(x)  = x B1 - sum_q f_q (1 + t_q) log1p(t_q),   B1 = sum_q f_neq_q L_q,
+//   F'(x) = C0 + sum_q f_q r_q log1p(t_q),           C0 = sum_q f_neq_q + B1
+// (the derivative of EntropicStep.h:47-62). The L_q are computed once per node;
+// an evaluation then needs log1p of |t| <= 2^-6 only (a short series), with a
+// full logarithm only for larger deviations. The two sums are O(|f_neq|)
+// instead of the O(1) terms of the direct form, so F is also better
+// conditioned.
+template <int LAT>
+struct HLog1p {
+  const double* f;
+  const double* r;
+  double B1, C0;
+  const LogEntry* tab;
+  __device__ __forceinline__ void operator()(double x, double& Fv, double& Dv) const {
+    using L = Lattice<LAT>;
+    double s = 0.0, d = 0.0;
+#pragma unroll
+    for (int q = 0; q < L::Q; ++q) {
+      const double t = -x * r[q];
+      const double opt = 1.0 + t;
+      double lp;
+      if (fabs(t) <= 0.015625) lp = log1p_small(t);
+      else if (opt > 0.0) lp = fast_log(opt, tab);
+      else lp = -745.0;  // g = 0 at alpha_max: g ln g -> 0
+      if (opt > 0.0) s = fma(f[q] * opt, lp, s);
+      d = fma(f[q] * r[q], lp, d);
+    }
+    Fv = fma(x, B1, -s);
+    Dv = C0 + d;
+  }
+};
+
+// L_q, B1, C0 and r_q of a node (27 logarithms, 27 divisions).
+template <int LAT>
+__device__ __forceinline__ HLog1p<LAT> make_hlog1p(const double f[], const double fn[], double r[],
+                                                   const LogEntry* tab) {
+  using L = Lattice<LAT>;
+  double B1 = 0.0, sfn = 0.0;
+#pragma unroll
+  for (int q = 0; q < L::Q; ++q) {
+    B1 = fma(fn[q], fast_log(f[q] * (1.0 / L::w(q)), tab), B1);
+    sfn += fn[q];
+    r[q] = fn[q] / f[q];
+  }
+  return HLog1p<LAT>{f, r, B1, sfn + B1, tab};
+}
+
+}  // namespace mlbm

@@ -1,0 +1,85 @@
+// FP64 natural logarithm and log1p for the entropy function.
+//
+// ln(x), table-driven after P. T. P. Tang, "Table-driven implementation of
+// the logarithm function in IEEE floating-point arithmetic", ACM TOMS 16(4),
+// 1990: write x = 2^e m with m in [1, 2); j = the top 7 fraction bits of m;
+// inv_j = RN(1 / c_j) for the centre c_j = 1 + (j + 1/2)/128 of m's interval;
+// r = m inv_j - 1 with a single rounding (one FMA), |r| < 0.0045;
+// ln x = e ln2 + ln(1/inv_j) + log1p(r), with ln(1/inv_j) and ln2 held as
+// double-double constants and log1p(r) a degree-7 Taylor polynomial
+// (truncation < 2e-20). The absolute error is a few ulp of ln 2 for any
+// positive normal or subnormal x (the relative error grows only where
+// ln x -> 0, which the entropy sums, weighted by f ~ 1e-2, do not see).
+//
+// The table (128 x {inv, hi, lo}) is built on the host in extended precision
+// by make_log_table() and staged into shared memory by each block.
+#pragma once
+
+#include <stdint.h>
+
+namespace mlbm {
+
+constexpr int LOG_TABLE = 128;
+
+struct LogEntry {
+  double inv;  // RN(1 / c_j)
+  double hi;   // -ln(inv) = ln(1/inv), leading part
+  double lo;   // trailing part
+};
+
+// ln 2 split so that e * kLn2Hi is exact for |e| < 2^11 (kLn2Hi has 42
+// significant bits): kLn2Hi + kLn2Lo = ln 2 to ~1e-29.
+constexpr double kLn2Hi = 0x1.62e42fefa3800p-1;
+constexpr double kLn2Lo = 0x1.ef35793c76730p-45;
+
+// Degree-7 Taylor polynomial of log1p(r) = r - r^2/2 + r^3/3 - ... - r^8/8,
+// truncated after r^7 (|r| < 0.0045 gives |r|^8/8 < 2e-20).
+__device__ __forceinline__ double log1p_series7(double r) {
+  double p = 1.0 / 7.0;
+  p = fma(p, r, -1.0 / 6.0);
+  p = fma(p, r, 1.0 / 5.0);
+  p = fma(p, r, -1.0 / 4.0);
+  p = fma(p, r, 1.0 / 3.0);
+  p = fma(p, r, -0.5);
+  return fma(p * r, r, r);
+}
+
+// log1p(t) for |t| <= 2^-6 by its Taylor series to t^9 (truncation
+// |t|^10/10 < 1e-19 relative to t).
+__device__ __forceinline__ double log1p_small(double t) {
+  double p = 1.0 / 9.0;
+  p = fma(p, t, -1.0 / 8.0);
+  p = fma(p, t, 1.0 / 7.0);
+  p = fma(p, t, -1.0 / 6.0);
+  p = fma(p, t, 1.0 / 5.0);
+  p = fma(p, t, -1.0 / 4.0);
+  p = fma(p, t, 1.0 / 3.0);
+  p = fma(p, t, -0.5);
+  return fma(p * t, t, t);
+}
+
+// ln(x) for x > 0 (finite). `tab` is the shared-memory table.
+__device__ __forceinline__ double fast_log(double x, const LogEntry* tab) {
+  int64_t bits = __double_as_longlong(x);
+  int e = (int)((bits >> 52) & 0x7ff);
+  if (e == 0) {  // subnormal: scale by 2^54
+    bits = __double_as_longlong(x * 18014398509481984.0);
+    e = (int)((bits >> 52) & 0x7ff) - 54;
+  }
+  e -= 1023;
+  const int j = (int)((bits >> 45) & (LOG_TABLE - 1));
+  const double m = __longlong_as_double((bits & 0x000fffffffffffffLL) | 0x3ff0000000000000LL);
+  const LogEntry t = tab[j];
+  const double r = fma(m, t.inv, -1.0);
+  const double ed = (double)e;
+  const double hi = fma(ed, kLn2Hi, t.hi);  // exact product, one rounding in the sum
+  const double lo = fma(ed, kLn2Lo, t.lo) + log1p_series7(r);
+  return hi + lo;
+}
+
+// Block-cooperative staging of the table into shared memory.
+__device__ __forceinline__ void stage_log_table(LogEntry* sh, const LogEntry* __restrict__ g) {
+  for (int i = threadIdx.x; i < LOG_TABLE; i += blockDim.x) sh[i] = g[i];
+}
+
+}  // namespace mlbm

@@ -24,6 +24,10 @@ cudaError_t lowp_to_f64(int lattice, int storage, const void* f, int q, double* 
 cudaError_t f64_to_lowp(int lattice, int storage, const double* in, int q, void* f, long long V,
                         cudaStream_t s);
 
+// The FP64 logarithm of fastlog.cuh applied to x[0..n) (accuracy tests).
+cudaError_t fast_log_eval(const double* x, double* out, long long n, const void* table,
+                          cudaStream_t s);
+
 // Diagnostics: sum the per-block partials in a fixed order (deterministic).
 cudaError_t finalize_diag(const double* partials, int nblocks, double* out, cudaStream_t s);
 

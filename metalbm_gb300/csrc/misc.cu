@@ -2,6 +2,7 @@
 // the per-block diagnostics partials, and the sample-logger dispatch.
 
 #include "common.cuh"
+#include "fastlog.cuh"
 #include "kernels.h"
 
 namespace mlbm {
@@ -36,6 +37,22 @@ __global__ void finalize_diag_kernel(const double* __restrict__ partials, int nb
   }
   if (threadIdx.x == 0)
     for (int k = 0; k < DIAG_FIELDS; ++k) out[k] = sh[k][0];
+}
+
+__global__ void fast_log_kernel(const double* __restrict__ x, double* __restrict__ out, long long n,
+                                const LogEntry* __restrict__ table) {
+  __shared__ LogEntry tab[LOG_TABLE];
+  stage_log_table(tab, table);
+  __syncthreads();
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = fast_log(x[i], tab);
+}
+
+cudaError_t fast_log_eval(const double* x, double* out, long long n, const void* table,
+                          cudaStream_t s) {
+  fast_log_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(x, out, n,
+                                                             (const LogEntry*)table);
+  return cudaGetLastError();
 }
 
 cudaError_t finalize_diag(const double* partials, int nblocks, double* out, cudaStream_t s) {

@@ -16,6 +16,7 @@
 
 #include "common.cuh"
 #include "kernels.h"
+#include "entropy.cuh"
 #include "solver.cuh"
 
 namespace mlbm {
@@ -263,33 +264,12 @@ __device__ __forceinline__ bool newton_reference(const double f[], const double 
   return false;
 }
 
-// Residual-mode H function (the oracle's form): F = A - sum g ln(g/w),
-// F' = sum f_neq (1 + ln(g/w)), g = f - x f_neq, A = sum f ln(f/w).
-template <int LAT>
-struct HResidualF64 {
-  const double* f;
-  const double* fneq;
-  double A;
-  __device__ __forceinline__ void operator()(double x, double& Fv, double& Dv) const {
-    using L = Lattice<LAT>;
-    double S = 0.0, Dd = 0.0;
-#pragma unroll
-    for (int q = 0; q < L::Q; ++q) {
-      const double g = f[q] - x * fneq[q];
-      const double l = log((g > 0.0 ? g : 4.9406564584124654e-324) / L::w(q));
-      if (g > 0.0) S = S + g * l;
-      Dd = Dd + fneq[q] * (1 + l);
-    }
-    Fv = A - S;
-    Dv = Dd;
-  }
-};
-
 // ELBM::calculateAlpha (Collision.h:351-375) in either solver mode. c[] holds
 // the solver counters of this thread.
 template <int LAT>
 __device__ __forceinline__ double entropic_alpha(const StepParams& p, const double f[],
-                                                 const double fneq[], double guess, unsigned c[]) {
+                                                 const double fneq[], double guess, unsigned c[],
+                                                 const LogEntry* tab) {
   using L = Lattice<LAT>;
   bool small = true;
 #pragma unroll
@@ -320,10 +300,8 @@ __device__ __forceinline__ double entropic_alpha(const StepParams& p, const doub
     ++c[CNT_FALLBACK];
     return 2.0;
   }
-  double A = 0.0;
-#pragma unroll
-  for (int q = 0; q < L::Q; ++q) A = A + f[q] * log(f[q] / L::w(q));
-  const HResidualF64<LAT> ev{f, fneq, A};
+  double r[L::Q];
+  const HLog1p<LAT> ev = make_hlog1p<LAT>(f, fneq, r, tab);
   return residual_alpha_solve(ev, guess, guess, alphaMax, p.newton_tol, p.newton_maxit, c);
 }
 
@@ -331,6 +309,9 @@ template <int LAT, int FS>
 __global__ void __launch_bounds__(128) elbm_f64_kernel(const double* __restrict__ prev,
                                                        double* __restrict__ next, StepParams p) {
   using L = Lattice<LAT>;
+  __shared__ LogEntry s_log[LOG_TABLE];
+  stage_log_table(s_log, reinterpret_cast<const LogEntry*>(p.log_table));
+  __syncthreads();
   const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const bool active = idx < p.V;
   double mass = 0.0, energy = 0.0, mach = 0.0, amin = 1e300, amax = -1e300;
@@ -351,7 +332,7 @@ __global__ void __launch_bounds__(128) elbm_f64_kernel(const double* __restrict_
 #pragma unroll
     for (int q = 0; q < L::Q; ++q) fneq[q] = f[q] - fneq[q];
     const double guess = p.alpha_field[idx];
-    const double alpha = entropic_alpha<LAT>(p, f, fneq, guess, cnt);
+    const double alpha = entropic_alpha<LAT>(p, f, fneq, guess, cnt, s_log);
     const double tauEff = 1.0 / (alpha * p.beta);
     const double inv = 1.0 / tauEff;
     double fsh[FS == FS_EDM ? L::Q : 1];

@@ -20,6 +20,8 @@
 #include "common.cuh"
 #include "kernels.h"
 #include "mlp_device.cuh"
+#include "entropy.cuh"
+#include "fastlog.cuh"
 #include "solver.cuh"
 
 namespace mlbm {
@@ -175,24 +177,6 @@ __device__ __forceinline__ void eq_dev(float rhop, float rho, const float u[3], 
   }
 }
 
-template <int LAT, int FS>
-__device__ __forceinline__ float sourcef(const StepParams& p, int q, float rho, const float u[3],
-                                         const float F[3], const float ks[27]) {
-  using L = Lattice<LAT>;
-  if (FS == FS_GUO) {
-    // ((c - u) + 3 (c.u) c) . F  (ForcingScheme.h:110-116)
-    const float cu3 = 3.0f * cdotf<LAT>(q, u);
-    float R = 0.0f;
-#pragma unroll
-    for (int d = 0; d < L::D; ++d) {
-      const int c = L::c(q, d);
-      R = fmaf((float)c - u[d] + (float)c * cu3, F[d], R);
-    }
-    return ks[q] * R;
-  }
-  return 0.0f;
-}
-
 template <int LAT, int ST>
 __device__ __forceinline__ void pull_dev(const typename Storage<ST>::T* __restrict__ prev,
                                          long long V, const PullOffsets& o,
@@ -264,14 +248,45 @@ __device__ __forceinline__ void lowp_store_fields(const StepParams& p, long long
 }
 
 // ---- BGK ------------------------------------------------------------------
+// Per-node body force in float from the float profile tables.
+template <int D>
+__device__ __forceinline__ void node_force_float(const StepParams& p, uint32_t x, uint32_t y,
+                                                 uint32_t z, float F[3]) {
+  F[0] = 0.0f; F[1] = 0.0f; F[2] = 0.0f;
+  switch (p.force_type) {
+    case FORCE_CONSTANT:
+      F[0] = p.amp_f[0]; F[1] = p.amp_f[1]; F[2] = D == 3 ? p.amp_f[2] : 0.0f;
+      break;
+    case FORCE_SINUSOIDAL:
+      F[0] = __ldg(p.force_table_f[0] + x);
+      F[1] = __ldg(p.force_table_f[1] + y);
+      if (D == 3) F[2] = __ldg(p.force_table_f[2] + z);
+      break;
+    case FORCE_KOLMOGOROV: {
+      const uint32_t c = p.kol_axis == 0 ? x : (p.kol_axis == 1 ? y : z);
+      const float v = __ldg(p.force_table_f[0] + c);
+      F[0] = p.kol_comp == 0 ? v : 0.0f;
+      F[1] = p.kol_comp == 1 ? v : 0.0f;
+      F[2] = p.kol_comp == 2 ? v : 0.0f;
+      break;
+    }
+    default:
+      break;
+  }
+}
+
+// BGK in deviation variables (d = f - w):
+//   d' = d + 2 beta (d_eq - d) + S,   d_eq_q = w_q (rho' + rho P_q)
+// with the pair algebra P(+-cu) = E +- O of the TruncationMa3 polynomial and,
+// for Guo (ForcingScheme.h:100-117), S_q = kt w_q [(c_q - u).F + 3 (c_q.u)(c_q.F)]
+// = kt w_q (3 cu cF - u.F +- cF) for the pair; EDM: S_q = w_q rho (P_q(v) - P_q(u)),
+// v = u + F/rho (ForcingScheme.h:183-197).
 template <int LAT, int FS, int ST>
 __global__ void __launch_bounds__(256) bgk_lowp_kernel(const typename Storage<ST>::T* __restrict__ prev,
                                                        typename Storage<ST>::T* __restrict__ next,
                                                        StepParams p) {
   using L = Lattice<LAT>;
-  __shared__ float ks[27];
-  if (FS == FS_GUO && threadIdx.x < L::Q) ks[threadIdx.x] = (float)p.guo_k[threadIdx.x];
-  if (FS == FS_GUO) __syncthreads();
+  using T = typename Storage<ST>::T;
   const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const bool active = idx < p.V;
   double mass = 0.0, energy = 0.0, mach = 0.0;
@@ -283,58 +298,70 @@ __global__ void __launch_bounds__(256) bgk_lowp_kernel(const typename Storage<ST
     pull_dev<LAT, ST>(prev, p.V, o, d);
     float rhop, rho, u[3];
     moments_dev<LAT>(d, rhop, rho, u);
-    float Ff[3];
-    double F[3];
-    node_force_f<LAT>(p, x, y, z, Ff, F);
+    float F[3] = {0.0f, 0.0f, 0.0f};
+    if (FS != FS_NONE) node_force_float<L::D>(p, x, y, z, F);
     const float u2 = u[0] * u[0] + u[1] * u[1] + u[2] * u[2];
-    float deq[L::Q];
-    eq_dev<LAT>(rhop, rho, u, u2, deq);
-    float dsh[FS == FS_EDM ? L::Q : 1];
+    const PolyNode n = poly_node(u2);
+    const float b = p.bgk_b_f;
+    float uF = 0.0f, v[3] = {0.0f, 0.0f, 0.0f};
+    PolyNode nv = n;
+    if (FS == FS_GUO) uF = u[0] * F[0] + u[1] * F[1] + u[2] * F[2];
     if (FS == FS_EDM) {
-      const float inv = 1.0f / rho;
-      float v[3];
+      const float ir = 1.0f / rho;
 #pragma unroll
-      for (int k = 0; k < 3; ++k) v[k] = fmaf(Ff[k], inv, u[k]);
-      eq_dev<LAT>(rhop, rho, v, v[0] * v[0] + v[1] * v[1] + v[2] * v[2], dsh);
+      for (int k = 0; k < 3; ++k) v[k] = fmaf(F[k], ir, u[k]);
+      nv = poly_node(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
     }
-    const float b = (float)p.bgk_b;
+    T* out = next + idx;
+    {  // rest population
+      const float w = (float)L::w(0);
+      const float deq = w * fmaf(rho, n.common, rhop);
+      float r = fmaf(b, deq - d[0], d[0]);
+      if (FS == FS_GUO) r = fmaf(p.guo_kt_f * w, -uF, r);
+      if (FS == FS_EDM) r = fmaf(w * rho, nv.common - n.common, r);
+      Storage<ST>::template store<LAT>(out, 0, r);
+    }
 #pragma unroll
-    for (int q = 0; q < L::Q; ++q) {
-      float r = fmaf(b, deq[q] - d[q], d[q]);
-      if (FS == FS_GUO) r += sourcef<LAT, FS>(p, q, rho, u, Ff, ks);
-      if (FS == FS_EDM) r += dsh[q] - deq[q];
-      Storage<ST>::template store<LAT>(next + (long long)q * p.V + idx, q, r);
+    for (int q = 1; q < L::Q; ++q) {
+      if (is_pair_leader<LAT>(q)) {
+        const int qb = opposite<LAT>(q);
+        const float w = (float)L::w(q);
+        const float cu = cdotf<LAT>(q, u);
+        float E, O;
+        poly_pair(n, cu, E, O);
+        const float dq = w * fmaf(rho, E + O, rhop), dqb = w * fmaf(rho, E - O, rhop);
+        float rq = fmaf(b, dq - d[q], d[q]);
+        float rqb = fmaf(b, dqb - d[qb], d[qb]);
+        if (FS == FS_GUO) {
+          const float cF = cdotf<LAT>(q, F);
+          const float Es = fmaf(3.0f * cu, cF, -uF);
+          const float kw = p.guo_kt_f * w;
+          rq = fmaf(kw, Es + cF, rq);
+          rqb = fmaf(kw, Es - cF, rqb);
+        }
+        if (FS == FS_EDM) {
+          float Ev, Ov;
+          poly_pair(nv, cdotf<LAT>(q, v), Ev, Ov);
+          const float wr = w * rho;
+          rq = fmaf(wr, (Ev + Ov) - (E + O), rq);
+          rqb = fmaf(wr, (Ev - Ov) - (E - O), rqb);
+        }
+        Storage<ST>::template store<LAT>(out + (long long)q * p.V, q, rq);
+        Storage<ST>::template store<LAT>(out + (long long)qb * p.V, qb, rqb);
+      }
     }
     if (!(rho > 0.0f) || !isfinite(rho)) atomicOr(p.err_word, ERR_NONFINITE);
-    mass = (double)rho;
-    lowp_store_fields<LAT>(p, idx, rho, u, F, FS != FS_NONE, 2.0, energy, mach);
+    if (p.store || p.diag) {
+      double Fd[3];
+      node_force<L::D>(p, x, y, z, Fd);
+      if (p.diag) mass = (double)rho;
+      lowp_store_fields<LAT>(p, idx, rho, u, Fd, FS != FS_NONE, 2.0, energy, mach);
+    }
   }
   if (p.diag) block_reduce_diag(mass, energy, mach, 2.0, 2.0, p.diag_partials);
 }
 
 // ---- Entropic SRT with an FP64 alpha solve --------------------------------
-// F(alpha) = A - sum g ln(g/w), g = f - alpha f_neq, A = sum f ln(f/w)
-// (EntropicStep.h:31-45); F'(alpha) = sum f_neq (1 + ln(g/w)) (47-62).
-template <int LAT>
-struct HResidualMixed {
-  const double* f;
-  const double* fn;
-  double A;
-  __device__ __forceinline__ void operator()(double x, double& Fv, double& Dv) const {
-    using L = Lattice<LAT>;
-    double S = 0.0, Dd = 0.0;
-#pragma unroll
-    for (int q = 0; q < L::Q; ++q) {
-      const double g = f[q] - x * fn[q];
-      const double l = log((g > 0.0 ? g : 4.9406564584124654e-324) * (1.0 / L::w(q)));
-      if (g > 0.0) S = fma(g, l, S);
-      Dd = fma(fn[q], 1.0 + l, Dd);
-    }
-    Fv = A - S;
-    Dv = Dd;
-  }
-};
-
 // The alpha solve needs f_neq with the exact mass and momentum of the
 // stored state, so the entropic kernel widens the stored populations to FP64
 // and forms rho, u, f_eq and f_neq there; FP32 deviations would leave a
@@ -345,6 +372,9 @@ __global__ void __launch_bounds__(128) elbm_lowp_kernel(const typename Storage<S
                                                         typename Storage<ST>::T* __restrict__ next,
                                                         StepParams p) {
   using L = Lattice<LAT>;
+  __shared__ LogEntry s_log[LOG_TABLE];
+  stage_log_table(s_log, reinterpret_cast<const LogEntry*>(p.log_table));
+  __syncthreads();
   const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const bool active = idx < p.V;
   double mass = 0.0, energy = 0.0, mach = 0.0, amin = 1e300, amax = -1e300;
@@ -404,10 +434,8 @@ __global__ void __launch_bounds__(128) elbm_lowp_kernel(const typename Storage<S
       const double prevA = (double)p.alpha_field_f32[idx];
       const double plain = p.guess_mode == GUESS_TWO ? 2.0 : prevA;
       const double guess = LEARNED ? (double)learned : plain;
-      double A = 0.0;
-#pragma unroll
-      for (int q = 0; q < L::Q; ++q) A = fma(f[q], log(f[q] * (1.0 / L::w(q))), A);
-      const HResidualMixed<LAT> ev{f, fn, A};
+      double r[L::Q];
+      const HLog1p<LAT> ev = make_hlog1p<LAT>(f, fn, r, s_log);
       alpha = residual_alpha_solve(ev, guess, plain, alphaMax, p.newton_tol, p.newton_maxit, cnt);
     }
     const double ab = alpha * p.beta;

@@ -49,6 +49,11 @@ class InputDeck:
     deviationThreshold: float = 1e-3
     device: int = 0
 
+    def __post_init__(self):
+        self.forceAmplitude = tuple(self.forceAmplitude)
+        self.forceWaveLength = tuple(self.forceWaveLength)
+        self.globalLength = tuple(self.globalLength)
+
     @property
     def Q(self) -> int:
         return Q_OF[self.latticeT]
@@ -228,6 +233,40 @@ class Lattice:
         d = capi.Diag()
         self._check(self._lib.mlbm_get_diagnostics(self._h, ct.byref(d)))
         return d.as_dict()
+
+    def alpha(self) -> np.ndarray:
+        a = np.empty(self.V)
+        self._check(self._lib.mlbm_get_alpha(self._h, _dptr(a), capi.LAYOUT_DENSE))
+        return a
+
+    def set_alpha(self, alpha: np.ndarray):
+        a = np.ascontiguousarray(alpha, np.float64)
+        self._check(self._lib.mlbm_set_alpha(self._h, _dptr(a), capi.LAYOUT_DENSE))
+
+    # --- checkpoint / restart
+    def save_checkpoint(self, path) -> None:
+        """Populations (FP64, dense [Q][V]), the alpha field, the step count and
+        the deck, in one .npz (the reference writes the distribution with its
+        DistributionWriter, Writer.h:385-449, every backUpStep)."""
+        import json
+        from dataclasses import asdict
+        d = self.diagnostics()
+        np.savez(path, f=self.populations(), alpha=self.alpha(), step=np.int64(d["step"]),
+                 deck=np.array(json.dumps(asdict(self.deck))))
+
+    @staticmethod
+    def from_checkpoint(path, **deck_overrides) -> "Lattice":
+        """A lattice restored from save_checkpoint: populations and alpha as
+        saved (the reference's restart reads f and re-initialises alpha to 2,
+        Initialize.h:118-145; restoring alpha as well continues an entropic
+        run exactly)."""
+        import json
+        z = np.load(path)
+        deck = InputDeck(**{**json.loads(str(z["deck"])), **deck_overrides})
+        lat = Lattice(deck)
+        lat.set_populations(z["f"])
+        lat.set_alpha(z["alpha"])
+        return lat
 
     # --- sample logger and learned alpha
     def set_sample_nodes(self, nodes: np.ndarray):

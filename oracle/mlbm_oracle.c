@@ -226,34 +226,43 @@ static int newton(const hfun_t* h, double tol, int maxit, double* xR, double xMi
   return 0;
 }
 
-/* Residual-mode H-function: F = A - sum g ln(g/w) with A = sum f ln(f/w)
- * precomputed, and F' = sum f_neq (1 + ln(g/w)) from the same logarithms.
- * A population with g <= 0 (alpha at alpha_max) contributes its limit 0 to
- * g ln g; alpha_max keeps every other g positive. */
-static void h_residual(const hfun_t* h, double A, double alpha, double* F, double* dF) {
-  double S = 0.0, Dv = 0.0;
+/* Residual-mode entropy function in log1p form. With r = f_neq/f and
+ * t = -x r (g = f (1 + t)), ln(g/w) = L + log1p(t), L = ln(f/w), and
+ *   F(x)  = x B1 - sum f (1 + t) log1p(t),  B1 = sum f_neq L,
+ *   F'(x) = C0 + sum f r log1p(t),          C0 = sum f_neq + B1,
+ * the same function as sum f ln(f/w) - sum g ln(g/w) (EntropicStep.h:31-45)
+ * and its derivative (47-62), formed from O(|f_neq|) terms. */
+typedef struct {
+  const double* f;
+  const double* r;
+  double B1, C0;
+  int Q;
+} hlog1p_t;
+
+static void h_log1p(const hlog1p_t* h, double x, double* F, double* dF) {
+  double s = 0.0, d = 0.0;
   for (int q = 0; q < h->Q; ++q) {
-    const double g = h->f[q] - alpha * h->fneq[q];
-    if (g > 0.0) {
-      const double l = log(g / h->w[q]);
-      S += g * l;
-      Dv += h->fneq[q] * (1 + l);
-    } else {
-      Dv += h->fneq[q] * (1 + log(4.9406564584124654e-324 / h->w[q]));
-    }
+    const double t = -x * h->r[q];
+    const double opt = 1.0 + t;
+    double lp;
+    if (fabs(t) <= 0.015625) lp = log1p(t);
+    else if (opt > 0.0) lp = log(opt);
+    else lp = -745.0; /* g = 0 at alpha_max: g ln g -> 0 */
+    if (opt > 0.0) s = fma(h->f[q] * opt, lp, s);
+    d = fma(h->f[q] * h->r[q], lp, d);
   }
-  *F = A - S;
-  *dF = Dv;
+  *F = fma(x, h->B1, -s);
+  *dF = h->C0 + d;
 }
 
 /* Safeguarded bisection-Newton on [xMin, xMax], the update rule of
  * Bisection_NewtonRaphsonSolver (EntropicStep.h:142-220) with |F| <= tol as
  * the acceptance test. */
-static int bisection_newton_residual(const hfun_t* h, double A, double tol, int maxit,
-                                     double* xR, double xMin, double xMax, long long* iters) {
+static int bisection_newton_residual(const hlog1p_t* h, double tol, int maxit, double* xR,
+                                     double xMin, double xMax, long long* iters) {
   double fLow, fHigh, d;
-  h_residual(h, A, xMin, &fLow, &d);
-  h_residual(h, A, xMax, &fHigh, &d);
+  h_log1p(h, xMin, &fLow, &d);
+  h_log1p(h, xMax, &fHigh, &d);
   if ((fLow > 0.0 && fHigh > 0.0) || (fLow < 0.0 && fHigh < 0.0)) return 0;
   if (fabs(fLow) <= tol) { *xR = xMin; return 1; }
   if (fabs(fHigh) <= tol) { *xR = xMax; return 1; }
@@ -262,7 +271,7 @@ static int bisection_newton_residual(const hfun_t* h, double A, double tol, int 
   double x = 0.5 * (xMin + xMax);
   double dxOld = fabs(xMax - xMin), dx = dxOld;
   double fe, de;
-  h_residual(h, A, x, &fe, &de);
+  h_log1p(h, x, &fe, &de);
   for (int it = 1; it <= maxit; ++it) {
     if (fabs(fe) <= tol) { *xR = x; return 1; }
     ++*iters;
@@ -279,7 +288,7 @@ static int bisection_newton_residual(const hfun_t* h, double A, double tol, int 
       x -= dx;
       if (xTemp == x) { *xR = x; return 1; }
     }
-    h_residual(h, A, x, &fe, &de);
+    h_log1p(h, x, &fe, &de);
     if (fe < 0.0) xLow = x; else xHigh = x;
   }
   *xR = x;
@@ -287,25 +296,31 @@ static int bisection_newton_residual(const hfun_t* h, double A, double tol, int 
 }
 
 /* Residual-mode solve from a guess (see mlbm_oracle.h). */
-static double solve_residual(const hfun_t* h, double tol, int maxit, double guess, double xMax,
-                             long long* iters, long long* fallbacks, long long* bisections) {
-  double A = 0.0;
-  for (int q = 0; q < h->Q; ++q) A += h->f[q] * log(h->f[q] / h->w[q]);
+static double solve_residual(const double* f, const double* fneq, const double* w, int Q,
+                             double tol, int maxit, double guess, double xMax, long long* iters,
+                             long long* fallbacks, long long* bisections) {
+  double r[QMAX], B1 = 0.0, sfn = 0.0;
+  for (int q = 0; q < Q; ++q) {
+    B1 = fma(fneq[q], log(f[q] * (1.0 / w[q])), B1);
+    sfn += fneq[q];
+    r[q] = fneq[q] / f[q];
+  }
+  const hlog1p_t h = {f, r, B1, sfn + B1, Q};
   double x = guess;
   if (x > 1.0 && x < xMax) {
     double fe, de;
-    h_residual(h, A, x, &fe, &de);
+    h_log1p(&h, x, &fe, &de);
     if (fabs(fe) <= tol) return x;
     for (int it = 1; it <= maxit; ++it) {
       ++*iters;
       x -= fe / de;
       if (!(x > 1.0 && x < xMax)) break;
-      h_residual(h, A, x, &fe, &de);
+      h_log1p(&h, x, &fe, &de);
       if (fabs(fe) <= tol) return x;
     }
   }
   ++*bisections;
-  if (bisection_newton_residual(h, A, tol, maxit, &x, 1.0, xMax, iters)) return x;
+  if (bisection_newton_residual(&h, tol, maxit, &x, 1.0, xMax, iters)) return x;
   ++*fallbacks;
   return 2.0;
 }
@@ -332,8 +347,8 @@ static double entropic_alpha(const oracle_state* s, const double* f, const doubl
   const hfun_t h = {f, fneq, s->L.w, Q};
   if (c->guess_mode == ORACLE_GUESS_TWO) guess = 2.0;
   if (c->alpha_mode == ORACLE_ALPHA_RESIDUAL)
-    return solve_residual(&h, c->newton_tolerance, c->newton_max_iterations, guess, alphaMax,
-                          iters, fallbacks, bisections);
+    return solve_residual(f, fneq, s->L.w, Q, c->newton_tolerance, c->newton_max_iterations,
+                          guess, alphaMax, iters, fallbacks, bisections);
   double alpha = guess;
   if (newton(&h, c->newton_tolerance, c->newton_max_iterations, &alpha, 1., alphaMax, iters))
     return alpha;

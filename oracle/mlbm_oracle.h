@@ -34,7 +34,9 @@ enum { ORACLE_F_NONE = 0, ORACLE_F_CONSTANT = 1, ORACLE_F_SINUSOIDAL = 2, ORACLE
  *   of iterations, the safeguarded bisection-Newton of EntropicStep.h:142-220
  *   on [1, alpha_max] with the same residual test; alpha = 2 if both fail.
  *   F(alpha) = sum f ln(f/w) - sum g ln(g/w), g = f - alpha f_neq
- *   (EntropicStep.h:31-45), with sum f ln(f/w) formed once per node. */
+ *   (EntropicStep.h:31-45), evaluated as x B1 - sum f (1+t) log1p(t) with
+ *   t = -alpha f_neq/f and B1 = sum f_neq ln(f/w) (the same function, formed
+ *   from O(|f_neq|) terms; see mlbm_oracle.c). */
 enum { ORACLE_ALPHA_REFERENCE = 0, ORACLE_ALPHA_RESIDUAL = 1 };
 /* Starting guess: the node's alpha from the previous step (Algorithm.h:103-106)
  * or the constant 2. */

@@ -9,8 +9,8 @@ import pytest
 from conftest import ROOT
 
 
-def header_functions():
-    text = (ROOT / "include" / "mlbm" / "mlbm.h").read_text()
+def header_functions(name="mlbm.h"):
+    text = (ROOT / "include" / "mlbm" / name).read_text()
     text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
     return sorted(set(re.findall(r"\b(mlbm_[a-z_0-9]+)\s*\(", text)))
 
@@ -32,9 +32,11 @@ def test_header_declares_the_boundary():
 
 def test_library_exports_every_declared_symbol(lib):
     from metalbm_gb300 import capi
-    missing = [n for n in header_functions() if not hasattr(lib, n)]
+    missing = [n for n in header_functions() + header_functions("mlbm_testing.h")
+               if not hasattr(lib, n)]
     assert not missing, missing
     assert sorted(capi.EXPORTS) == header_functions()
+    assert sorted(capi.TESTING_EXPORTS) == header_functions("mlbm_testing.h")
 
 
 def test_config_defaults_are_the_reference_deck(lib):

@@ -177,7 +177,9 @@ def test_diagnostics_match_fields():
 @pytest.mark.gpu
 @pytest.mark.parametrize("storage,tol", [("f32", 2e-4), ("f16_shifted", 5e-3)])
 @pytest.mark.parametrize("lattice", ["D2Q9", "D3Q19", "D3Q27"])
-def test_low_precision_storage_tracks_f64(storage, tol, lattice):
+@pytest.mark.parametrize("forcing,force", [("Guo", "Kolmogorov"), ("ExactDifferenceMethod", "Sinusoidal"),
+                                           ("ShanChen", "Constant"), ("None", "None")])
+def test_low_precision_storage_tracks_f64(storage, tol, lattice, forcing, force):
     """FP32 / FP16-shifted storage with FP32 collision against the FP64
     kernel: the stored-population rounding bounds the error of u."""
     from metalbm_gb300 import InputDeck, Lattice, fields
@@ -186,14 +188,18 @@ def test_low_precision_storage_tracks_f64(storage, tol, lattice):
     rho, u = fields.perturbed_rest(shape, D, 0.02, seed=4, rho_amplitude=0.005)
     out = {}
     for st in ("f64", storage):
-        with Lattice(InputDeck(latticeT=lattice, forcingSchemeT="Guo", forceT="Kolmogorov",
-                               relaxationTime=0.6, forceAmplitude=(1e-4, 0, 0),
-                               forceWaveLength=(8.0, 1, 1), globalLength=shape, storage=st)) as lat:
+        with Lattice(InputDeck(latticeT=lattice, forcingSchemeT=forcing, forceT=force,
+                               relaxationTime=0.6, forceAmplitude=(1e-4, -5e-5, 2e-5),
+                               forceWaveLength=(8.0, 6.0, 5.0), globalLength=shape,
+                               storage=st)) as lat:
             lat.init_equilibrium(rho, u)
-            lat.step(20, store=True)
+            lat.step(20, store=True, diagnostics=True)
             out[st] = lat.fields()
+            out[st + "_d"] = lat.diagnostics()
     assert rel(out[storage]["u"], out["f64"]["u"]) <= tol
     assert rel(out[storage]["rho"], out["f64"]["rho"]) <= tol * 1e-2
+    assert np.array_equal(out[storage]["force"], out["f64"]["force"])
+    assert abs(out[storage + "_d"]["energy"] - out["f64_d"]["energy"]) <= 4 * tol * out["f64_d"]["energy"]
 
 
 @pytest.mark.gpu
@@ -265,3 +271,26 @@ def test_cpp_routine_drop_in(case, tmp_path):
         assert np.array_equal(f, g["f"]) and np.array_equal(rho, g["rho"])
     else:
         assert rel(f, g["f"]) <= TOL_F64 and rel(rho, g["rho"]) <= TOL_F64
+
+
+@pytest.mark.gpu
+def test_fast_log_accuracy():
+    """The entropic kernels' FP64 logarithm (Tang's table-driven method)
+    against the host libm: absolute error within a few ulp of ln 2, relative
+    error within 2 ulp away from x = 1."""
+    import ctypes as ct
+    from metalbm_gb300 import capi
+    lib = capi.load()
+    rng = np.random.default_rng(0)
+    x = np.concatenate([np.exp(rng.uniform(-700, 700, 200000)),
+                        rng.uniform(0.5, 2.0, 200000), 1.0 + rng.uniform(-1e-3, 1e-3, 50000),
+                        np.array([1.0, 2.0, 0.5, 5e-324, 1e-310, 1.7e308])])
+    out = np.empty_like(x)
+    dp = ct.POINTER(ct.c_double)
+    assert lib.mlbm_testing_fast_log(x.ctypes.data_as(dp), out.ctypes.data_as(dp), x.size) == 0
+    ref = np.log(x)
+    ulp_ln2 = np.spacing(np.log(2.0))
+    absbound = np.maximum(4 * ulp_ln2, 3 * np.spacing(np.abs(ref)))
+    assert (np.abs(out - ref) <= absbound).all(), np.abs(out - ref).max()
+    away = np.abs(ref) >= 0.5
+    assert (np.abs(out - ref)[away] <= 2 * np.spacing(np.abs(ref[away]))).all()

@@ -1,0 +1,100 @@
+"""Workflows of the drop-in on the GPU: the D2Q9 plain-method configuration
+end to end, checkpoint / restart, alpha state, bounded waits."""
+import numpy as np
+import pytest
+
+
+@pytest.mark.gpu
+def test_d2q9_kolmogorov_1000_steps_matches_oracle_with_diagnostics():
+    """BASELINE configuration [0]: D2Q9 BGK FP64, 256^2, tau 0.6, Guo,
+    Kolmogorov F_x(y) = 1e-5 sin(2 pi 4 y / 256), rho0 = 1, u ~ U[-1e-4, 1e-4]
+    (seed 0), f at equilibrium, 1000 steps; energy, enstrophy and max Mach
+    every 100 steps. The GPU state equals the oracle bit for bit at every
+    record; the fused energy / Mach reductions agree with the fields."""
+    from metalbm_gb300 import InputDeck, Lattice, fields, spectral
+    from oracle import OracleConfig, OraclePort
+    shape = (256, 256, 1)
+    rho, u = fields.perturbed_rest(shape, 2, 1e-4, seed=0)
+    deck = InputDeck(latticeT="D2Q9", forcingSchemeT="Guo", forceT="Kolmogorov", relaxationTime=0.6,
+                     forceAmplitude=(1e-5, 0, 0), forceWaveLength=(64.0, 1, 1),
+                     globalLength=(256, 256, 1))
+    port = OraclePort(OracleConfig(lattice="D2Q9", forcing="Guo", force="Kolmogorov", tau=0.6,
+                                   amplitude=(1e-5, 0, 0), wavelength=(64.0, 1, 1),
+                                   size=(256, 256, 1), threads=8))
+    port.init_equilibrium(rho, u)
+    records = []
+    with Lattice(deck) as lat:
+        lat.init_equilibrium(rho, u)
+        for rec in range(10):
+            lat.step(100, store=True, diagnostics=True)
+            port.step(100)
+            fl, d = lat.fields(), lat.diagnostics()
+            pf = port.fields()
+            assert np.array_equal(lat.populations(), port.populations())
+            assert np.array_equal(fl["u"], pf["u"]) and np.array_equal(fl["rho"], pf["rho"])
+            e = spectral.energy(pf["rho"], pf["u"])
+            assert abs(d["energy"] - e) <= 1e-13 * e
+            assert abs(d["max_mach"] - np.sqrt(3 * (pf["u"] ** 2).sum(0)).max()) <= 1e-15
+            records.append((100 * (rec + 1), d["energy"], spectral.enstrophy(fl["u"], shape),
+                            d["max_mach"]))
+    assert all(r[1] > 0 and r[2] > 0 for r in records)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("storage", ["f64", "f32"])
+def test_checkpoint_restart_continues_exactly(storage, tmp_path):
+    from metalbm_gb300 import InputDeck, Lattice, fields
+    shape = (12, 10, 8)
+    rho, u = fields.taylor_green(shape, u0=0.08)
+    deck = InputDeck(latticeT="D3Q27", collisionT="ELBM", relaxationTime=0.5005, globalLength=shape,
+                     storage=storage, alphaSolver="residual", newtonTolerance=1e-12,
+                     deviationThreshold=0.0)
+    with Lattice(deck) as a:
+        a.init_equilibrium(rho, u)
+        a.step(4)
+        a.save_checkpoint(tmp_path / "ck.npz")
+        a.step(4)
+        fa, aa = a.populations(), a.alpha()
+    with Lattice.from_checkpoint(tmp_path / "ck.npz") as b:
+        b.step(4)
+        assert np.array_equal(b.populations(), fa) and np.array_equal(b.alpha(), aa)
+
+
+@pytest.mark.gpu
+def test_alpha_starts_at_two_without_init_equilibrium():
+    """create + set_populations: the alpha guesses are 2 (initAlpha), so the
+    step equals the init_equilibrium path on the same populations."""
+    from metalbm_gb300 import InputDeck, Lattice, fields
+    shape = (10, 8, 6)
+    rho, u = fields.taylor_green(shape, u0=0.08)
+    deck = InputDeck(latticeT="D3Q27", collisionT="ELBM", relaxationTime=0.5005, globalLength=shape)
+    with Lattice(deck) as a:
+        a.init_equilibrium(rho, u)
+        f0 = a.populations()
+        a.step(3)
+        ref = a.populations()
+    with Lattice(deck) as b:
+        assert (b.alpha() == 2.0).all()
+        b.set_populations(f0)
+        b.step(3)
+        assert np.array_equal(b.populations(), ref)
+
+
+@pytest.mark.gpu
+def test_sync_gives_up_after_its_timeout():
+    """mlbm_sync returns MLBM_ERR_TIMEOUT when the work outlasts the limit,
+    leaves the handle usable, and a later unbounded sync succeeds."""
+    from metalbm_gb300 import InputDeck, Lattice, MlbmError, capi, fields
+    shape = (128, 128, 128)
+    rho, u = fields.taylor_green(shape, u0=0.05)
+    deck = InputDeck(latticeT="D3Q27", collisionT="ELBM", relaxationTime=0.5005, globalLength=shape,
+                     alphaSolver="residual", newtonTolerance=1e-12, deviationThreshold=0.0)
+    with Lattice(deck) as lat:
+        lat.init_equilibrium(rho, u)
+        lat.step(20)
+        with pytest.raises(MlbmError) as e:
+            lat.sync(1)
+        assert e.value.code == capi.ERR_TIMEOUT
+        lat.sync(-1)
+        lat.step(1, diagnostics=True)
+        assert lat.diagnostics()["solved_nodes"] > 0

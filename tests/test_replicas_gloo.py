@@ -1,0 +1,35 @@
+"""The N > 1 path of bench.py (independent replicas, one per rank): the job
+time is the max over ranks and the job value counts every rank's nodes.
+Two gloo ranks on the CPU."""
+import os
+
+import pytest
+
+
+def _worker(rank, world, port, q):
+    import torch.distributed as dist
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    import bench
+    t = bench.max_over_ranks(100.0 + 50.0 * rank, dist)
+    dist.barrier()
+    q.put((rank, t, bench.job_value(1000, 10, world, t)))
+    dist.destroy_process_group()
+
+
+def test_max_over_ranks_and_job_value_two_ranks():
+    import socket
+    import torch.multiprocessing as mp
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        port = s.getsockname()[1]
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    procs = [ctx.Process(target=_worker, args=(r, 2, port, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    out = sorted(q.get(timeout=120) for _ in procs)
+    for p in procs:
+        p.join(timeout=60)
+    assert [o[1] for o in out] == [150.0, 150.0]
+    assert out[0][2] == pytest.approx(2 * 1000 * 10 / 0.150 / 1e6)
