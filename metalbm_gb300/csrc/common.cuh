@@ -143,6 +143,31 @@ __device__ __forceinline__ void node_force(const StepParams& p, uint32_t x, uint
   }
 }
 
+// float -> double, exact, with integer operations: a conversion instruction
+// between FP32 and FP64 executes on the FP64 path, which GB300 narrows to a
+// small fraction of the FP32 rate. Valid for finite, normal, nonzero floats
+// (populations); anything else takes the conversion instruction.
+__device__ __forceinline__ double widen_exact(float v) {
+  const uint32_t b = __float_as_uint(v);
+  const uint32_t e = (b >> 23) & 0xffu;
+  if (e == 0u || e == 0xffu) return (double)v;
+  const uint32_t hi = (b & 0x80000000u) | (((b & 0x7fffffffu) >> 3) + (896u << 20));
+  const uint32_t lo = b << 29;
+  return __hiloint2double((int)hi, (int)lo);
+}
+
+// double -> float, round to nearest even, with integer operations (same
+// reason); results outside the normal float range take the instruction.
+__device__ __forceinline__ float narrow_rn(double x) {
+  const uint32_t hi = (uint32_t)__double2hiint(x), lo = (uint32_t)__double2loint(x);
+  const uint32_t e = (hi >> 20) & 0x7ffu;
+  if (e <= 896u || e >= 1151u) return (float)x;  // not a normal float after rounding
+  uint32_t bits = ((((hi & 0x7fffffffu) - (896u << 20)) << 3) | (lo >> 29));
+  const uint32_t rem = lo & 0x1fffffffu;
+  bits += (rem > 0x10000000u || (rem == 0x10000000u && (bits & 1u))) ? 1u : 0u;
+  return __uint_as_float(bits | (hi & 0x80000000u));
+}
+
 // Warp + block reduction of the diagnostics, written to partials[blockIdx.x].
 __device__ __forceinline__ void block_reduce_diag(double mass, double energy, double mach,
                                                   double amin, double amax, double* partials) {

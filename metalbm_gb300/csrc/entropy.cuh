@@ -23,20 +23,32 @@ struct HLog1p {
   const double* f;
   const double* r;
   double B1, C0;
+  double rmax;  // max_q |r_q|
   const LogEntry* tab;
   __device__ __forceinline__ void operator()(double x, double& Fv, double& Dv) const {
     using L = Lattice<LAT>;
     double s = 0.0, d = 0.0;
+    if (x * rmax <= 0.0009765625) {
+      // every |t| <= 2^-10: degree-5 series, truncation < |t|^6/6 < 3e-19
 #pragma unroll
-    for (int q = 0; q < L::Q; ++q) {
-      const double t = -x * r[q];
-      const double opt = 1.0 + t;
-      double lp;
-      if (fabs(t) <= 0.015625) lp = log1p_small(t);
-      else if (opt > 0.0) lp = fast_log(opt, tab);
-      else lp = -745.0;  // g = 0 at alpha_max: g ln g -> 0
-      if (opt > 0.0) s = fma(f[q] * opt, lp, s);
-      d = fma(f[q] * r[q], lp, d);
+      for (int q = 0; q < L::Q; ++q) {
+        const double t = -x * r[q];
+        const double lp = log1p_tiny(t);
+        s = fma(fma(f[q], t, f[q]), lp, s);
+        d = fma(f[q] * r[q], lp, d);
+      }
+    } else {
+#pragma unroll
+      for (int q = 0; q < L::Q; ++q) {
+        const double t = -x * r[q];
+        const double opt = 1.0 + t;
+        double lp;
+        if (fabs(t) <= 0.015625) lp = log1p_small(t);
+        else if (opt > 0.0) lp = fast_log(opt, tab);
+        else lp = -745.0;  // g = 0 at alpha_max: g ln g -> 0
+        if (opt > 0.0) s = fma(f[q] * opt, lp, s);
+        d = fma(f[q] * r[q], lp, d);
+      }
     }
     Fv = fma(x, B1, -s);
     Dv = C0 + d;
@@ -48,14 +60,30 @@ template <int LAT>
 __device__ __forceinline__ HLog1p<LAT> make_hlog1p(const double f[], const double fn[], double r[],
                                                    const LogEntry* tab) {
   using L = Lattice<LAT>;
-  double B1 = 0.0, sfn = 0.0;
+  double B1 = 0.0, sfn = 0.0, rmax = 0.0;
 #pragma unroll
   for (int q = 0; q < L::Q; ++q) {
     B1 = fma(fn[q], fast_log(f[q] * (1.0 / L::w(q)), tab), B1);
     sfn += fn[q];
     r[q] = fn[q] / f[q];
+    rmax = fmax(rmax, fabs(r[q]));
   }
-  return HLog1p<LAT>{f, r, B1, sfn + B1, tab};
+  return HLog1p<LAT>{f, r, B1, sfn + B1, rmax, tab};
+}
+
+// The same with r_q given (the caller already formed them).
+template <int LAT>
+__device__ __forceinline__ HLog1p<LAT> make_hlog1p_r(const double f[], const double fn[],
+                                                     const double r[], double rmax,
+                                                     const LogEntry* tab) {
+  using L = Lattice<LAT>;
+  double B1 = 0.0, sfn = 0.0;
+#pragma unroll
+  for (int q = 0; q < L::Q; ++q) {
+    B1 = fma(fn[q], fast_log(f[q] * (1.0 / L::w(q)), tab), B1);
+    sfn += fn[q];
+  }
+  return HLog1p<LAT>{f, r, B1, sfn + B1, rmax, tab};
 }
 
 }  // namespace mlbm

@@ -58,6 +58,16 @@ __device__ __forceinline__ double log1p_small(double t) {
   return fma(p * t, t, t);
 }
 
+// log1p(t) for |t| <= 2^-10 by its Taylor series to t^5 (truncation
+// |t|^6/6 < 3e-19).
+__device__ __forceinline__ double log1p_tiny(double t) {
+  double p = 1.0 / 5.0;
+  p = fma(p, t, -1.0 / 4.0);
+  p = fma(p, t, 1.0 / 3.0);
+  p = fma(p, t, -0.5);
+  return fma(p * t, t, t);
+}
+
 // ln(x) for x > 0 (finite). `tab` is the shared-memory table.
 __device__ __forceinline__ double fast_log(double x, const LogEntry* tab) {
   int64_t bits = __double_as_longlong(x);

@@ -55,11 +55,12 @@ __device__ __forceinline__ double residual_alpha_solve(const Eval& eval, double 
       phase = P_LOW;
     } else if (phase == P_LOW) {
       fLow = fe;
-      if (fabs(fe) <= tol) { result = 1.0; ok = true; phase = P_DONE; continue; }
       x = alphaMax;
       phase = P_HIGH;
     } else if (phase == P_HIGH) {
+      // bracket check before either end is accepted (EntropicStep.h:151-164)
       if ((fLow > 0.0 && fe > 0.0) || (fLow < 0.0 && fe < 0.0)) { phase = P_DONE; continue; }
+      if (fabs(fLow) <= tol) { result = 1.0; ok = true; phase = P_DONE; continue; }
       if (fabs(fe) <= tol) { result = alphaMax; ok = true; phase = P_DONE; continue; }
       if (fLow < 0.0) { xLow = 1.0; xHigh = alphaMax; } else { xLow = alphaMax; xHigh = 1.0; }
       x = 0.5 * (1.0 + alphaMax);

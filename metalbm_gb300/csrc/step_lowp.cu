@@ -379,16 +379,47 @@ __global__ void __launch_bounds__(128) elbm_lowp_kernel(const typename Storage<S
   const bool active = idx < p.V;
   double mass = 0.0, energy = 0.0, mach = 0.0, amin = 1e300, amax = -1e300;
   unsigned cnt[CNT_COUNT] = {0, 0, 0, 0, 0, 0, 0, 0};
-  double f[L::Q], fn[L::Q], rho = 1.0, u[3] = {0.0, 0.0, 0.0}, F[3] = {0.0, 0.0, 0.0};
-  if (active) {
-    uint32_t x, y, z;
-    node_coords(p, idx, x, y, z);
-    const PullOffsets o = pull_offsets(p, x, y, z);
+  double f[L::Q];
+  uint32_t x = 0, y = 0, z = 0;
+  float learned = 2.0f;
+  {
+    float dv[L::Q];  // FP32 deviations f - w (model features)
+    if (active) {
+      node_coords(p, idx, x, y, z);
+      const PullOffsets o = pull_offsets(p, x, y, z);
 #pragma unroll
-    for (int q = 0; q < L::Q; ++q)
-      f[q] = load_f64<LAT, ST>(prev + (long long)q * p.V + o.at(L::c(q, 0), L::c(q, 1), L::c(q, 2)), q);
-    rho = f[0];
-    double j[3] = {0.0, 0.0, 0.0};
+      for (int q = 0; q < L::Q; ++q) {
+        const auto* src = prev + (long long)q * p.V + o.at(L::c(q, 0), L::c(q, 1), L::c(q, 2));
+        if constexpr (ST == ST_F32) {
+          const float v = __ldg(src);
+          f[q] = widen_exact(v);  // exact, without a conversion instruction
+          dv[q] = v - (float)L::w(q);
+        } else {
+          const float dev = __half2float(__ldg(src)) * (1.0f / (float)(1 << shift_exponent<LAT>(q)));
+          f[q] = L::w(q) + widen_exact(dev);
+          dv[q] = dev;
+        }
+      }
+    } else {
+#pragma unroll
+      for (int q = 0; q < L::Q; ++q) { f[q] = L::w(q); dv[q] = 0.0f; }
+    }
+    // Learned guess: every thread of the block takes part (tile inference),
+    // on features f_neq / rho from the FP32 deviations (the BF16 inference
+    // does not need FP64 inputs).
+    if (LEARNED) {
+      float rhop, rf, uf[3], deq[L::Q];
+      moments_dev<LAT>(dv, rhop, rf, uf);
+      eq_dev<LAT>(rhop, rf, uf, uf[0] * uf[0] + uf[1] * uf[1] + uf[2] * uf[2], deq);
+      const float irf = 1.0f / rf;
+      float xin[L::Q];
+#pragma unroll
+      for (int q = 0; q < L::Q; ++q) xin[q] = (dv[q] - deq[q]) * irf;
+      learned = mlp_guess_block<L::Q>(reinterpret_cast<const MlpDev*>(p.mlp), xin);
+    }
+  }
+  if (active) {
+    double rho = f[0], j[3] = {0.0, 0.0, 0.0}, u[3], F[3] = {0.0, 0.0, 0.0};
 #pragma unroll
     for (int q = 1; q < L::Q; ++q) {
       rho += f[q];
@@ -401,45 +432,39 @@ __global__ void __launch_bounds__(128) elbm_lowp_kernel(const typename Storage<S
     const double ir = 1.0 / rho;
 #pragma unroll
     for (int k = 0; k < 3; ++k) u[k] = j[k] * ir;
-    node_force<L::D>(p, x, y, z, F);
-    feq_pairs_f64<LAT>(rho, u, fn);
-#pragma unroll
-    for (int q = 0; q < L::Q; ++q) fn[q] = f[q] - fn[q];
-  } else {
-#pragma unroll
-    for (int q = 0; q < L::Q; ++q) { f[q] = L::w(q); fn[q] = 0.0; }
-  }
-  // Learned guess: every thread of the block takes part (tile inference).
-  float learned = 2.0f;
-  if (LEARNED) {
-    float xin[L::Q];
-    const double ir = 1.0 / rho;
-#pragma unroll
-    for (int q = 0; q < L::Q; ++q) xin[q] = (float)(fn[q] * ir);
-    learned = mlp_guess_block<L::Q>(reinterpret_cast<const MlpDev*>(p.mlp), xin);
-  }
-  if (active) {
-    bool small = true;
-    double alphaMax = 2.5;
+    if (FS != FS_NONE) node_force<L::D>(p, x, y, z, F);
+    // r_q = f_neq_q / f_q; alpha_max = min(2.5, 1 / max_q r_q) over r_q > 0
+    // (Collision.h:305-326); the deviation test |f_neq|/f <= threshold
+    // (Collision.h:284-303) on |r_q|.
+    double r[L::Q], rpos = 0.0, rabs = 0.0;
+    feq_pairs_f64<LAT>(rho, u, r);
 #pragma unroll
     for (int q = 0; q < L::Q; ++q) {
-      if (fabs(fn[q]) > p.deviation_threshold * f[q]) small = false;
-      if (fn[q] > 0.0) alphaMax = fmin(alphaMax, f[q] / fn[q]);
+      r[q] = (f[q] - r[q]) / f[q];
+      rpos = fmax(rpos, r[q]);
+      rabs = fmax(rabs, fabs(r[q]));
     }
+    const bool small = !(rabs > p.deviation_threshold);
+    const double alphaMax = rpos > 0.4 ? 1.0 / rpos : 2.5;
     double alpha;
     if (small) { ++cnt[CNT_SHORTCUT]; alpha = 2.0; }
     else if (alphaMax < 2.0) { ++cnt[CNT_LIMITED]; alpha = 0.95 * alphaMax; }
     else {
       ++cnt[CNT_SOLVED];
-      const double prevA = (double)p.alpha_field_f32[idx];
+      const double prevA = widen_exact(p.alpha_field_f32[idx]);
       const double plain = p.guess_mode == GUESS_TWO ? 2.0 : prevA;
-      const double guess = LEARNED ? (double)learned : plain;
-      double r[L::Q];
-      const HLog1p<LAT> ev = make_hlog1p<LAT>(f, fn, r, s_log);
+      const double guess = LEARNED ? widen_exact(learned) : plain;
+      double B1 = 0.0, sfn = 0.0;
+#pragma unroll
+      for (int q = 0; q < L::Q; ++q) {
+        const double fnq = r[q] * f[q];
+        B1 = fma(fnq, fast_log(f[q] * (1.0 / L::w(q)), s_log), B1);
+        sfn += fnq;
+      }
+      const HLog1p<LAT> ev{f, r, B1, sfn + B1, rabs, s_log};
       alpha = residual_alpha_solve(ev, guess, plain, alphaMax, p.newton_tol, p.newton_maxit, cnt);
     }
     const double ab = alpha * p.beta;
-    double Fs[3] = {F[0], F[1], F[2]};
     double fsh[FS == FS_EDM ? L::Q : 1];
     if (FS == FS_EDM) {
       double v[3];
@@ -449,8 +474,9 @@ __global__ void __launch_bounds__(128) elbm_lowp_kernel(const typename Storage<S
     }
 #pragma unroll
     for (int q = 0; q < L::Q; ++q) {
-      // f - alpha beta f_neq + S  (Collision.h:243-258)
-      double r = fma(-ab, fn[q], f[q]);
+      // f - alpha beta f_neq + S  (Collision.h:243-258), f_neq = r f
+      const double fnq = r[q] * f[q];
+      double rr = fma(-ab, fnq, f[q]);
       if (FS == FS_GUO) {
         double cu = 0.0;
 #pragma unroll
@@ -460,19 +486,26 @@ __global__ void __launch_bounds__(128) elbm_lowp_kernel(const typename Storage<S
         }
         double R = 0.0;
 #pragma unroll
-        for (int k = 0; k < L::D; ++k) R = fma((double)L::c(q, k) - u[k] + L::c(q, k) * 3.0 * cu, Fs[k], R);
-        r += p.guo_k[q] * R;
+        for (int k = 0; k < L::D; ++k) R = fma((double)L::c(q, k) - u[k] + L::c(q, k) * 3.0 * cu, F[k], R);
+        rr += p.guo_k[q] * R;
       }
-      if (FS == FS_EDM) r += fsh[q] - (f[q] - fn[q]);
-      store_f64<LAT, ST>(next + (long long)q * p.V + idx, q, r);
+      if (FS == FS_EDM) rr += fsh[q] - (f[q] - fnq);
+      auto* dst = next + (long long)q * p.V + idx;
+      if constexpr (ST == ST_F32) {
+        *dst = narrow_rn(rr);
+      } else {
+        *dst = __float2half_rn(narrow_rn((rr - L::w(q)) * (double)(1 << shift_exponent<LAT>(q))));
+      }
     }
-    p.alpha_field_f32[idx] = (float)alpha;
+    p.alpha_field_f32[idx] = narrow_rn(alpha);
     if (!(rho > 0.0) || !isfinite(rho)) atomicOr(p.err_word, ERR_NONFINITE);
-    mass = rho;
-    amin = alpha;
-    amax = alpha;
-    const float uf[3] = {(float)u[0], (float)u[1], (float)u[2]};
-    lowp_store_fields<LAT>(p, idx, (float)rho, uf, F, FS != FS_NONE, alpha, energy, mach);
+    if (p.store || p.diag) {
+      mass = rho;
+      amin = alpha;
+      amax = alpha;
+      const float uf[3] = {(float)u[0], (float)u[1], (float)u[2]};
+      lowp_store_fields<LAT>(p, idx, (float)rho, uf, F, FS != FS_NONE, alpha, energy, mach);
+    }
   }
   add_counters(p.counters, cnt);
   if (p.diag) block_reduce_diag(mass, energy, mach, amin, amax, p.diag_partials);

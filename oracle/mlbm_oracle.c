@@ -14,6 +14,7 @@
 
 #include <math.h>
 #include <pthread.h>
+#include <stdint.h>
 #include <stdlib.h>
 #include <string.h>
 
@@ -226,30 +227,125 @@ static int newton(const hfun_t* h, double tol, int maxit, double* xR, double xMi
   return 0;
 }
 
+/* ---- Residual mode: the FP64 logarithm and log1p series of the kernels ----
+ * ln(x) after P. T. P. Tang, ACM TOMS 16(4), 1990: x = 2^e m, j = top 7
+ * fraction bits of m, inv_j = RN(1/c_j) for the interval centre c_j,
+ * r = fma(m, inv_j, -1), ln x = e ln2 + ln(1/inv_j) + log1p(r) with a
+ * degree-7 series; the table is built in the host's extended precision. The
+ * kernels use the same function, so the residual-mode step is reproduced
+ * operation for operation. */
+typedef struct {
+  double inv, hi, lo;
+} logent_t;
+
+static logent_t g_log_table[128];
+static pthread_once_t g_log_once = PTHREAD_ONCE_INIT;
+
+static void build_log_table(void) {
+  for (int j = 0; j < 128; ++j) {
+    const double c = 1.0 + (j + 0.5) / 128.0;
+    const double inv = 1.0 / c;
+    const long double L = -logl((long double)inv);
+    const double hi = (double)L;
+    g_log_table[j].inv = inv;
+    g_log_table[j].hi = hi;
+    g_log_table[j].lo = (double)(L - (long double)hi);
+  }
+}
+
+static double series7(double r) {
+  double p = 1.0 / 7.0;
+  p = fma(p, r, -1.0 / 6.0);
+  p = fma(p, r, 1.0 / 5.0);
+  p = fma(p, r, -1.0 / 4.0);
+  p = fma(p, r, 1.0 / 3.0);
+  p = fma(p, r, -0.5);
+  return fma(p * r, r, r);
+}
+
+static double series9(double t) {
+  double p = 1.0 / 9.0;
+  p = fma(p, t, -1.0 / 8.0);
+  p = fma(p, t, 1.0 / 7.0);
+  p = fma(p, t, -1.0 / 6.0);
+  p = fma(p, t, 1.0 / 5.0);
+  p = fma(p, t, -1.0 / 4.0);
+  p = fma(p, t, 1.0 / 3.0);
+  p = fma(p, t, -0.5);
+  return fma(p * t, t, t);
+}
+
+static double series5(double t) {
+  double p = 1.0 / 5.0;
+  p = fma(p, t, -1.0 / 4.0);
+  p = fma(p, t, 1.0 / 3.0);
+  p = fma(p, t, -0.5);
+  return fma(p * t, t, t);
+}
+
+static double tang_log(double x) {
+  const double kLn2Hi = 0x1.62e42fefa3800p-1, kLn2Lo = 0x1.ef35793c76730p-45;
+  uint64_t bits;
+  memcpy(&bits, &x, sizeof bits);
+  int e = (int)((bits >> 52) & 0x7ff);
+  if (e == 0) {
+    const double xs = x * 18014398509481984.0;
+    memcpy(&bits, &xs, sizeof bits);
+    e = (int)((bits >> 52) & 0x7ff) - 54;
+  }
+  e -= 1023;
+  const int j = (int)((bits >> 45) & 127);
+  const uint64_t mb = (bits & 0x000fffffffffffffULL) | 0x3ff0000000000000ULL;
+  double m;
+  memcpy(&m, &mb, sizeof m);
+  const logent_t t = g_log_table[j];
+  const double r = fma(m, t.inv, -1.0);
+  const double ed = (double)e;
+  const double hi = fma(ed, kLn2Hi, t.hi);
+  const double lo = fma(ed, kLn2Lo, t.lo) + series7(r);
+  return hi + lo;
+}
+
+double oracle_fast_log(double x) {
+  pthread_once(&g_log_once, build_log_table);
+  return tang_log(x);
+}
+
 /* Residual-mode entropy function in log1p form. With r = f_neq/f and
  * t = -x r (g = f (1 + t)), ln(g/w) = L + log1p(t), L = ln(f/w), and
  *   F(x)  = x B1 - sum f (1 + t) log1p(t),  B1 = sum f_neq L,
  *   F'(x) = C0 + sum f r log1p(t),          C0 = sum f_neq + B1,
  * the same function as sum f ln(f/w) - sum g ln(g/w) (EntropicStep.h:31-45)
- * and its derivative (47-62), formed from O(|f_neq|) terms. */
+ * and its derivative (47-62), formed from O(|f_neq|) terms. log1p is a
+ * degree-5 series when every |t| <= 2^-10, degree 9 for |t| <= 2^-6, and the
+ * logarithm above otherwise. */
 typedef struct {
   const double* f;
   const double* r;
-  double B1, C0;
+  double B1, C0, rmax;
   int Q;
 } hlog1p_t;
 
 static void h_log1p(const hlog1p_t* h, double x, double* F, double* dF) {
   double s = 0.0, d = 0.0;
-  for (int q = 0; q < h->Q; ++q) {
-    const double t = -x * h->r[q];
-    const double opt = 1.0 + t;
-    double lp;
-    if (fabs(t) <= 0.015625) lp = log1p(t);
-    else if (opt > 0.0) lp = log(opt);
-    else lp = -745.0; /* g = 0 at alpha_max: g ln g -> 0 */
-    if (opt > 0.0) s = fma(h->f[q] * opt, lp, s);
-    d = fma(h->f[q] * h->r[q], lp, d);
+  if (x * h->rmax <= 0.0009765625) {
+    for (int q = 0; q < h->Q; ++q) {
+      const double t = -x * h->r[q];
+      const double lp = series5(t);
+      s = fma(fma(h->f[q], t, h->f[q]), lp, s);
+      d = fma(h->f[q] * h->r[q], lp, d);
+    }
+  } else {
+    for (int q = 0; q < h->Q; ++q) {
+      const double t = -x * h->r[q];
+      const double opt = 1.0 + t;
+      double lp;
+      if (fabs(t) <= 0.015625) lp = series9(t);
+      else if (opt > 0.0) lp = tang_log(opt);
+      else lp = -745.0; /* g = 0 at alpha_max: g ln g -> 0 */
+      if (opt > 0.0) s = fma(h->f[q] * opt, lp, s);
+      d = fma(h->f[q] * h->r[q], lp, d);
+    }
   }
   *F = fma(x, h->B1, -s);
   *dF = h->C0 + d;
@@ -299,13 +395,15 @@ static int bisection_newton_residual(const hlog1p_t* h, double tol, int maxit, d
 static double solve_residual(const double* f, const double* fneq, const double* w, int Q,
                              double tol, int maxit, double guess, double xMax, long long* iters,
                              long long* fallbacks, long long* bisections) {
-  double r[QMAX], B1 = 0.0, sfn = 0.0;
+  pthread_once(&g_log_once, build_log_table);
+  double r[QMAX], B1 = 0.0, sfn = 0.0, rmax = 0.0;
   for (int q = 0; q < Q; ++q) {
-    B1 = fma(fneq[q], log(f[q] * (1.0 / w[q])), B1);
+    B1 = fma(fneq[q], tang_log(f[q] * (1.0 / w[q])), B1);
     sfn += fneq[q];
     r[q] = fneq[q] / f[q];
+    rmax = fmax(rmax, fabs(r[q]));
   }
-  const hlog1p_t h = {f, r, B1, sfn + B1, Q};
+  const hlog1p_t h = {f, r, B1, sfn + B1, rmax, Q};
   double x = guess;
   if (x > 1.0 && x < xMax) {
     double fe, de;

@@ -75,6 +75,9 @@ void oracle_get_fields(const oracle_state* s, double* rho, double* u, double* al
 void oracle_get_counters(const oracle_state* s, long long* newton_iterations,
                          long long* fallbacks, long long* bisections);
 
+/* The residual mode's FP64 logarithm (Tang's table-driven method). */
+double oracle_fast_log(double x);
+
 /* Single-node entry points for unit tests: equilibrium population q. */
 double oracle_equilibrium(int lattice, double rho, const double* u, int q);
 int oracle_lattice_q(int lattice);

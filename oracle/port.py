@@ -76,6 +76,8 @@ def _load():
         lib.oracle_equilibrium.restype = ct.c_double
         lib.oracle_equilibrium.argtypes = [ct.c_int, ct.c_double, dp, ct.c_int]
         lib.oracle_lattice_tables.argtypes = [ct.c_int, dp, dp]
+        lib.oracle_fast_log.restype = ct.c_double
+        lib.oracle_fast_log.argtypes = [ct.c_double]
         _lib = lib
     return _lib
 
@@ -179,3 +181,8 @@ def equilibrium(lattice: str, rho: float, u, q: int) -> float:
     uu = np.zeros(3)
     uu[:len(u)] = u
     return _load().oracle_equilibrium(LATTICES[lattice], float(rho), _ptr(uu), int(q))
+
+
+def fast_log(x: float) -> float:
+    """The residual mode's FP64 logarithm (Tang's table-driven method)."""
+    return _load().oracle_fast_log(float(x))

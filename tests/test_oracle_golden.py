@@ -105,3 +105,18 @@ def test_density_known_answer():
     port.set_populations(f)
     port.step(1)
     assert port.fields()["rho"][0] == 9 * 5.0 + 9 * 8 / 2
+
+
+def test_residual_mode_logarithm_accuracy():
+    """Tang's table-driven logarithm of the residual solver (oracle copy)
+    against libm: within a few ulp of ln 2 absolute, 2 ulp relative away from 1."""
+    from oracle.port import fast_log
+    rng = np.random.default_rng(1)
+    xs = np.concatenate([np.exp(rng.uniform(-700, 700, 5000)), rng.uniform(0.5, 2.0, 5000),
+                         [1.0, 2.0, 0.5, 5e-324, 1e-310, 1.7e308]])
+    got = np.array([fast_log(x) for x in xs])
+    ref = np.log(xs)
+    bound = np.maximum(4 * np.spacing(np.log(2.0)), 3 * np.spacing(np.abs(ref)))
+    assert (np.abs(got - ref) <= bound).all()
+    away = np.abs(ref) >= 0.5
+    assert (np.abs(got - ref)[away] <= 2 * np.spacing(np.abs(ref[away]))).all()
