@@ -155,27 +155,36 @@ def job_value(nodes_per_rank: int, steps: int, world: int, max_ms: float) -> flo
 
 
 def time_steps(lat, steps: int, torch, dist=None):
-    """Time `steps` single-step calls with CUDA events on the handle's stream.
-    Returns (total ms, list of per-launch ms)."""
+    """Time one mlbm_step call of `steps` steps with CUDA events on the
+    handle's stream (so the solver counters cover exactly the timed steps).
+    Returns (total ms, launches of the library's kernels in the region)."""
     from metalbm_gb300.lattice import kernel_launch_count
     stream = torch.cuda.ExternalStream(lat.stream)
-    ev = [torch.cuda.Event(enable_timing=True) for _ in range(steps + 1)]
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     lat.sync()
     if dist is not None:
         dist.barrier()
     torch.cuda.synchronize()
     n0 = kernel_launch_count()
-    ev[0].record(stream)
-    for i in range(steps):
-        lat.step(1)
-        ev[i + 1].record(stream)
+    e0.record(stream)
+    lat.step(steps)
+    e1.record(stream)
     lat.sync()
     torch.cuda.synchronize()
     launches = kernel_launch_count() - n0
-    per = [ev[i].elapsed_time(ev[i + 1]) for i in range(steps)]
     if dist is not None:
         dist.barrier()
-    return ev[0].elapsed_time(ev[steps]), per, launches
+    return e0.elapsed_time(e1), launches
+
+
+def solver_stats(d: dict) -> dict:
+    """Per-solved-node statistics of the alpha solve over the timed steps."""
+    solved = max(d["solved_nodes"], 1)
+    return {"newton_iterations_per_solved_node": d["newton_iterations"] / solved,
+            "guess_hit_fraction": d["guess_hits"] / solved,
+            "fallback_fraction": 1.0 - d["guess_hits"] / solved,
+            "bisection_nodes": d["bisection_nodes"], "alpha2_fallback_nodes": d["fallback_nodes"],
+            "series_form_fraction": d["series_nodes"] / solved}
 
 
 def load_or_train_model(deck, torch):
@@ -244,7 +253,8 @@ def run_ours(args):
         dist.barrier()
     name = args.workload
     w = WORKLOADS[name]
-    deck = deck_for(name, device=local)
+    grid_over = {"globalLength": (args.grid,) * 3} if args.grid else {}
+    deck = deck_for(name, device=local, **grid_over)
     shape = deck.shape
     V = int(np.prod(shape))
     rho, u = initial_field(name, shape)
@@ -254,7 +264,7 @@ def run_ours(args):
     # --- arm 1: the learned guess (or the only arm for BGK workloads)
     if entropic:
         model, model_src = load_or_train_model(deck, torch)
-        deck_l = deck_for(name, device=local, alphaGuess="learned")
+        deck_l = deck_for(name, device=local, alphaGuess="learned", **grid_over)
     else:
         deck_l = deck
     lat = Lattice(deck_l)
@@ -263,44 +273,49 @@ def run_ours(args):
     lat.init_equilibrium(rho, u)
     lat.step(args.warmup)
     with ClockSampler(local) as clk:
-        total_ms, per, launches = time_steps(lat, args.steps, torch, dist)
-    lat.step(1, diagnostics=True)
+        total_ms, launches = time_steps(lat, args.steps, torch, dist)
     dl = lat.diagnostics()
     lat.close()
     total_ms = max_over_ranks(total_ms, dist, f"cuda:{local}")
 
-    # --- arm 2: plain Newton from the previous alpha, same state, same GPU
+    # --- arms 2 and 3: plain Newton from the previous step's alpha (the
+    # reference's guess, Algorithm.h:103-106) and from alpha = 2; same
+    # initial state, same residual tolerance, same GPU
     if entropic:
-        lat = Lattice(deck_for(name, device=local, alphaGuess="previous"))
-        lat.init_equilibrium(rho, u)
-        lat.step(args.warmup)
-        nt_ms, nt_per, _ = time_steps(lat, args.steps, torch, dist)
-        lat.step(1, diagnostics=True)
-        dn = lat.diagnostics()
-        lat.close()
-        nt_ms = max_over_ranks(nt_ms, dist, f"cuda:{local}")
-        newton_mlups = job_value(V, args.steps, world, nt_ms)
-        solved = max(dl["solved_nodes"], 1)
+        value_l = job_value(V, args.steps, world, total_ms)
+        arms = {}
+        for guess in ("previous", "two"):
+            lat = Lattice(deck_for(name, device=local, alphaGuess=guess, **grid_over))
+            lat.init_equilibrium(rho, u)
+            lat.step(args.warmup)
+            ms, _ = time_steps(lat, args.steps, torch, dist)
+            d = lat.diagnostics()
+            lat.close()
+            ms = max_over_ranks(ms, dist, f"cuda:{local}")
+            arms[guess] = {"value": job_value(V, args.steps, world, ms), "unit": "MLUPS",
+                           "ms_per_step": ms / args.steps, **solver_stats(d)}
+        sl = solver_stats(dl)
         extra = {
-            "newton_alpha": {"value": newton_mlups, "unit": "MLUPS",
-                             "ms_per_step": nt_ms / args.steps,
-                             "newton_iterations_per_solved_node": dn["newton_iterations"] / max(dn["solved_nodes"], 1),
-                             "guess_hit_fraction": dn["guess_hits"] / max(dn["solved_nodes"], 1),
-                             "fallback_nodes": dn["fallback_nodes"]},
-            "learned_alpha": {"newton_iterations_per_solved_node": dl["newton_iterations"] / solved,
-                              "fallback_fraction": (dl["solved_nodes"] - dl["guess_hits"]) / solved,
-                              "alpha2_fallback_nodes": dl["fallback_nodes"],
-                              "model": model_src},
-            "speedup_learned_vs_newton": job_value(V, args.steps, world, total_ms) / newton_mlups,
-            "newton_iterations_saved_per_solved_node":
-                dn["newton_iterations"] / max(dn["solved_nodes"], 1) - dl["newton_iterations"] / solved,
+            "newton_alpha": arms["previous"],
+            "newton_alpha_from_2": arms["two"],
+            "learned_alpha": {**sl, "model": model_src},
+            "speedup_learned_vs_newton": value_l / arms["previous"]["value"],
+            "speedup_learned_vs_newton_from_2": value_l / arms["two"]["value"],
+            "newton_iterations_saved_per_solved_node": {
+                "vs_previous_alpha": arms["previous"]["newton_iterations_per_solved_node"]
+                - sl["newton_iterations_per_solved_node"],
+                "vs_alpha_2": arms["two"]["newton_iterations_per_solved_node"]
+                - sl["newton_iterations_per_solved_node"]},
             "residual_tolerance": deck.newtonTolerance,
+            "solver_stats_over": f"the {args.steps} timed steps",
         }
 
     value = job_value(V, args.steps, world, total_ms)
+    pop_gb = V * {"D2Q9": 9, "D3Q19": 19, "D3Q27": 27}[deck.latticeT] * \
+        {"f64": 8, "f32": 4, "f16_shifted": 2}[deck.storage] * 2 / 1e9
     peaks, peak_src = measured_peaks()
     bpn = w["bytes_per_node"]
-    avg_launch_ms = float(np.mean(per))
+    avg_launch_ms = total_ms / args.steps
     achieved = bpn * V / (avg_launch_ms * 1e-3) / 1e9
     traffic = None
     tfile = ROOT / "profiles" / "traffic.json"
@@ -334,7 +349,8 @@ def run_ours(args):
                        "storage": deck.storage, "grid": list(shape), "beta": 1 / (2 * deck.relaxationTime),
                        "alpha_solver": deck.alphaSolver if entropic else None,
                        "parallelism": f"replicas x{world}",
-                       "l2": f"inputs {V * 27 * 4 * 2 / 1e9:.1f} GB > 129 MB L2, no flush needed"},
+                       "l2": f"populations {pop_gb:.1f} GB read and written per step > 129 MB L2, "
+                             "no flush needed"},
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
             "clocks": clk.summary(), **extra,
         }
@@ -436,6 +452,9 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="entropic_learned_512", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
+    ap.add_argument("--grid", type=int, default=0,
+                    help="cubic grid side overriding the workload's (profiling captures of a "
+                         "smaller case; not a bench configuration)")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")

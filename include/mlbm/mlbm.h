@@ -126,7 +126,9 @@ typedef struct {
   long long shortcut_nodes;    /* nodes with every |f_neq|/f below the threshold */
   unsigned int error_word;     /* bit 0: non-finite population; bit 1: negative density */
   unsigned int reserved0;
-  double reserved[6];
+  long long series_nodes;      /* solved nodes of the FP32/FP16-storage kernels whose
+                                  entropy function took the moment-series form */
+  double reserved[5];
 } mlbm_diag;
 
 /* Learned alpha guess: an MLP in -> 32 -> 32 -> 1 with tanh hidden layers.

@@ -14,6 +14,16 @@ extern "C" {
  * Host arrays; allocates temporary device buffers. */
 int mlbm_testing_fast_log(const double* x, double* out, long long n);
 
+/* The entropy-balance function F(x) and its derivative as the FP32-storage
+ * entropic kernel evaluates them, for `nodes` nodes given as FP32 populations
+ * f[nodes][Q] and FP64 non-equilibrium parts fneq[nodes][Q], at the nx points
+ * x[]: F and D are [nodes][nx]; series[node] = 1 where the moment-series form
+ * was used. mode 0 chooses the form as the kernel does (series when
+ * max_q |f_neq/f| <= 0.0125), 1 forces the direct log1p form, 2 the series.
+ * Host arrays; allocates temporary device buffers. */
+int mlbm_testing_entropy(int lattice, const float* f, const double* fneq, long long nodes,
+                         const double* x, int nx, int mode, double* F, double* D, int* series);
+
 #ifdef __cplusplus
 }
 #endif

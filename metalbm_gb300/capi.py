@@ -34,7 +34,7 @@ EXPORTS = [
     "mlbm_last_error", "mlbm_kernel_launch_count", "mlbm_step_f64_noalloc",
     "mlbm_get_alpha", "mlbm_set_alpha",
 ]
-TESTING_EXPORTS = ["mlbm_testing_fast_log"]
+TESTING_EXPORTS = ["mlbm_testing_fast_log", "mlbm_testing_entropy"]
 
 
 class Config(ct.Structure):
@@ -55,7 +55,8 @@ class Diag(ct.Structure):
                 ("guess_hits", ct.c_longlong), ("bisection_nodes", ct.c_longlong),
                 ("fallback_nodes", ct.c_longlong), ("limited_nodes", ct.c_longlong),
                 ("shortcut_nodes", ct.c_longlong), ("error_word", ct.c_uint),
-                ("reserved0", ct.c_uint), ("reserved", ct.c_double * 6)]
+                ("reserved0", ct.c_uint), ("series_nodes", ct.c_longlong),
+                ("reserved", ct.c_double * 5)]
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_ if not k.startswith("reserved")}
@@ -116,6 +117,8 @@ def load(path: Path | str | None = None):
         "mlbm_kernel_launch_count": ([], ct.c_ulonglong),
         "mlbm_step_f64_noalloc": ([ct.POINTER(Config), vp, vp, vp, vp, vp, vp], ct.c_int),
         "mlbm_testing_fast_log": ([dp, dp, ct.c_longlong], ct.c_int),
+        "mlbm_testing_entropy": ([ct.c_int, fp, dp, ct.c_longlong, dp, ct.c_int, ct.c_int, dp,
+                                  dp, ct.POINTER(ct.c_int)], ct.c_int),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)

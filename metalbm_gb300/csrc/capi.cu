@@ -69,12 +69,18 @@ struct mlbm_handle {
   float* force_table_f[3] = {nullptr, nullptr, nullptr};
   double* partials = nullptr;
   int partial_blocks = 0;
+  int main_blocks = 0;          // blocks of the (first) step kernel
+  // entropic FP32/FP16 step: second-pass worklist
+  unsigned* defer_list = nullptr;
+  unsigned* defer_count = nullptr;
+  int defer_blocks = 0;
   double* diag_dev = nullptr;
   unsigned long long* counters = nullptr;
   unsigned* err_word = nullptr;
   double* staging = nullptr;    // V doubles
   MlpDev* mlp = nullptr;
   LogEntry* log_table = nullptr;
+  LogEntryFine* log_table_fine = nullptr;
   bool have_model = false;
   long long* sample_nodes = nullptr;
   long long n_samples = 0;
@@ -233,7 +239,7 @@ static void release(mlbm_handle* h) {
                   h->force_table[0], h->force_table[1], h->force_table[2], h->force_table_f[0],
                   h->force_table_f[1], h->force_table_f[2], h->partials,
                   h->diag_dev, h->counters, h->err_word, h->staging, h->mlp, h->log_table,
-                  h->sample_nodes,
+                  h->log_table_fine, h->defer_list, h->defer_count, h->sample_nodes,
                   h->sample_feat, h->sample_alpha, h->sample_solved};
   for (void* p : ptrs)
     if (p) cudaFree(p);
@@ -244,6 +250,15 @@ static void release(mlbm_handle* h) {
 // Table of the FP64 logarithm (fastlog.cuh): for the centre c_j of each of
 // the 128 mantissa intervals, inv_j = RN(1/c_j) and -ln(inv_j) split into a
 // double-double, evaluated in the host's extended precision.
+static void make_log_table_fine(LogEntryFine* t) {
+  for (int j = 0; j < LOG_TABLE_FINE; ++j) {
+    const double c = 1.0 + (j + 0.5) / (double)LOG_TABLE_FINE;
+    const double inv = 1.0 / c;
+    t[j].inv = inv;
+    t[j].hi = (double)(-std::log((long double)inv));
+  }
+}
+
 static void make_log_table(LogEntry* t) {
   for (int j = 0; j < LOG_TABLE; ++j) {
     const double c = 1.0 + (j + 0.5) / (double)LOG_TABLE;
@@ -358,18 +373,43 @@ extern "C" int mlbm_create(const mlbm_config* cfg, mlbm_handle** out) {
     if ((rc = device_alloc(h, (void**)&h->alpha32, sizeof(float) * V))) return bail(rc);
   }
   const int bs = 128;  // smallest block size of the step kernels
-  h->partial_blocks = (int)((V + bs - 1) / bs);
+  h->main_blocks = (int)((V + bs - 1) / bs);
+  h->partial_blocks = h->main_blocks;
+  const bool two_pass = c.collision != MLBM_BGK && c.storage != MLBM_STORAGE_F64;
+  if (two_pass) {
+    if (V > 0xffffffffLL) {
+      h->error = "entropic FP32/FP16 lattices are limited to 2^32 - 1 nodes";
+      return bail(MLBM_ERR_INVALID);
+    }
+    int sms = 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c.device) != cudaSuccess ||
+        sms <= 0) {
+      cudaGetLastError();
+      sms = 1;
+    }
+    h->defer_blocks = 2 * sms;
+    h->partial_blocks += h->defer_blocks;
+    if ((rc = device_alloc(h, (void**)&h->defer_list, sizeof(unsigned) * (size_t)V)) ||
+        (rc = device_alloc(h, (void**)&h->defer_count, 2 * sizeof(unsigned))))
+      return bail(rc);
+    cudaMemsetAsync(h->defer_count, 0, 2 * sizeof(unsigned), h->stream);
+  }
   if ((rc = device_alloc(h, (void**)&h->partials, sizeof(double) * DIAG_FIELDS * h->partial_blocks)) ||
       (rc = device_alloc(h, (void**)&h->diag_dev, sizeof(double) * DIAG_FIELDS)) ||
       (rc = device_alloc(h, (void**)&h->counters, sizeof(unsigned long long) * CNT_COUNT)) ||
       (rc = device_alloc(h, (void**)&h->err_word, sizeof(unsigned))) ||
       (rc = device_alloc(h, (void**)&h->mlp, sizeof(MlpDev))) ||
-      (rc = device_alloc(h, (void**)&h->log_table, sizeof(LogEntry) * LOG_TABLE)))
+      (rc = device_alloc(h, (void**)&h->log_table, sizeof(LogEntry) * LOG_TABLE)) ||
+      (rc = device_alloc(h, (void**)&h->log_table_fine, sizeof(LogEntryFine) * LOG_TABLE_FINE)))
     return bail(rc);
   {
     LogEntry tab[LOG_TABLE];
     make_log_table(tab);
-    if (cudaMemcpy(h->log_table, tab, sizeof tab, cudaMemcpyHostToDevice) != cudaSuccess) {
+    static LogEntryFine fine[LOG_TABLE_FINE];
+    static std::once_flag fine_once;
+    std::call_once(fine_once, [] { make_log_table_fine(fine); });
+    if (cudaMemcpy(h->log_table, tab, sizeof tab, cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(h->log_table_fine, fine, sizeof fine, cudaMemcpyHostToDevice) != cudaSuccess) {
       h->error = "log table upload failed";
       return bail(MLBM_ERR_CUDA);
     }
@@ -451,6 +491,7 @@ extern "C" int mlbm_create(const mlbm_config* cfg, mlbm_handle** out) {
   p.newton_tol = c.newton_tolerance;
   p.newton_maxit = c.newton_max_iterations;
   p.deviation_threshold = c.deviation_threshold;
+  p.deviation_threshold_f = (float)c.deviation_threshold;
   p.rho_out = h->rho;
   p.u_out = h->u;
   p.force_out = h->force;
@@ -461,6 +502,11 @@ extern "C" int mlbm_create(const mlbm_config* cfg, mlbm_handle** out) {
   p.err_word = h->err_word;
   p.mlp = h->mlp;
   p.log_table = h->log_table;
+  p.log_table_fine = h->log_table_fine;
+  p.defer_list = h->defer_list;
+  p.defer_count = h->defer_count;
+  p.defer_blocks = h->defer_blocks;
+  p.defer_slot0 = h->main_blocks;
 
   if (cudaStreamSynchronize(h->stream) != cudaSuccess) {
     h->error = std::string("device initialisation failed: ") + cudaGetErrorString(cudaGetLastError());
@@ -558,6 +604,7 @@ extern "C" int mlbm_step(mlbm_handle* h, int nsteps, unsigned int flags) {
   for (int s = 0; s < nsteps; ++s) {
     const bool last = s == nsteps - 1;
     StepParams p = h->base;
+    p.parity = (int)(h->steps & 1);
     p.store = last && (flags & MLBM_STEP_STORE_FIELDS) ? 1 : 0;
     p.diag = last && (flags & MLBM_STEP_DIAGNOSTICS) ? 1 : 0;
     const void* prev = h->f[h->cur];
@@ -567,11 +614,11 @@ extern "C" int mlbm_step(mlbm_handle* h, int nsteps, unsigned int flags) {
                                    (const double*)prev, (double*)next, p, h->stream)
                         : step_lowp(h->cfg.lattice, collision, h->cfg.forcing_scheme, h->storage,
                                     prev, next, p, h->stream);
-    count_launches(1);
+    count_launches(h->defer_blocks > 0 ? 2 : 1);
     if (e != cudaSuccess) return fail(h, MLBM_ERR_CUDA, "step kernel: %s", cudaGetErrorString(e));
     if (p.diag) {
-      const int bs = (h->storage == MLBM_STORAGE_F64 ? (collision ? 128 : 256) : (collision ? 128 : 256));
-      const int nb = (int)((h->V + bs - 1) / bs);
+      const int bs = collision ? 128 : 256;
+      const int nb = (int)((h->V + bs - 1) / bs) + h->defer_blocks;
       e = finalize_diag(h->partials, nb, h->diag_dev, h->stream);
       count_launches(1);
       if (e != cudaSuccess) return fail(h, MLBM_ERR_CUDA, "diagnostics: %s", cudaGetErrorString(e));
@@ -660,6 +707,7 @@ extern "C" int mlbm_get_diagnostics(mlbm_handle* h, mlbm_diag* out) {
   out->fallback_nodes = (long long)c[CNT_FALLBACK];
   out->limited_nodes = (long long)c[CNT_LIMITED];
   out->shortcut_nodes = (long long)c[CNT_SHORTCUT];
+  out->series_nodes = (long long)c[CNT_SERIES];
   out->error_word = err;
   return MLBM_OK;
 }
@@ -877,5 +925,51 @@ extern "C" int mlbm_testing_fast_log(const double* x, double* out, long long n) 
   if (e == cudaSuccess) e = cudaMemcpy(out, dout, sizeof(double) * n, cudaMemcpyDeviceToHost);
   cudaFree(dx); cudaFree(dout); cudaFree(dtab);
   if (e != cudaSuccess) return fail(nullptr, MLBM_ERR_CUDA, "fast log: %s", cudaGetErrorString(e));
+  return MLBM_OK;
+}
+
+extern "C" int mlbm_testing_entropy(int lattice, const float* f, const double* fneq,
+                                    long long nodes, const double* x, int nx, int mode,
+                                    double* F, double* D, int* series) {
+  if (lattice < 0 || lattice > 2 || !f || !fneq || !x || !F || !D || !series || nodes <= 0 ||
+      nx <= 0 || mode < 0 || mode > 2)
+    return MLBM_ERR_INVALID;
+  const int Q = lattice == 0 ? 9 : (lattice == 1 ? 19 : 27);
+  LogEntry tab[LOG_TABLE];
+  make_log_table(tab);
+  LogEntryFine fine[LOG_TABLE_FINE];
+  make_log_table_fine(fine);
+  const size_t nf = sizeof(float) * Q * nodes, nn = sizeof(double) * Q * nodes,
+               nxb = sizeof(double) * nx, no = sizeof(double) * nx * nodes,
+               ns = sizeof(int) * nodes;
+  void *df = nullptr, *dn = nullptr, *dx = nullptr, *dF = nullptr, *dD = nullptr,
+       *dS = nullptr, *dt = nullptr, *dtf = nullptr;
+  auto release = [&]() {
+    cudaFree(df); cudaFree(dn); cudaFree(dx); cudaFree(dF); cudaFree(dD); cudaFree(dS);
+    cudaFree(dt); cudaFree(dtf);
+  };
+  if (cudaMalloc(&df, nf) != cudaSuccess || cudaMalloc(&dn, nn) != cudaSuccess ||
+      cudaMalloc(&dx, nxb) != cudaSuccess || cudaMalloc(&dF, no) != cudaSuccess ||
+      cudaMalloc(&dD, no) != cudaSuccess || cudaMalloc(&dS, ns) != cudaSuccess ||
+      cudaMalloc(&dt, sizeof tab) != cudaSuccess || cudaMalloc(&dtf, sizeof fine) != cudaSuccess) {
+    release();
+    cudaGetLastError();
+    return fail(nullptr, MLBM_ERR_ALLOC, "testing buffers");
+  }
+  cudaError_t e = cudaMemcpy(df, f, nf, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(dn, fneq, nn, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(dx, x, nxb, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(dt, tab, sizeof tab, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(dtf, fine, sizeof fine, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess)
+    e = entropy_test(lattice, (const float*)df, (const double*)dn, nodes, (const double*)dx, nx,
+                     mode, dt, dtf, (double*)dF, (double*)dD, (int*)dS, 0);
+  count_launches(1);
+  if (e == cudaSuccess) e = cudaDeviceSynchronize();
+  if (e == cudaSuccess) e = cudaMemcpy(F, dF, no, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(D, dD, no, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(series, dS, ns, cudaMemcpyDeviceToHost);
+  release();
+  if (e != cudaSuccess) return fail(nullptr, MLBM_ERR_CUDA, "entropy test: %s", cudaGetErrorString(e));
   return MLBM_OK;
 }

@@ -59,6 +59,7 @@ struct StepParams {
   double newton_tol;
   int newton_maxit;
   double deviation_threshold;
+  float deviation_threshold_f;
   // optional outputs on this step
   int store;                 // write rho, u_hydro, alpha(, force) fields
   int diag;                  // fused diagnostics reduction
@@ -72,11 +73,18 @@ struct StepParams {
   unsigned* err_word;
   const void* mlp;           // device MlpDev* (learned guess)
   const void* log_table;     // device LogEntry[LOG_TABLE] (fastlog.cuh)
+  const void* log_table_fine;  // device LogEntryFine[LOG_TABLE_FINE] (fastlog.cuh)
+  // entropic FP32/FP16 step: worklist of the nodes left to the second pass
+  unsigned* defer_list;      // [V] node indices
+  unsigned* defer_count;     // [2] list lengths, used by alternating steps
+  int parity;                // step number & 1
+  int defer_blocks;          // grid of the second pass
+  int defer_slot0;           // its first block's slot in diag_partials
 };
 
 enum : int {
   CNT_SOLVED = 0, CNT_ITER = 1, CNT_HITS = 2, CNT_BISECT = 3, CNT_FALLBACK = 4,
-  CNT_LIMITED = 5, CNT_SHORTCUT = 6, CNT_COUNT = 8
+  CNT_LIMITED = 5, CNT_SHORTCUT = 6, CNT_SERIES = 7, CNT_COUNT = 8
 };
 constexpr int DIAG_FIELDS = 5;
 
@@ -210,7 +218,7 @@ __device__ __forceinline__ void block_reduce_diag(double mass, double energy, do
 // Warp-aggregated add of the solver counters.
 __device__ __forceinline__ void add_counters(unsigned long long* counters, const unsigned c[CNT_COUNT]) {
 #pragma unroll
-  for (int k = 0; k < 7; ++k) {
+  for (int k = 0; k < CNT_COUNT; ++k) {
     unsigned v = c[k];
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);

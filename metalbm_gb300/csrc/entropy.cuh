@@ -2,6 +2,7 @@
 // the FP64-storage and FP32/FP16-storage entropic kernels.
 #pragma once
 
+#include "common.cuh"
 #include "fastlog.cuh"
 #include "lattice.cuh"
 
@@ -52,6 +53,40 @@ struct HLog1p {
     }
     Fv = fma(x, B1, -s);
     Dv = C0 + d;
+  }
+};
+
+// Moment-series form of the same function for small deviations. With
+// (1 + t) log1p(t) = t + sum_{k>=2} (-1)^k t^k / (k (k - 1)), t_q = -x r_q,
+// and the moments M_k = sum_q f_q r_q^k (M_1 = sum_q f_neq_q = 0 for the
+// TruncationMa3 equilibrium of all three lattices, whose weights make
+// sum_q w_q P_q(u) vanish identically):
+//   F(x)  = x B1 - sum_{k>=2} x^k M_k / (k (k - 1)),
+//   F'(x) = B1   - sum_{k>=2} x^(k-1) M_k / (k - 1).
+// Kept to k = 8, which is accurate to |F error| <= rho (2.5 r)^9 / 72 < 5e-16
+// for x <= alpha_max <= 2.5 and r = max_q |r_q| <= kSeriesRmax. M_2..M_4 are
+// FP64 sums; M_5..M_8 are FP32 sums, whose terms are bounded by
+// 4.9 r^3 M_2 and lose at most 1.6e-6 of that (< 3e-15 absolute at the limit).
+// An evaluation is then a handful of FP64 operations instead of Q logarithms
+// or series.
+constexpr float kSeriesRmax = 0.0125f;
+
+struct HSeries {
+  double c1;          // B1
+  double a2, a3, a4;  // M2/2, M3/6, M4/12
+  double b2, b3, b4;  // M2,   M3/2, M4/3
+  float h5, h6, h7, h8;  // M5/20, M6/30, M7/42, M8/56
+  float g5, g6, g7, g8;  // M5/4,  M6/5,  M7/6,  M8/7
+  __device__ __forceinline__ void operator()(double x, double& Fv, double& Dv) const {
+    const float xf = narrow_rn(x);
+    const float x2f = xf * xf;
+    const float x4f = x2f * x2f;
+    const float h = fmaf(fmaf(fmaf(h8, xf, h7), xf, h6), xf, h5) * (x4f * xf);
+    const float g = fmaf(fmaf(fmaf(g8, xf, g7), xf, g6), xf, g5) * x4f;
+    const double p = fma(fma(a4, x, a3), x, a2);
+    const double q = fma(fma(b4, x, b3), x, b2);
+    Fv = fma(x, c1, -fma(x * x, p, widen_exact(h)));
+    Dv = fma(-x, q, c1 - widen_exact(g));
   }
 };
 

@@ -17,6 +17,8 @@
 
 #include <stdint.h>
 
+#include "common.cuh"
+
 namespace mlbm {
 
 constexpr int LOG_TABLE = 128;
@@ -31,6 +33,7 @@ struct LogEntry {
 // significant bits): kLn2Hi + kLn2Lo = ln 2 to ~1e-29.
 constexpr double kLn2Hi = 0x1.62e42fefa3800p-1;
 constexpr double kLn2Lo = 0x1.ef35793c76730p-45;
+constexpr double kLn2 = 0x1.62e42fefa39efp-1;  // RN(ln 2)
 
 // Degree-7 Taylor polynomial of log1p(r) = r - r^2/2 + r^3/3 - ... - r^8/8,
 // truncated after r^7 (|r| < 0.0045 gives |r|^8/8 < 2e-20).
@@ -85,6 +88,73 @@ __device__ __forceinline__ double fast_log(double x, const LogEntry* tab) {
   const double hi = fma(ed, kLn2Hi, t.hi);  // exact product, one rounding in the sum
   const double lo = fma(ed, kLn2Lo, t.lo) + log1p_series7(r);
   return hi + lo;
+}
+
+// The exponent e as a double without a conversion instruction (integer to
+// FP64 conversion runs on GB300's narrow FP64 path): the bit pattern of
+// 1.5 * 2^52 + e, minus 1.5 * 2^52, exact for |e| < 2^51.
+__device__ __forceinline__ double exponent_as_double(int e) {
+  return __longlong_as_double(0x4338000000000000LL + (long long)e) - 6755399441055744.0;
+}
+
+// ln(x) to about 1e-15 absolute for positive normal or subnormal x: the same
+// reduction as fast_log without the double-double tails, and a degree-5
+// series (truncation |r|^6/6 < 6e-16 for |r| <= 2^-8). For sums weighted by
+// small factors (B1 = sum f_neq ln(f/w) of the entropy function), where the
+// error is multiplied by sum |f_neq| <= rho max|f_neq/f|.
+__device__ __forceinline__ double fast_log_short(double x, const LogEntry* tab) {
+  int64_t bits = __double_as_longlong(x);
+  int e = (int)((bits >> 52) & 0x7ff);
+  if (e == 0) {
+    bits = __double_as_longlong(x * 18014398509481984.0);
+    e = (int)((bits >> 52) & 0x7ff) - 54;
+  }
+  e -= 1023;
+  const int j = (int)((bits >> 45) & (LOG_TABLE - 1));
+  const double m = __longlong_as_double((bits & 0x000fffffffffffffLL) | 0x3ff0000000000000LL);
+  const LogEntry t = tab[j];
+  const double r = fma(m, t.inv, -1.0);
+  double p = 1.0 / 5.0;
+  p = fma(p, r, -1.0 / 4.0);
+  p = fma(p, r, 1.0 / 3.0);
+  p = fma(p, r, -0.5);
+  const double lp = fma(p * r, r, r);
+  return fma(exponent_as_double(e), kLn2, t.hi) + lp;
+}
+
+// Finer table for ln(x) inside the moment-series tier of the entropy function:
+// 1024 intervals, entry {RN(1/c_j), RN(ln(1/inv_j))}, c_j = 1 + (j + 1/2)/1024.
+constexpr int LOG_TABLE_FINE = 1024;
+struct LogEntryFine {
+  double inv;
+  double hi;
+};
+
+// ln(x) with |r| <= 2^-11 after the reduction and
+// log1p(r) = r + r^2 (r/3 - 1/2) + O(r^4), the r^2 tail in FP32:
+// |tail| <= 1.2e-7 with a relative error of a few float roundings, so the
+// result is within 5e-14 of ln(x) (truncation r^4/4 <= 1.4e-14 included).
+// Used for B1 = sum f_neq ln(f/w) when max|f_neq/f| <= 0.0125, where the
+// error is multiplied by sum |f_neq| <= 0.0125 rho.
+__device__ __forceinline__ double fast_log_fine(double x, const LogEntryFine* tab) {
+  int64_t bits = __double_as_longlong(x);
+  int e = (int)((bits >> 52) & 0x7ff);
+  if (e == 0) {
+    bits = __double_as_longlong(x * 18014398509481984.0);
+    e = (int)((bits >> 52) & 0x7ff) - 54;
+  }
+  e -= 1023;
+  const int j = (int)((bits >> 42) & (LOG_TABLE_FINE - 1));
+  const double m = __longlong_as_double((bits & 0x000fffffffffffffLL) | 0x3ff0000000000000LL);
+  const LogEntryFine t = tab[j];
+  const double r = fma(m, t.inv, -1.0);
+  const float rf = narrow_rn(r);
+  const float tail = (rf * rf) * fmaf(rf, 1.0f / 3.0f, -0.5f);
+  return fma(exponent_as_double(e), kLn2, t.hi) + (r + widen_exact(tail));
+}
+
+__device__ __forceinline__ void stage_log_table_fine(LogEntryFine* sh, const LogEntryFine* __restrict__ g) {
+  for (int i = threadIdx.x; i < LOG_TABLE_FINE; i += blockDim.x) sh[i] = g[i];
 }
 
 // Block-cooperative staging of the table into shared memory.

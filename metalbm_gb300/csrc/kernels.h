@@ -28,6 +28,22 @@ cudaError_t f64_to_lowp(int lattice, int storage, const double* in, int q, void*
 cudaError_t fast_log_eval(const double* x, double* out, long long n, const void* table,
                           cudaStream_t s);
 
+// The entropic FP32-storage kernel's entropy function F(x), F'(x) at nodes
+// given as FP32 populations and FP64 f_neq [nodes][Q] (tests); mode 0: the
+// kernel's choice of form, 1: direct, 2: moment series.
+cudaError_t entropy_test(int lattice, const float* f, const double* fneq, long long nodes,
+                         const double* x, int nx, int mode, const void* table, const void* table_fine,
+                         double* F, double* D, int* series, cudaStream_t s);
+cudaError_t entropy_test_L0(const float* f, const double* fneq, long long nodes, const double* x,
+                            int nx, int mode, const void* table, const void* table_fine, double* F, double* D,
+                            int* series, cudaStream_t s);
+cudaError_t entropy_test_L1(const float* f, const double* fneq, long long nodes, const double* x,
+                            int nx, int mode, const void* table, const void* table_fine, double* F, double* D,
+                            int* series, cudaStream_t s);
+cudaError_t entropy_test_L2(const float* f, const double* fneq, long long nodes, const double* x,
+                            int nx, int mode, const void* table, const void* table_fine, double* F, double* D,
+                            int* series, cudaStream_t s);
+
 // Diagnostics: sum the per-block partials in a fixed order (deterministic).
 cudaError_t finalize_diag(const double* partials, int nblocks, double* out, cudaStream_t s);
 

@@ -68,6 +68,15 @@ cudaError_t finalize_diag(const double* partials, int nblocks, double* out, cuda
   if (S == 2) { MLBM_BY_LAT(L, F##_L0_S2 ARGS, F##_L1_S2 ARGS, F##_L2_S2 ARGS) } \
   return cudaErrorInvalidValue;
 
+cudaError_t entropy_test(int lattice, const float* f, const double* fneq, long long nodes,
+                         const double* x, int nx, int mode, const void* table,
+                         const void* table_fine, double* F, double* D, int* series,
+                         cudaStream_t s) {
+  MLBM_BY_LAT(lattice, entropy_test_L0(f, fneq, nodes, x, nx, mode, table, table_fine, F, D, series, s),
+              entropy_test_L1(f, fneq, nodes, x, nx, mode, table, table_fine, F, D, series, s),
+              entropy_test_L2(f, fneq, nodes, x, nx, mode, table, table_fine, F, D, series, s))
+}
+
 cudaError_t step_f64(int lattice, int collision, int forcing, const double* prev, double* next,
                      const StepParams& p, cudaStream_t s) {
   MLBM_BY_LAT(lattice, step_f64_L0(collision, forcing, prev, next, p, s),

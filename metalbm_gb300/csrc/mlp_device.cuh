@@ -46,8 +46,9 @@ __device__ __forceinline__ void mma_bf16_16816(float d[4], const uint32_t a[4], 
       : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
 }
 
-// One 32-node warp tile: rows (the warp's nodes) x features in smem -> guess
-// for this thread's own node. Every lane of the warp must call it.
+// One 32-node warp tile: rows (the warp's nodes) x features in smem -> the
+// guess minus 2 (kept apart so the caller adds 2 in its own precision) for
+// this thread's own node. Every lane of the warp must call it.
 template <int Q>
 __device__ __forceinline__ float mlp_guess_warp(const MlpDev* __restrict__ m, const float x[Q],
                                                 __nv_bfloat16* rows /* 32 x MLP_ROW */,
@@ -152,13 +153,13 @@ __device__ __forceinline__ float mlp_guess_warp(const MlpDev* __restrict__ m, co
     }
   }
   __syncwarp();
-  const float out = 2.0f + m->out_scale * (ysh[lane] + m->b3);
+  const float out = m->out_scale * (ysh[lane] + m->b3);
   __syncwarp();
   return out;
 }
 
 // Block-level entry: every thread of the (128-thread) block calls it with its
-// node's features; returns the guess for that node.
+// node's features; returns the guess minus 2 for that node.
 template <int Q>
 __device__ __forceinline__ float mlp_guess_block(const MlpDev* __restrict__ m, const float x[Q]) {
   __shared__ __align__(16) __nv_bfloat16 rows[4][32 * MLP_ROW];

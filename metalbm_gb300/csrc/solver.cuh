@@ -17,7 +17,16 @@
 
 namespace mlbm {
 
-template <class Eval>
+// kFloatStep: Newton and bisection-Newton steps fe/de in FP32 (a step with a
+// relative error of 1e-7 is still a convergent step; acceptance is decided by
+// the FP64 residual alone).
+template <int kFloatStep>
+__device__ __forceinline__ double newton_step(double fe, double de) {
+  if constexpr (kFloatStep) return widen_exact(__fdiv_rn(narrow_rn(fe), narrow_rn(de)));
+  else return fe / de;
+}
+
+template <class Eval, bool kFloatStep = false>
 __device__ __forceinline__ double residual_alpha_solve(const Eval& eval, double guess,
                                                        double alt, double alphaMax, double tol,
                                                        int maxit, unsigned c[]) {
@@ -47,7 +56,7 @@ __device__ __forceinline__ double residual_alpha_solve(const Eval& eval, double 
       phase = P_NEWTON;
       if (newton_left-- > 0) {
         ++iters;
-        const double xn = x - fe / de;
+        const double xn = x - newton_step<kFloatStep>(fe, de);
         if (xn > 1.0 && xn < alphaMax) { x = xn; continue; }
       }
       ++c[CNT_BISECT];
@@ -83,7 +92,7 @@ __device__ __forceinline__ double residual_alpha_solve(const Eval& eval, double 
         if (xLow == x) { result = x; ok = true; phase = P_DONE; }
       } else {
         dxOld = dx;
-        dx = fe / de;
+        dx = newton_step<kFloatStep>(fe, de);
         const double xt = x;
         x -= dx;
         if (xt == x) { result = x; ok = true; phase = P_DONE; }

@@ -220,7 +220,8 @@ __device__ __forceinline__ void node_force_f(const StepParams& p, uint32_t x, ui
 template <int LAT>
 __device__ __forceinline__ void lowp_store_fields(const StepParams& p, long long idx, float rho,
                                                   const float u[3], const double F[3], bool shifted,
-                                                  double alpha, double& energy, double& mach) {
+                                                  double alpha, double& energy, double& mach,
+                                                  bool write_alpha = true) {
   using L = Lattice<LAT>;
   double uh[3] = {0.0, 0.0, 0.0};
   const double r = (double)rho;
@@ -233,7 +234,7 @@ __device__ __forceinline__ void lowp_store_fields(const StepParams& p, long long
       p.u_out[(long long)k * p.V + idx] = uh[k];
       p.force_out[(long long)k * p.V + idx] = F[k];
     }
-    if (p.alpha_field_f32) p.alpha_field_f32[idx] = (float)alpha;
+    if (p.alpha_field_f32 && write_alpha) p.alpha_field_f32[idx] = narrow_rn(alpha);
   }
   if (p.diag) {
     double e = 0.0, s = 0.0;
@@ -362,153 +363,506 @@ __global__ void __launch_bounds__(256) bgk_lowp_kernel(const typename Storage<ST
 }
 
 // ---- Entropic SRT with an FP64 alpha solve --------------------------------
-// The alpha solve needs f_neq with the exact mass and momentum of the
-// stored state, so the entropic kernel widens the stored populations to FP64
-// and forms rho, u, f_eq and f_neq there; FP32 deviations would leave a
-// residual mass of the order of the storage rounding in f_neq, and F(alpha)
-// would then have no root in [1, alpha_max] on well-resolved flows.
+// The alpha solve needs f_neq with the exact mass and momentum of the stored
+// state, so rho, u, f_eq and f_neq are formed in FP64 from the exact stored
+// values (FP32 deviations would leave a residual mass of the order of the
+// storage rounding in f_neq, and F(alpha) would then have no root in
+// [1, alpha_max] on well-resolved flows). Everything else runs in FP32 or in
+// integer operations: GB300 issues FP64 arithmetic and FP32<->FP64
+// conversions at a small fraction of the FP32 rate, and the kernel is bound by
+// that pipe.
+//   * 1/f_q: an FP32 reciprocal refined by one FP64 Newton step (relative
+//     error ~2^-46);
+//   * alpha_max, the deviation test and the series-tier test: on FP32 r_q;
+//   * F(alpha): the moment series (HSeries) when max|r_q| <= kSeriesRmax, the
+//     log1p form (HLowpDirect) otherwise;
+//   * the update f - alpha beta f_neq (+ forcing) in FP32, rounded once into
+//     the storage format.
+
+// The node's pulled populations as stored: F32 keeps f_q, F16 keeps the exact
+// deviation f_q - w_q.
+template <int LAT, int ST>
+struct Pulled {
+  float v[Lattice<LAT>::Q];
+  __device__ __forceinline__ double f64(int q) const {
+    if constexpr (ST == ST_F32) return widen_exact(v[q]);
+    else return Lattice<LAT>::w(q) + widen_exact(v[q]);
+  }
+  __device__ __forceinline__ float f32(int q) const {
+    if constexpr (ST == ST_F32) return v[q];
+    else return (float)Lattice<LAT>::w(q) + v[q];
+  }
+  __device__ __forceinline__ float dev(int q) const {
+    if constexpr (ST == ST_F32) return v[q] - (float)Lattice<LAT>::w(q);
+    else return v[q];
+  }
+};
+
+// 1/f to ~2^-46 relative: FP32 reciprocal, widened exactly, one Newton step.
+__device__ __forceinline__ double recip_refined(double f, float f32) {
+  const double y0 = widen_exact(__frcp_rn(f32));
+  return fma(y0, fma(-f, y0, 1.0), y0);
+}
+
+// The log1p form of the entropy function (HLog1p, with C0 = B1 since
+// sum f_neq = 0) over the stored populations and r_q.
+template <int LAT, int ST>
+struct HLowpDirect {
+  const Pulled<LAT, ST>* P;
+  const double* r;
+  double B1, rmax;
+  const LogEntry* tab;
+  __device__ __forceinline__ void operator()(double x, double& Fv, double& Dv) const {
+    using L = Lattice<LAT>;
+    double s = 0.0, d = 0.0;
+#pragma unroll
+    for (int q = 0; q < L::Q; ++q) {
+      const double f = P->f64(q);
+      const double t = -x * r[q];
+      const double opt = 1.0 + t;
+      double lp;
+      if (fabs(t) <= 0.015625) lp = log1p_small(t);
+      else if (opt > 0.0) lp = fast_log(opt, tab);
+      else lp = -745.0;  // g = 0 at alpha_max: g ln g -> 0
+      if (opt > 0.0) s = fma(f * opt, lp, s);
+      d = fma(f * r[q], lp, d);
+    }
+    Fv = fma(x, B1, -s);
+    Dv = B1 + d;
+  }
+};
+
+template <int LAT, int ST, bool SERIES>
+struct HLowp {
+  HSeries S;
+  HLowpDirect<LAT, ST> D;
+  __device__ __forceinline__ void operator()(double x, double& Fv, double& Dv) const {
+    if constexpr (SERIES) S(x, Fv, Dv);
+    else D(x, Fv, Dv);
+  }
+};
+
+// Series tiers: above kSeriesM4Rmax the fourth moment is an FP64 sum (its
+// term x^4 M4/12 <= 3.3 rho r^4 would lose up to 1.6e-6 of itself in FP32),
+// below it every moment from M4 on is an FP32 sum (< 1.5e-15 absolute).
+constexpr float kSeriesM4Rmax = 0.004f;
+
+// B1 and the moments (series form), or r_q in place of f_neq_q in n[]
+// (direct form).
+template <int LAT, int ST, bool SERIES>
+__device__ __forceinline__ HLowp<LAT, ST, SERIES> make_entropy_eval(const Pulled<LAT, ST>& P,
+                                                                    double n[], float rabs,
+                                                                    const LogEntry* tab,
+                                                                    const LogEntryFine* fine) {
+  using L = Lattice<LAT>;
+  HLowp<LAT, ST, SERIES> ev;
+  double B1 = 0.0;
+  if constexpr (SERIES) {
+#pragma unroll
+    for (int q = 0; q < L::Q; ++q) B1 = fma(n[q], fast_log_fine(P.f64(q) * (1.0 / L::w(q)), fine), B1);
+    double M2 = 0.0, M3 = 0.0, M4 = 0.0;
+    float M4f = 0.0f, M5 = 0.0f, M6 = 0.0f, M7 = 0.0f, M8 = 0.0f;
+    const bool m4_f64 = rabs > kSeriesM4Rmax;
+#pragma unroll
+    for (int q = 0; q < L::Q; ++q) {
+      const float rcp = __frcp_rn(P.f32(q));
+      const double f = P.f64(q);
+      const double y0 = widen_exact(rcp);
+      const double g = n[q] * fma(y0, fma(-f, y0, 1.0), y0);  // r_q
+      const double p2 = g * n[q];                             // f r^2
+      M2 += p2;
+      M3 = fma(p2, g, M3);
+      if (m4_f64) M4 = fma(p2 * g, g, M4);
+      const float nf = narrow_rn(n[q]);
+      const float rf = nf * rcp;
+      const float r3 = rf * rf * rf;
+      float t = nf * r3;  // f r^4
+      M4f += t;
+      t *= rf; M5 += t;
+      t *= rf; M6 += t;
+      t *= rf; M7 += t;
+      t *= rf; M8 += t;
+    }
+    if (!m4_f64) M4 = widen_exact(M4f);
+    ev.S = HSeries{B1, M2 * 0.5, M3 * (1.0 / 6.0), M4 * (1.0 / 12.0), M2, M3 * 0.5,
+                   M4 * (1.0 / 3.0), M5 * (1.0f / 20.0f), M6 * (1.0f / 30.0f),
+                   M7 * (1.0f / 42.0f), M8 * (1.0f / 56.0f), M5 * 0.25f, M6 * 0.2f,
+                   M7 * (1.0f / 6.0f), M8 * (1.0f / 7.0f)};
+  } else {
+#pragma unroll
+    for (int q = 0; q < L::Q; ++q) {
+      const double f = P.f64(q);
+      B1 = fma(n[q], fast_log_short(f * (1.0 / L::w(q)), tab), B1);
+      n[q] *= recip_refined(f, P.f32(q));
+    }
+  }
+  ev.D = HLowpDirect<LAT, ST>{&P, n, B1, (double)rabs, tab};
+  return ev;
+}
+
+// v * 2^60 as an exact integer for a float |v| < 4 (bits below 2^-60
+// dropped, an absolute 1e-18); `bad` is set for larger or non-finite values.
+__device__ __forceinline__ long long fixed60(float v, bool& bad) {
+  const uint32_t b = __float_as_uint(v);
+  const int e = (int)((b >> 23) & 0xffu);
+  bad |= e >= 129;
+  const long long m = (long long)((b & 0x7fffffu) | (e ? 0x800000u : 0u));
+  const int sh = e - 90;  // v = m 2^(e - 150)
+  const long long a = sh >= 0 ? (m << (sh & 63)) : (m >> min(-sh, 63));
+  return (b >> 31) ? -a : a;
+}
+
+// rho (or rho - 1 for F16 storage, whose stored deviations sum to it) and
+// the momentum as exact fixed-point sums of the stored values, each rounded
+// once to FP64; FP64 sums where a value is out of the fixed-point range.
+template <int LAT, int ST>
+__device__ __forceinline__ void moments_exact(const Pulled<LAT, ST>& P, double& rho, double& rhop,
+                                              double j[3]) {
+  using L = Lattice<LAT>;
+  long long S = 0, J[3] = {0, 0, 0};
+  bool bad = false;
+#pragma unroll
+  for (int q = 0; q < L::Q; ++q) {
+    const long long a = fixed60(P.v[q], bad);
+    S += a;
+#pragma unroll
+    for (int k = 0; k < L::D; ++k) {
+      if (L::c(q, k) > 0) J[k] += a;
+      if (L::c(q, k) < 0) J[k] -= a;
+    }
+  }
+  if (!bad) {
+    const double s = 0x1p-60;
+    const double Sd = (double)S * s;
+    rho = ST == ST_F32 ? Sd : 1.0 + Sd;
+    rhop = ST == ST_F32 ? Sd - 1.0 : Sd;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) j[k] = (double)J[k] * s;
+  } else {
+    rho = P.f64(0);
+    j[0] = j[1] = j[2] = 0.0;
+#pragma unroll
+    for (int q = 1; q < L::Q; ++q) {
+      const double f = P.f64(q);
+      rho += f;
+#pragma unroll
+      for (int k = 0; k < L::D; ++k) {
+        if (L::c(q, k) > 0) j[k] += f;
+        if (L::c(q, k) < 0) j[k] -= f;
+      }
+    }
+    rhop = rho - 1.0;
+  }
+}
+
+// f_neq_q = f_q - rho w_q (1 + P_q) = (f_q - rho w_q) - rho w_q P_q with the
+// TruncationMa3 polynomial in its pair form P(+-cu) = E +- O (Equilibrium.h:17-33).
+// f_q - rho w_q is formed from the stored value: f_q - rho w_q for F32,
+// (f_q - w_q) - (rho - 1) w_q for F16.
+template <int LAT, int ST>
+__device__ __forceinline__ void neq_pairs(const Pulled<LAT, ST>& P, double rho, double rhop,
+                                          const double u[3], double n[]) {
+  using L = Lattice<LAT>;
+  const double u2 = u[0] * u[0] + u[1] * u[1] + u[2] * u[2];
+  const double common = u2 * (1.125 * u2 - 1.5);
+  const double A = fma(-6.75, u2, 4.5), B = fma(-4.5, u2, 3.0);
+  auto base = [&](int q) {
+    if constexpr (ST == ST_F32) return P.f64(q) - rho * L::w(q);
+    else return widen_exact(P.v[q]) - rhop * L::w(q);
+  };
+  n[0] = fma(-rho * L::w(0), common, base(0));
+#pragma unroll
+  for (int q = 1; q < L::Q; ++q) {
+    if (is_pair_leader<LAT>(q)) {
+      const int qb = opposite<LAT>(q);
+      double cu = 0.0;
+#pragma unroll
+      for (int k = 0; k < L::D; ++k) {
+        if (L::c(q, k) > 0) cu += u[k];
+        if (L::c(q, k) < 0) cu -= u[k];
+      }
+      const double c2 = cu * cu;
+      const double E = fma(c2, fma(3.375, c2, A), common);
+      const double O = cu * fma(4.5, c2, B);
+      const double rw = rho * L::w(q);
+      n[q] = fma(-rw, E + O, base(q));
+      n[qb] = fma(-rw, E - O, base(qb));
+    }
+  }
+}
+
+// The entropic step runs as two kernels. The main pass completes every node
+// whose deviations allow the moment-series entropy function (all of them on
+// resolved flows), the alpha = 2 shortcut and the alpha_max-limited nodes,
+// and appends the others to a worklist; a persistent second pass finishes the
+// listed nodes with the log1p form. Each kernel's register allocation then
+// covers one form only (the series-only main pass fits 3 blocks of 128
+// threads per SM without spills).
+enum : int { ELBM_MAIN = 0, ELBM_DEFERRED = 1 };
+
+template <int LAT, int FS, int ST, bool LEARNED, int MODE>
+__device__ __forceinline__ void elbm_node(const typename Storage<ST>::T* __restrict__ prev,
+                                          typename Storage<ST>::T* __restrict__ next,
+                                          const StepParams& p, bool active, long long idx,
+                                          const LogEntry* s_log, const LogEntryFine* s_fine,
+                                          unsigned cnt[], bool& defer, double& mass,
+                                          double& energy, double& mach, double& amin,
+                                          double& amax) {
+  using L = Lattice<LAT>;
+  Pulled<LAT, ST> P;
+  uint32_t x = 0, y = 0, z = 0;
+  if (active) {
+    node_coords(p, idx, x, y, z);
+    const PullOffsets o = pull_offsets(p, x, y, z);
+#pragma unroll
+    for (int q = 0; q < L::Q; ++q) {
+      const auto* src = prev + (long long)q * p.V + o.at(L::c(q, 0), L::c(q, 1), L::c(q, 2));
+      if constexpr (ST == ST_F32) P.v[q] = __ldg(src);
+      else P.v[q] = __half2float(__ldg(src)) * (1.0f / (float)(1 << shift_exponent<LAT>(q)));
+    }
+  } else {
+#pragma unroll
+    for (int q = 0; q < L::Q; ++q) P.v[q] = ST == ST_F32 ? (float)L::w(q) : 0.0f;
+  }
+  // Learned guess: every thread of the block takes part (tile inference), on
+  // features f_neq / rho from the FP32 deviations.
+  float learned = 0.0f;
+  if (LEARNED) {
+    float dv[L::Q], rhop, rf, uf[3], deq[L::Q];
+#pragma unroll
+    for (int q = 0; q < L::Q; ++q) dv[q] = P.dev(q);
+    moments_dev<LAT>(dv, rhop, rf, uf);
+    eq_dev<LAT>(rhop, rf, uf, uf[0] * uf[0] + uf[1] * uf[1] + uf[2] * uf[2], deq);
+    const float irf = 1.0f / rf;
+    float xin[L::Q];
+#pragma unroll
+    for (int q = 0; q < L::Q; ++q) xin[q] = (dv[q] - deq[q]) * irf;
+    learned = mlp_guess_block<L::Q>(reinterpret_cast<const MlpDev*>(p.mlp), xin);
+  }
+  if (!active) return;
+  double rho, rhop, j[3], u[3];
+  moments_exact<LAT, ST>(P, rho, rhop, j);
+  const double ir = recip_refined(rho, narrow_rn(rho));
+#pragma unroll
+  for (int k = 0; k < 3; ++k) u[k] = j[k] * ir;
+  // n_q = f_neq_q; r_q = n_q / f_q in FP32 for the bracket and the tests
+  double n[L::Q];
+  neq_pairs<LAT, ST>(P, rho, rhop, u, n);
+  float rpos = 0.0f, rabs = 0.0f;
+#pragma unroll
+  for (int q = 0; q < L::Q; ++q) {
+    const float rq = narrow_rn(n[q]) * __frcp_rn(P.f32(q));
+    rpos = fmaxf(rpos, rq);
+    rabs = fmaxf(rabs, fabsf(rq));
+  }
+  // alpha_max = min(2.5, 1 / max_q r_q) over r_q > 0 (Collision.h:305-326);
+  // the deviation test |f_neq|/f <= threshold (Collision.h:284-303)
+  const bool small = !(rabs > p.deviation_threshold_f);
+  const double alphaMax = rpos > 0.4f ? widen_exact(__frcp_rn(rpos)) : 2.5;
+  double alpha = 2.0;
+  bool direct = false;  // n[] holds r_q instead of f_neq_q
+  if (MODE == ELBM_MAIN && small) { ++cnt[CNT_SHORTCUT]; alpha = 2.0; }
+  else if (MODE == ELBM_MAIN && alphaMax < 2.0) { ++cnt[CNT_LIMITED]; alpha = 0.95 * alphaMax; }
+  else {
+    const bool series = MODE == ELBM_MAIN && rabs <= kSeriesRmax;
+    if (MODE == ELBM_MAIN && !series) {
+      defer = true;
+    } else {
+      ++cnt[CNT_SOLVED];
+      if (series) ++cnt[CNT_SERIES];
+      direct = !series;
+      const double prevA = widen_exact(p.alpha_field_f32[idx]);
+      const double plain = p.guess_mode == GUESS_TWO ? 2.0 : prevA;
+      const double guess = LEARNED ? 2.0 + widen_exact(learned) : plain;
+      if constexpr (MODE == ELBM_MAIN) {
+        const auto ev = make_entropy_eval<LAT, ST, true>(P, n, rabs, s_log, s_fine);
+        alpha = residual_alpha_solve<decltype(ev), true>(ev, guess, plain, alphaMax, p.newton_tol,
+                                                         p.newton_maxit, cnt);
+      } else {
+        const auto ev = make_entropy_eval<LAT, ST, false>(P, n, rabs, s_log, s_fine);
+        alpha = residual_alpha_solve<decltype(ev), true>(ev, guess, plain, alphaMax, p.newton_tol,
+                                                         p.newton_maxit, cnt);
+      }
+    }
+  }
+  if (!defer) {
+    // update in FP32: f - alpha beta f_neq + S (Collision.h:243-258)
+    const float ab = narrow_rn(alpha * p.beta);
+    float uf[3] = {0.0f, 0.0f, 0.0f}, Ff[3] = {0.0f, 0.0f, 0.0f}, rf = 1.0f, uF = 0.0f;
+    PolyNode nu{0.0f, 0.0f}, nv{0.0f, 0.0f};
+    float vf[3] = {0.0f, 0.0f, 0.0f};
+    if (FS != FS_NONE) {
+      node_force_float<L::D>(p, x, y, z, Ff);
+#pragma unroll
+      for (int k = 0; k < 3; ++k) uf[k] = narrow_rn(u[k]);
+      rf = narrow_rn(rho);
+      uF = uf[0] * Ff[0] + uf[1] * Ff[1] + uf[2] * Ff[2];
+      if (FS == FS_EDM) {
+        nu = poly_node(uf[0] * uf[0] + uf[1] * uf[1] + uf[2] * uf[2]);
+        const float irf = 1.0f / rf;
+#pragma unroll
+        for (int k = 0; k < 3; ++k) vf[k] = fmaf(Ff[k], irf, uf[k]);
+        nv = poly_node(vf[0] * vf[0] + vf[1] * vf[1] + vf[2] * vf[2]);
+      }
+    }
+    float src[L::Q];
+#pragma unroll
+    for (int q = 0; q < L::Q; ++q) src[q] = 0.0f;
+    if (FS == FS_GUO || FS == FS_EDM) {
+      if (FS == FS_GUO) src[0] = -(p.guo_kt_f * (float)L::w(0)) * uF;
+      else src[0] = (float)L::w(0) * rf * (nv.common - nu.common);
+#pragma unroll
+      for (int q = 1; q < L::Q; ++q) {
+        if (is_pair_leader<LAT>(q)) {
+          const int qb = opposite<LAT>(q);
+          const float w = (float)L::w(q);
+          if (FS == FS_GUO) {
+            // S_q = kt w_q [(c_q - u).F + 3 (c_q.u)(c_q.F)] (ForcingScheme.h:100-117)
+            const float cF = cdotf<LAT>(q, Ff);
+            const float Es = fmaf(3.0f * cdotf<LAT>(q, uf), cF, -uF);
+            const float kw = p.guo_kt_f * w;
+            src[q] = kw * (Es + cF);
+            src[qb] = kw * (Es - cF);
+          } else {
+            // S_q = f_eq(rho, u + F/rho) - f_eq(rho, u) (ForcingScheme.h:183-197)
+            float E, O, Ev, Ov;
+            poly_pair(nu, cdotf<LAT>(q, uf), E, O);
+            poly_pair(nv, cdotf<LAT>(q, vf), Ev, Ov);
+            const float wr = w * rf;
+            src[q] = wr * ((Ev + Ov) - (E + O));
+            src[qb] = wr * ((Ev - Ov) - (E - O));
+          }
+        }
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < L::Q; ++q) {
+      const float nf = direct ? narrow_rn(n[q] * P.f64(q)) : narrow_rn(n[q]);
+      float rr = fmaf(-ab, nf, P.v[q]);  // f (F32) or f - w (F16)
+      if (FS == FS_GUO || FS == FS_EDM) rr += src[q];
+      auto* dst = next + (long long)q * p.V + idx;
+      if constexpr (ST == ST_F32) *dst = rr;
+      else *dst = __float2half_rn(rr * (float)(1 << shift_exponent<LAT>(q)));
+    }
+    const float stored = narrow_rn(alpha);  // alpha persists in FP32
+    p.alpha_field_f32[idx] = stored;
+    if (p.diag) {
+      amin = fmin(amin, widen_exact(stored));
+      amax = fmax(amax, widen_exact(stored));
+    }
+  }
+  if (MODE == ELBM_MAIN) {
+    if (!(rho > 0.0) || !isfinite(rho)) atomicOr(p.err_word, ERR_NONFINITE);
+    if (p.store || p.diag) {
+      // rho, u_hydro and F of every node; alpha by the kernel that solves it
+      mass = rho;
+      double F[3] = {0.0, 0.0, 0.0};
+      if (FS != FS_NONE) node_force<L::D>(p, x, y, z, F);
+      const float ufl[3] = {narrow_rn(u[0]), narrow_rn(u[1]), narrow_rn(u[2])};
+      lowp_store_fields<LAT>(p, idx, narrow_rn(rho), ufl, F, FS != FS_NONE, alpha, energy, mach,
+                             !defer);
+    }
+  }
+}
+
+// Resident blocks per SM the main pass's register allocation is sized for.
+#ifndef MLBM_ELBM_MIN_BLOCKS
+#define MLBM_ELBM_MIN_BLOCKS 3
+#endif
+
 template <int LAT, int FS, int ST, bool LEARNED>
-__global__ void __launch_bounds__(128) elbm_lowp_kernel(const typename Storage<ST>::T* __restrict__ prev,
+__global__ void __launch_bounds__(128, MLBM_ELBM_MIN_BLOCKS) elbm_lowp_kernel(const typename Storage<ST>::T* __restrict__ prev,
                                                         typename Storage<ST>::T* __restrict__ next,
                                                         StepParams p) {
-  using L = Lattice<LAT>;
-  __shared__ LogEntry s_log[LOG_TABLE];
-  stage_log_table(s_log, reinterpret_cast<const LogEntry*>(p.log_table));
+  __shared__ LogEntryFine s_fine[LOG_TABLE_FINE];
+  stage_log_table_fine(s_fine, reinterpret_cast<const LogEntryFine*>(p.log_table_fine));
+  // the worklist counter of the next step (its last reader was the previous
+  // step's second pass, which has completed)
+  if (blockIdx.x == 0 && threadIdx.x == 0) p.defer_count[p.parity ^ 1] = 0u;
   __syncthreads();
   const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const bool active = idx < p.V;
   double mass = 0.0, energy = 0.0, mach = 0.0, amin = 1e300, amax = -1e300;
   unsigned cnt[CNT_COUNT] = {0, 0, 0, 0, 0, 0, 0, 0};
-  double f[L::Q];
-  uint32_t x = 0, y = 0, z = 0;
-  float learned = 2.0f;
-  {
-    float dv[L::Q];  // FP32 deviations f - w (model features)
-    if (active) {
-      node_coords(p, idx, x, y, z);
-      const PullOffsets o = pull_offsets(p, x, y, z);
-#pragma unroll
-      for (int q = 0; q < L::Q; ++q) {
-        const auto* src = prev + (long long)q * p.V + o.at(L::c(q, 0), L::c(q, 1), L::c(q, 2));
-        if constexpr (ST == ST_F32) {
-          const float v = __ldg(src);
-          f[q] = widen_exact(v);  // exact, without a conversion instruction
-          dv[q] = v - (float)L::w(q);
-        } else {
-          const float dev = __half2float(__ldg(src)) * (1.0f / (float)(1 << shift_exponent<LAT>(q)));
-          f[q] = L::w(q) + widen_exact(dev);
-          dv[q] = dev;
-        }
-      }
-    } else {
-#pragma unroll
-      for (int q = 0; q < L::Q; ++q) { f[q] = L::w(q); dv[q] = 0.0f; }
-    }
-    // Learned guess: every thread of the block takes part (tile inference),
-    // on features f_neq / rho from the FP32 deviations (the BF16 inference
-    // does not need FP64 inputs).
-    if (LEARNED) {
-      float rhop, rf, uf[3], deq[L::Q];
-      moments_dev<LAT>(dv, rhop, rf, uf);
-      eq_dev<LAT>(rhop, rf, uf, uf[0] * uf[0] + uf[1] * uf[1] + uf[2] * uf[2], deq);
-      const float irf = 1.0f / rf;
-      float xin[L::Q];
-#pragma unroll
-      for (int q = 0; q < L::Q; ++q) xin[q] = (dv[q] - deq[q]) * irf;
-      learned = mlp_guess_block<L::Q>(reinterpret_cast<const MlpDev*>(p.mlp), xin);
-    }
-  }
-  if (active) {
-    double rho = f[0], j[3] = {0.0, 0.0, 0.0}, u[3], F[3] = {0.0, 0.0, 0.0};
-#pragma unroll
-    for (int q = 1; q < L::Q; ++q) {
-      rho += f[q];
-#pragma unroll
-      for (int k = 0; k < L::D; ++k) {
-        if (L::c(q, k) > 0) j[k] += f[q];
-        if (L::c(q, k) < 0) j[k] -= f[q];
-      }
-    }
-    const double ir = 1.0 / rho;
-#pragma unroll
-    for (int k = 0; k < 3; ++k) u[k] = j[k] * ir;
-    if (FS != FS_NONE) node_force<L::D>(p, x, y, z, F);
-    // r_q = f_neq_q / f_q; alpha_max = min(2.5, 1 / max_q r_q) over r_q > 0
-    // (Collision.h:305-326); the deviation test |f_neq|/f <= threshold
-    // (Collision.h:284-303) on |r_q|.
-    double r[L::Q], rpos = 0.0, rabs = 0.0;
-    feq_pairs_f64<LAT>(rho, u, r);
-#pragma unroll
-    for (int q = 0; q < L::Q; ++q) {
-      r[q] = (f[q] - r[q]) / f[q];
-      rpos = fmax(rpos, r[q]);
-      rabs = fmax(rabs, fabs(r[q]));
-    }
-    const bool small = !(rabs > p.deviation_threshold);
-    const double alphaMax = rpos > 0.4 ? 1.0 / rpos : 2.5;
-    double alpha;
-    if (small) { ++cnt[CNT_SHORTCUT]; alpha = 2.0; }
-    else if (alphaMax < 2.0) { ++cnt[CNT_LIMITED]; alpha = 0.95 * alphaMax; }
-    else {
-      ++cnt[CNT_SOLVED];
-      const double prevA = widen_exact(p.alpha_field_f32[idx]);
-      const double plain = p.guess_mode == GUESS_TWO ? 2.0 : prevA;
-      const double guess = LEARNED ? widen_exact(learned) : plain;
-      double B1 = 0.0, sfn = 0.0;
-#pragma unroll
-      for (int q = 0; q < L::Q; ++q) {
-        const double fnq = r[q] * f[q];
-        B1 = fma(fnq, fast_log(f[q] * (1.0 / L::w(q)), s_log), B1);
-        sfn += fnq;
-      }
-      const HLog1p<LAT> ev{f, r, B1, sfn + B1, rabs, s_log};
-      alpha = residual_alpha_solve(ev, guess, plain, alphaMax, p.newton_tol, p.newton_maxit, cnt);
-    }
-    const double ab = alpha * p.beta;
-    double fsh[FS == FS_EDM ? L::Q : 1];
-    if (FS == FS_EDM) {
-      double v[3];
-#pragma unroll
-      for (int k = 0; k < 3; ++k) v[k] = u[k] + F[k] / rho;
-      feq_pairs_f64<LAT>(rho, v, fsh);
-    }
-#pragma unroll
-    for (int q = 0; q < L::Q; ++q) {
-      // f - alpha beta f_neq + S  (Collision.h:243-258), f_neq = r f
-      const double fnq = r[q] * f[q];
-      double rr = fma(-ab, fnq, f[q]);
-      if (FS == FS_GUO) {
-        double cu = 0.0;
-#pragma unroll
-        for (int k = 0; k < L::D; ++k) {
-          if (L::c(q, k) > 0) cu += u[k];
-          if (L::c(q, k) < 0) cu -= u[k];
-        }
-        double R = 0.0;
-#pragma unroll
-        for (int k = 0; k < L::D; ++k) R = fma((double)L::c(q, k) - u[k] + L::c(q, k) * 3.0 * cu, F[k], R);
-        rr += p.guo_k[q] * R;
-      }
-      if (FS == FS_EDM) rr += fsh[q] - (f[q] - fnq);
-      auto* dst = next + (long long)q * p.V + idx;
-      if constexpr (ST == ST_F32) {
-        *dst = narrow_rn(rr);
-      } else {
-        *dst = __float2half_rn(narrow_rn((rr - L::w(q)) * (double)(1 << shift_exponent<LAT>(q))));
-      }
-    }
-    p.alpha_field_f32[idx] = narrow_rn(alpha);
-    if (!(rho > 0.0) || !isfinite(rho)) atomicOr(p.err_word, ERR_NONFINITE);
-    if (p.store || p.diag) {
-      mass = rho;
-      amin = alpha;
-      amax = alpha;
-      const float uf[3] = {(float)u[0], (float)u[1], (float)u[2]};
-      lowp_store_fields<LAT>(p, idx, (float)rho, uf, F, FS != FS_NONE, alpha, energy, mach);
-    }
+  bool defer = false;
+  elbm_node<LAT, FS, ST, LEARNED, ELBM_MAIN>(prev, next, p, active, idx, nullptr, s_fine, cnt,
+                                             defer, mass, energy, mach, amin, amax);
+  // warp-aggregated append to the worklist
+  const unsigned m = __ballot_sync(0xffffffffu, defer);
+  if (m) {
+    const int lane = threadIdx.x & 31, leader = __ffs(m) - 1;
+    unsigned base = 0;
+    if (lane == leader) base = atomicAdd(p.defer_count + p.parity, (unsigned)__popc(m));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (defer) p.defer_list[base + __popc(m & ((1u << lane) - 1u))] = (unsigned)idx;
   }
   add_counters(p.counters, cnt);
   if (p.diag) block_reduce_diag(mass, energy, mach, amin, amax, p.diag_partials);
+}
+
+// Second pass over the worklist (grid-stride; p.defer_blocks blocks).
+template <int LAT, int FS, int ST, bool LEARNED>
+__global__ void __launch_bounds__(128) elbm_lowp_deferred_kernel(const typename Storage<ST>::T* __restrict__ prev,
+                                                                 typename Storage<ST>::T* __restrict__ next,
+                                                                 StepParams p) {
+  __shared__ LogEntry s_log[LOG_TABLE];
+  stage_log_table(s_log, reinterpret_cast<const LogEntry*>(p.log_table));
+  __syncthreads();
+  const long long count = (long long)p.defer_count[p.parity];
+  double mass = 0.0, energy = 0.0, mach = 0.0, amin = 1e300, amax = -1e300;
+  unsigned cnt[CNT_COUNT] = {0, 0, 0, 0, 0, 0, 0, 0};
+  for (long long b = (long long)blockIdx.x * blockDim.x; b < count;
+       b += (long long)gridDim.x * blockDim.x) {
+    const long long i = b + threadIdx.x;
+    const bool active = i < count;
+    const long long idx = active ? (long long)p.defer_list[i] : 0;
+    bool defer = false;
+    elbm_node<LAT, FS, ST, LEARNED, ELBM_DEFERRED>(prev, next, p, active, idx, s_log, nullptr, cnt,
+                                                   defer, mass, energy, mach, amin, amax);
+  }
+  add_counters(p.counters, cnt);
+  if (p.diag)
+    block_reduce_diag(0.0, 0.0, 0.0, amin, amax,
+                      p.diag_partials + (size_t)p.defer_slot0 * DIAG_FIELDS);
+}
+
+// ---- entropy-function test hook ---------------------------------------------
+// F(x), F'(x) of nodes given as FP32 populations and FP64 f_neq, through the
+// same construction as the step kernel; mode 0 picks the form as the kernel
+// does, 1 forces the direct form, 2 the series form.
+template <int LAT>
+__global__ void entropy_test_kernel(const float* __restrict__ f, const double* __restrict__ fneq,
+                                    long long nodes, const double* __restrict__ xs, int nx,
+                                    int mode, const LogEntry* __restrict__ table,
+                                    const LogEntryFine* __restrict__ table_fine,
+                                    double* __restrict__ Fo, double* __restrict__ Do,
+                                    int* __restrict__ series_out) {
+  using L = Lattice<LAT>;
+  __shared__ LogEntry s_log[LOG_TABLE];
+  __shared__ LogEntryFine s_fine[LOG_TABLE_FINE];
+  stage_log_table(s_log, table);
+  stage_log_table_fine(s_fine, table_fine);
+  __syncthreads();
+  const long long s = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= nodes) return;
+  Pulled<LAT, ST_F32> P;
+  double n[L::Q];
+  float rabs = 0.0f;
+#pragma unroll
+  for (int q = 0; q < L::Q; ++q) {
+    P.v[q] = f[s * L::Q + q];
+    n[q] = fneq[s * L::Q + q];
+    rabs = fmaxf(rabs, fabsf(narrow_rn(n[q]) * __frcp_rn(P.v[q])));
+  }
+  const bool series = mode == 2 || (mode == 0 && rabs <= kSeriesRmax);
+  if (series) {
+    const auto ev = make_entropy_eval<LAT, ST_F32, true>(P, n, rabs, s_log, s_fine);
+    for (int i = 0; i < nx; ++i) ev(xs[i], Fo[s * nx + i], Do[s * nx + i]);
+  } else {
+    const auto ev = make_entropy_eval<LAT, ST_F32, false>(P, n, rabs, s_log, s_fine);
+    for (int i = 0; i < nx; ++i) ev(xs[i], Fo[s * nx + i], Do[s * nx + i]);
+  }
+  series_out[s] = series ? 1 : 0;
 }
 
 // ---- init and conversions ---------------------------------------------------
@@ -614,10 +968,13 @@ static cudaError_t launch_lowp(int collision, const void* prev, void* next, cons
   } else {
     const int bs = 128;
     const unsigned grid = (unsigned)((p.V + bs - 1) / bs);
-    if (p.guess_mode == GUESS_LEARNED)
+    if (p.guess_mode == GUESS_LEARNED) {
       elbm_lowp_kernel<LAT, FS, ST, true><<<grid, bs, 0, s>>>((const T*)prev, (T*)next, p);
-    else
+      elbm_lowp_deferred_kernel<LAT, FS, ST, true><<<p.defer_blocks, bs, 0, s>>>((const T*)prev, (T*)next, p);
+    } else {
       elbm_lowp_kernel<LAT, FS, ST, false><<<grid, bs, 0, s>>>((const T*)prev, (T*)next, p);
+      elbm_lowp_deferred_kernel<LAT, FS, ST, false><<<p.defer_blocks, bs, 0, s>>>((const T*)prev, (T*)next, p);
+    }
   }
   return cudaGetLastError();
 }
@@ -658,6 +1015,19 @@ cudaError_t MLBM_FN(f64_to_lowp_L)(const double* in, int q, void* f, long long V
   encode_kernel<MLBM_LAT, MLBM_ST><<<(unsigned)((V + 255) / 256), 256, 0, s>>>(in, q, (StT*)f, V);
   return cudaGetLastError();
 }
+
+#if MLBM_ST == 1
+cudaError_t MLBM_CAT(entropy_test_L, MLBM_LAT, , )(const float* f, const double* fneq, long long nodes,
+                                                  const double* x, int nx, int mode,
+                                                  const void* table, const void* table_fine,
+                                                  double* F, double* D, int* series,
+                                                  cudaStream_t s) {
+  entropy_test_kernel<MLBM_LAT><<<(unsigned)((nodes + 127) / 128), 128, 0, s>>>(
+      f, fneq, nodes, x, nx, mode, (const LogEntry*)table, (const LogEntryFine*)table_fine, F, D,
+      series);
+  return cudaGetLastError();
+}
+#endif
 
 cudaError_t MLBM_FN(log_samples_lowp_L)(const void* prev, const StepParams& p,
                                         const long long* nodes, long long n, double* features,

@@ -249,6 +249,56 @@ def test_mixed_entropic_tracks_f64():
 
 
 @pytest.mark.gpu
+def test_mixed_entropic_series_form_tracks_f64():
+    """At 64^3 most entropic nodes have max|f_neq/f| <= 0.0125 and take the
+    moment-series entropy function; alpha and u follow the FP64 step (whose
+    residual solve is bit-identical to the oracle's)."""
+    from metalbm_gb300 import InputDeck, Lattice, fields
+    shape = (64, 64, 64)
+    rho, u = fields.taylor_green(shape, u0=0.05)
+    out = {}
+    for st in ("f64", "f32"):
+        with Lattice(InputDeck(latticeT="D3Q27", collisionT="ELBM", relaxationTime=0.50025,
+                               globalLength=shape, storage=st, alphaSolver="residual",
+                               newtonTolerance=1e-12, deviationThreshold=0.0)) as lat:
+            lat.init_equilibrium(rho, u)
+            lat.step(6, store=True)
+            out[st] = lat.fields()
+            out[st + "_d"] = lat.diagnostics()
+    d = out["f32_d"]
+    assert d["fallback_nodes"] == 0 and d["solved_nodes"] > 0
+    assert d["series_nodes"] >= 0.5 * d["solved_nodes"]
+    assert np.abs(out["f32"]["alpha"] - out["f64"]["alpha"]).max() <= 1e-6
+    assert rel(out["f32"]["u"], out["f64"]["u"]) <= 1e-4
+
+
+@pytest.mark.gpu
+def test_two_pass_entropic_step_is_deterministic():
+    """The FP32 entropic step finishes large-deviation nodes in a second pass
+    over a worklist filled by atomics: results do not depend on the list's
+    order or on how the steps are grouped into calls, and the alpha range of
+    the diagnostics covers the nodes of both passes."""
+    from metalbm_gb300 import InputDeck, Lattice, fields
+    shape = (48, 40, 36)
+    rho, u = fields.taylor_green(shape, u0=0.05)
+    deck = InputDeck(latticeT="D3Q27", collisionT="ELBM", relaxationTime=0.50025,
+                     globalLength=shape, storage="f32", alphaSolver="residual",
+                     newtonTolerance=1e-12, deviationThreshold=0.0)
+    runs = []
+    for grouping in ([5], [1, 1, 1, 1, 1], [2, 3]):
+        with Lattice(deck) as lat:
+            lat.init_equilibrium(rho, u)
+            for k, n in enumerate(grouping):
+                lat.step(n, store=k == len(grouping) - 1, diagnostics=k == len(grouping) - 1)
+            runs.append((lat.populations(), lat.fields()["alpha"], lat.diagnostics()))
+    f0, a0, d0 = runs[0]
+    for f, a, d in runs[1:]:
+        assert np.array_equal(f, f0) and np.array_equal(a, a0)
+    assert 0 < d0["series_nodes"] < d0["solved_nodes"]  # both passes ran
+    assert d0["alpha_min"] == a0.min() and d0["alpha_max"] == a0.max()
+
+
+@pytest.mark.gpu
 def test_error_word_and_timeout_paths():
     """A NaN population sets the device error word (no trap); mlbm_sync
     reports it as MLBM_ERR_NUMERIC and the context stays usable."""
