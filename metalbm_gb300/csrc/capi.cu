@@ -15,6 +15,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <memory>
 #include <mutex>
 #include <new>
 #include <string>
@@ -250,12 +251,50 @@ static void release(mlbm_handle* h) {
 // Table of the FP64 logarithm (fastlog.cuh): for the centre c_j of each of
 // the 128 mantissa intervals, inv_j = RN(1/c_j) and -ln(inv_j) split into a
 // double-double, evaluated in the host's extended precision.
-static void make_log_table_fine(LogEntryFine* t) {
+// Lattice weights in the reference's population order (Lattice.h:145-210,
+// 535-612, 614-703).
+static const double* lattice_weights(int lattice) {
+  static const double w9[9] = {4.0 / 9.0, 1.0 / 36.0, 1.0 / 9.0, 1.0 / 36.0, 1.0 / 36.0,
+                               1.0 / 9.0, 1.0 / 36.0, 1.0 / 9.0, 1.0 / 9.0};
+  static const double w19[19] = {1.0 / 3.0,  1.0 / 18.0, 1.0 / 36.0, 1.0 / 36.0, 1.0 / 36.0,
+                                 1.0 / 36.0, 1.0 / 18.0, 1.0 / 36.0, 1.0 / 36.0, 1.0 / 36.0,
+                                 1.0 / 36.0, 1.0 / 18.0, 1.0 / 18.0, 1.0 / 36.0, 1.0 / 36.0,
+                                 1.0 / 18.0, 1.0 / 18.0, 1.0 / 36.0, 1.0 / 36.0};
+  static double w27[27];
+  static std::once_flag once;
+  std::call_once(once, [] {
+    const double v[4] = {8.0 / 27.0, 2.0 / 27.0, 1.0 / 54.0, 1.0 / 216.0};
+    for (int q = 0; q < 27; ++q) {
+      const int cls = (q == 0) ? 0 : ((q == 1 || q == 10 || q == 19 || q == 20 || q == 23 || q == 24) ? 1
+                        : ((q >= 6 && q <= 9) || (q >= 15 && q <= 18)) ? 3 : 2);
+      w27[q] = v[cls];
+    }
+  });
+  return lattice == MLBM_D2Q9 ? w9 : (lattice == MLBM_D3Q19 ? w19 : w27);
+}
+
+// Fine log table (1024 x {RN(1/c_j), RN(ln(1/inv_j))}) followed by the
+// lattice's constants C_q(d) = d ln 2 - ln(m_q), w_q = m_q 2^e_q.
+struct FineTable {
+  LogEntryFine t[LOG_TABLE_FINE];
+  double lnw[LNW_CONSTS];
+};
+static void make_log_table_fine(FineTable* ft, int lattice) {
   for (int j = 0; j < LOG_TABLE_FINE; ++j) {
     const double c = 1.0 + (j + 0.5) / (double)LOG_TABLE_FINE;
     const double inv = 1.0 / c;
-    t[j].inv = inv;
-    t[j].hi = (double)(-std::log((long double)inv));
+    ft->t[j].inv = inv;
+    ft->t[j].hi = (double)(-std::log((long double)inv));
+  }
+  const double* wl = lattice_weights(lattice);
+  const int Q = lattice == MLBM_D2Q9 ? 9 : (lattice == MLBM_D3Q19 ? 19 : 27);
+  for (int q = 0; q < 27; ++q) {
+    const double wq = q < Q ? wl[q] : 1.0;
+    int ew = 0;
+    const long double mw = 2.0L * std::frexp((long double)wq, &ew);  // wq = mw 2^(ew - 1)
+    for (int d = -1; d <= 1; ++d)
+      ft->lnw[3 * q + d + 1] =
+          (double)((long double)d * 0.693147180559945309417232121458176568L - std::log(mw));
   }
 }
 
@@ -400,16 +439,16 @@ extern "C" int mlbm_create(const mlbm_config* cfg, mlbm_handle** out) {
       (rc = device_alloc(h, (void**)&h->err_word, sizeof(unsigned))) ||
       (rc = device_alloc(h, (void**)&h->mlp, sizeof(MlpDev))) ||
       (rc = device_alloc(h, (void**)&h->log_table, sizeof(LogEntry) * LOG_TABLE)) ||
-      (rc = device_alloc(h, (void**)&h->log_table_fine, sizeof(LogEntryFine) * LOG_TABLE_FINE)))
+      (rc = device_alloc(h, (void**)&h->log_table_fine, sizeof(FineTable))))
     return bail(rc);
   {
     LogEntry tab[LOG_TABLE];
     make_log_table(tab);
-    static LogEntryFine fine[LOG_TABLE_FINE];
-    static std::once_flag fine_once;
-    std::call_once(fine_once, [] { make_log_table_fine(fine); });
+    std::unique_ptr<FineTable> fine(new FineTable);
+    make_log_table_fine(fine.get(), c.lattice);
     if (cudaMemcpy(h->log_table, tab, sizeof tab, cudaMemcpyHostToDevice) != cudaSuccess ||
-        cudaMemcpy(h->log_table_fine, fine, sizeof fine, cudaMemcpyHostToDevice) != cudaSuccess) {
+        cudaMemcpy(h->log_table_fine, fine.get(), sizeof(FineTable), cudaMemcpyHostToDevice) !=
+            cudaSuccess) {
       h->error = "log table upload failed";
       return bail(MLBM_ERR_CUDA);
     }
@@ -937,8 +976,8 @@ extern "C" int mlbm_testing_entropy(int lattice, const float* f, const double* f
   const int Q = lattice == 0 ? 9 : (lattice == 1 ? 19 : 27);
   LogEntry tab[LOG_TABLE];
   make_log_table(tab);
-  LogEntryFine fine[LOG_TABLE_FINE];
-  make_log_table_fine(fine);
+  std::unique_ptr<FineTable> fine(new FineTable);
+  make_log_table_fine(fine.get(), lattice);
   const size_t nf = sizeof(float) * Q * nodes, nn = sizeof(double) * Q * nodes,
                nxb = sizeof(double) * nx, no = sizeof(double) * nx * nodes,
                ns = sizeof(int) * nodes;
@@ -951,7 +990,7 @@ extern "C" int mlbm_testing_entropy(int lattice, const float* f, const double* f
   if (cudaMalloc(&df, nf) != cudaSuccess || cudaMalloc(&dn, nn) != cudaSuccess ||
       cudaMalloc(&dx, nxb) != cudaSuccess || cudaMalloc(&dF, no) != cudaSuccess ||
       cudaMalloc(&dD, no) != cudaSuccess || cudaMalloc(&dS, ns) != cudaSuccess ||
-      cudaMalloc(&dt, sizeof tab) != cudaSuccess || cudaMalloc(&dtf, sizeof fine) != cudaSuccess) {
+      cudaMalloc(&dt, sizeof tab) != cudaSuccess || cudaMalloc(&dtf, sizeof(FineTable)) != cudaSuccess) {
     release();
     cudaGetLastError();
     return fail(nullptr, MLBM_ERR_ALLOC, "testing buffers");
@@ -960,7 +999,7 @@ extern "C" int mlbm_testing_entropy(int lattice, const float* f, const double* f
   if (e == cudaSuccess) e = cudaMemcpy(dn, fneq, nn, cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemcpy(dx, x, nxb, cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemcpy(dt, tab, sizeof tab, cudaMemcpyHostToDevice);
-  if (e == cudaSuccess) e = cudaMemcpy(dtf, fine, sizeof fine, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(dtf, fine.get(), sizeof(FineTable), cudaMemcpyHostToDevice);
   if (e == cudaSuccess)
     e = entropy_test(lattice, (const float*)df, (const double*)dn, nodes, (const double*)dx, nx,
                      mode, dt, dtf, (double*)dF, (double*)dD, (int*)dS, 0);

@@ -73,7 +73,7 @@ struct StepParams {
   unsigned* err_word;
   const void* mlp;           // device MlpDev* (learned guess)
   const void* log_table;     // device LogEntry[LOG_TABLE] (fastlog.cuh)
-  const void* log_table_fine;  // device LogEntryFine[LOG_TABLE_FINE] (fastlog.cuh)
+  const void* log_table_fine;  // device LogEntryFine[LOG_TABLE_FINE] + double[LNW_CONSTS] (fastlog.cuh)
   // entropic FP32/FP16 step: worklist of the nodes left to the second pass
   unsigned* defer_list;      // [V] node indices
   unsigned* defer_count;     // [2] list lengths, used by alternating steps

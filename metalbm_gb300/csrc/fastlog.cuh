@@ -153,8 +153,25 @@ __device__ __forceinline__ double fast_log_fine(double x, const LogEntryFine* ta
   return fma(exponent_as_double(e), kLn2, t.hi) + (r + widen_exact(tail));
 }
 
-__device__ __forceinline__ void stage_log_table_fine(LogEntryFine* sh, const LogEntryFine* __restrict__ g) {
+// The fine table is followed in device memory by the lattice's constants
+// C_q(d) = d ln 2 - ln(m_q), d = -1, 0, 1, at [3 q + d + 1], where w_q = m_q 2^e_q
+// with m_q in [1, 2): ln(f_q / w_q) = C_q(d) + ln(mantissa of f_q) for
+// d = exponent(f_q) - e_q.
+constexpr int LNW_CONSTS = 81;
+
+__device__ __forceinline__ void stage_log_table_fine(LogEntryFine* sh, double* sh_lnw,
+                                                     const LogEntryFine* __restrict__ g) {
   for (int i = threadIdx.x; i < LOG_TABLE_FINE; i += blockDim.x) sh[i] = g[i];
+  const double* c = reinterpret_cast<const double*>(g + LOG_TABLE_FINE);
+  for (int i = threadIdx.x; i < LNW_CONSTS; i += blockDim.x) sh_lnw[i] = c[i];
+}
+
+// Binary exponent e of a positive constant w = m 2^e, m in [1, 2).
+__host__ __device__ constexpr int exponent_of(double w) {
+  int e = 0;
+  while (w >= 2.0) { w *= 0.5; ++e; }
+  while (w < 1.0) { w *= 2.0; --e; }
+  return e;
 }
 
 // Block-cooperative staging of the table into shared memory.

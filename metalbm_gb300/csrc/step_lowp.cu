@@ -442,10 +442,28 @@ struct HLowp {
   }
 };
 
-// Series tiers: above kSeriesM4Rmax the fourth moment is an FP64 sum (its
-// term x^4 M4/12 <= 3.3 rho r^4 would lose up to 1.6e-6 of itself in FP32),
-// below it every moment from M4 on is an FP32 sum (< 1.5e-15 absolute).
-constexpr float kSeriesM4Rmax = 0.004f;
+// Moment tiers of the series form (max_q |r_q| = rmax <= kSeriesRmax):
+//   A, rmax <= kSeriesTierA: M2 in FP64, M3..M8 as FP32 sums;
+//   B, above:                M2..M4 in FP64, M5..M8 as FP32 sums.
+// M2 = sum f_neq^2 / f is formed as sum f_neq^2 y0 (1 + e) with y0 the FP32
+// reciprocal of the stored f and e = 1 - f y0 (exact in FP32 for F32
+// storage): the FP64 part sum f_neq^2 y0 plus an FP32 correction.
+// The evaluation error of F is bounded per node (F's error sources):
+//   FP32 M3 (tier A):   (2.5^3/6) 2.1e-6 rho rmax^3 (9 roundings a term,
+//                       26 in the sum) = 5.5e-6 rho rmax^3, M4.. smaller;
+//   FP32 M5 (tier B):   (2.5^5/20) 2.3e-6 rho rmax^5;
+//   B1 (fast_log_fine and the FP32 tail sum): 2.5 x 2.4e-13 rho rmax;
+//   FP64 rounding and the k > 8 truncation: < 1e-15.
+// The solve accepts alpha when |F| <= tol - bound, so the residual of the
+// exact function stays within tol.
+constexpr float kSeriesTierA = 0.0025f;
+
+template <int LAT, int ST>
+__device__ __forceinline__ double series_error_bound(float rabs, double rho) {
+  const float r = rabs, rf = narrow_rn(rho);
+  const float m = r <= kSeriesTierA ? 5.6e-6f * r * r * r : 1.2e-5f * (r * r) * (r * r) * r;
+  return widen_exact(fmaf(rf, fmaf(6.0e-13f, r, m), 1.0e-15f));
+}
 
 // B1 and the moments (series form), or r_q in place of f_neq_q in n[]
 // (direct form).
@@ -453,37 +471,62 @@ template <int LAT, int ST, bool SERIES>
 __device__ __forceinline__ HLowp<LAT, ST, SERIES> make_entropy_eval(const Pulled<LAT, ST>& P,
                                                                     double n[], float rabs,
                                                                     const LogEntry* tab,
-                                                                    const LogEntryFine* fine) {
+                                                                    const LogEntryFine* fine,
+                                                                    const double* lnw) {
   using L = Lattice<LAT>;
   HLowp<LAT, ST, SERIES> ev;
   double B1 = 0.0;
   if constexpr (SERIES) {
-#pragma unroll
-    for (int q = 0; q < L::Q; ++q) B1 = fma(n[q], fast_log_fine(P.f64(q) * (1.0 / L::w(q)), fine), B1);
+    const bool tierB = rabs > kSeriesTierA;
     double M2 = 0.0, M3 = 0.0, M4 = 0.0;
-    float M4f = 0.0f, M5 = 0.0f, M6 = 0.0f, M7 = 0.0f, M8 = 0.0f;
-    const bool m4_f64 = rabs > kSeriesM4Rmax;
+    float B1t = 0.0f, M2c = 0.0f, M3f = 0.0f, M4f = 0.0f, M5 = 0.0f, M6 = 0.0f, M7 = 0.0f,
+          M8 = 0.0f;
 #pragma unroll
     for (int q = 0; q < L::Q; ++q) {
-      const float rcp = __frcp_rn(P.f32(q));
       const double f = P.f64(q);
-      const double y0 = widen_exact(rcp);
-      const double g = n[q] * fma(y0, fma(-f, y0, 1.0), y0);  // r_q
-      const double p2 = g * n[q];                             // f r^2
-      M2 += p2;
-      M3 = fma(p2, g, M3);
-      if (m4_f64) M4 = fma(p2 * g, g, M4);
       const float nf = narrow_rn(n[q]);
-      const float rf = nf * rcp;
-      const float r3 = rf * rf * rf;
-      float t = nf * r3;  // f r^4
-      M4f += t;
-      t *= rf; M5 += t;
+      // B1 += f_neq ln(f/w): ln(f/w) = C_q(d) + T_j + log1p(r'), r' = m inv_j - 1
+      {
+        const int64_t bits = __double_as_longlong(f);
+        const int d = (int)((bits >> 52) & 0x7ff) - (1023 + exponent_of(L::w(q)));
+        const LogEntryFine t = fine[(bits >> 42) & (LOG_TABLE_FINE - 1)];
+        const double m = __longlong_as_double((bits & 0x000fffffffffffffLL) | 0x3ff0000000000000LL);
+        const double rp = fma(m, t.inv, -1.0);
+        double C;
+        if (d >= -1 && d <= 1) C = lnw[3 * q + d + 1];
+        else C = fma(exponent_as_double(d), kLn2, lnw[3 * q + 1]);
+        B1 = fma(n[q], (C + t.hi) + rp, B1);
+        const float rpf = narrow_rn(rp);
+        B1t = fmaf(nf, (rpf * rpf) * fmaf(rpf, 1.0f / 3.0f, -0.5f), B1t);
+      }
+      // moments
+      const float y0f = __frcp_rn(P.f32(q));
+      const double y0 = widen_exact(y0f);
+      float e;
+      if constexpr (ST == ST_F32) e = fmaf(-P.v[q], y0f, 1.0f);
+      else e = narrow_rn(fma(-f, y0, 1.0));
+      const double n2 = n[q] * n[q];
+      M2 = fma(n2, y0, M2);
+      const float rf = nf * y0f;
+      M2c = fmaf(nf * rf, e, M2c);
+      float t = nf * (rf * rf);  // f r^3
+      if (tierB) {
+        const double g = n[q] * fma(y0, widen_exact(e), y0);  // r_q
+        const double p2 = g * n[q];
+        M3 = fma(p2, g, M3);
+        M4 = fma(p2 * g, g, M4);
+      } else {
+        M3f += t;
+        M4f = fmaf(t, rf, M4f);
+      }
+      t *= rf * rf; M5 += t;  // f r^5
       t *= rf; M6 += t;
       t *= rf; M7 += t;
       t *= rf; M8 += t;
     }
-    if (!m4_f64) M4 = widen_exact(M4f);
+    B1 += widen_exact(B1t);
+    M2 += widen_exact(M2c);
+    if (!tierB) { M3 = widen_exact(M3f); M4 = widen_exact(M4f); }
     ev.S = HSeries{B1, M2 * 0.5, M3 * (1.0 / 6.0), M4 * (1.0 / 12.0), M2, M3 * 0.5,
                    M4 * (1.0 / 3.0), M5 * (1.0f / 20.0f), M6 * (1.0f / 30.0f),
                    M7 * (1.0f / 42.0f), M8 * (1.0f / 56.0f), M5 * 0.25f, M6 * 0.2f,
@@ -605,7 +648,8 @@ __device__ __forceinline__ void elbm_node(const typename Storage<ST>::T* __restr
                                           typename Storage<ST>::T* __restrict__ next,
                                           const StepParams& p, bool active, long long idx,
                                           const LogEntry* s_log, const LogEntryFine* s_fine,
-                                          unsigned cnt[], bool& defer, double& mass,
+                                          const double* s_lnw, unsigned cnt[], bool& defer,
+                                          double& mass,
                                           double& energy, double& mach, double& amin,
                                           double& amax) {
   using L = Lattice<LAT>;
@@ -675,13 +719,14 @@ __device__ __forceinline__ void elbm_node(const typename Storage<ST>::T* __restr
       const double plain = p.guess_mode == GUESS_TWO ? 2.0 : prevA;
       const double guess = LEARNED ? 2.0 + widen_exact(learned) : plain;
       if constexpr (MODE == ELBM_MAIN) {
-        const auto ev = make_entropy_eval<LAT, ST, true>(P, n, rabs, s_log, s_fine);
-        alpha = residual_alpha_solve<decltype(ev), true>(ev, guess, plain, alphaMax, p.newton_tol,
+        const auto ev = make_entropy_eval<LAT, ST, true>(P, n, rabs, s_log, s_fine, s_lnw);
+        const double tol = p.newton_tol - series_error_bound<LAT, ST>(rabs, rho);
+        alpha = residual_alpha_solve<decltype(ev), true>(ev, guess, plain, alphaMax, tol,
                                                          p.newton_maxit, cnt);
       } else {
-        const auto ev = make_entropy_eval<LAT, ST, false>(P, n, rabs, s_log, s_fine);
-        alpha = residual_alpha_solve<decltype(ev), true>(ev, guess, plain, alphaMax, p.newton_tol,
-                                                         p.newton_maxit, cnt);
+        const auto ev = make_entropy_eval<LAT, ST, false>(P, n, rabs, s_log, s_fine, s_lnw);
+        alpha = residual_alpha_solve<decltype(ev), true>(ev, guess, plain, alphaMax,
+                                                         p.newton_tol - 4e-15, p.newton_maxit, cnt);
       }
     }
   }
@@ -775,7 +820,8 @@ __global__ void __launch_bounds__(128, MLBM_ELBM_MIN_BLOCKS) elbm_lowp_kernel(co
                                                         typename Storage<ST>::T* __restrict__ next,
                                                         StepParams p) {
   __shared__ LogEntryFine s_fine[LOG_TABLE_FINE];
-  stage_log_table_fine(s_fine, reinterpret_cast<const LogEntryFine*>(p.log_table_fine));
+  __shared__ double s_lnw[LNW_CONSTS];
+  stage_log_table_fine(s_fine, s_lnw, reinterpret_cast<const LogEntryFine*>(p.log_table_fine));
   // the worklist counter of the next step (its last reader was the previous
   // step's second pass, which has completed)
   if (blockIdx.x == 0 && threadIdx.x == 0) p.defer_count[p.parity ^ 1] = 0u;
@@ -785,8 +831,8 @@ __global__ void __launch_bounds__(128, MLBM_ELBM_MIN_BLOCKS) elbm_lowp_kernel(co
   double mass = 0.0, energy = 0.0, mach = 0.0, amin = 1e300, amax = -1e300;
   unsigned cnt[CNT_COUNT] = {0, 0, 0, 0, 0, 0, 0, 0};
   bool defer = false;
-  elbm_node<LAT, FS, ST, LEARNED, ELBM_MAIN>(prev, next, p, active, idx, nullptr, s_fine, cnt,
-                                             defer, mass, energy, mach, amin, amax);
+  elbm_node<LAT, FS, ST, LEARNED, ELBM_MAIN>(prev, next, p, active, idx, nullptr, s_fine, s_lnw,
+                                             cnt, defer, mass, energy, mach, amin, amax);
   // warp-aggregated append to the worklist
   const unsigned m = __ballot_sync(0xffffffffu, defer);
   if (m) {
@@ -817,8 +863,9 @@ __global__ void __launch_bounds__(128) elbm_lowp_deferred_kernel(const typename 
     const bool active = i < count;
     const long long idx = active ? (long long)p.defer_list[i] : 0;
     bool defer = false;
-    elbm_node<LAT, FS, ST, LEARNED, ELBM_DEFERRED>(prev, next, p, active, idx, s_log, nullptr, cnt,
-                                                   defer, mass, energy, mach, amin, amax);
+    elbm_node<LAT, FS, ST, LEARNED, ELBM_DEFERRED>(prev, next, p, active, idx, s_log, nullptr,
+                                                   nullptr, cnt, defer, mass, energy, mach, amin,
+                                                   amax);
   }
   add_counters(p.counters, cnt);
   if (p.diag)
@@ -840,8 +887,9 @@ __global__ void entropy_test_kernel(const float* __restrict__ f, const double* _
   using L = Lattice<LAT>;
   __shared__ LogEntry s_log[LOG_TABLE];
   __shared__ LogEntryFine s_fine[LOG_TABLE_FINE];
+  __shared__ double s_lnw[LNW_CONSTS];
   stage_log_table(s_log, table);
-  stage_log_table_fine(s_fine, table_fine);
+  stage_log_table_fine(s_fine, s_lnw, table_fine);
   __syncthreads();
   const long long s = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= nodes) return;
@@ -856,10 +904,10 @@ __global__ void entropy_test_kernel(const float* __restrict__ f, const double* _
   }
   const bool series = mode == 2 || (mode == 0 && rabs <= kSeriesRmax);
   if (series) {
-    const auto ev = make_entropy_eval<LAT, ST_F32, true>(P, n, rabs, s_log, s_fine);
+    const auto ev = make_entropy_eval<LAT, ST_F32, true>(P, n, rabs, s_log, s_fine, s_lnw);
     for (int i = 0; i < nx; ++i) ev(xs[i], Fo[s * nx + i], Do[s * nx + i]);
   } else {
-    const auto ev = make_entropy_eval<LAT, ST_F32, false>(P, n, rabs, s_log, s_fine);
+    const auto ev = make_entropy_eval<LAT, ST_F32, false>(P, n, rabs, s_log, s_fine, s_lnw);
     for (int i = 0; i < nx; ++i) ev(xs[i], Fo[s * nx + i], Do[s * nx + i]);
   }
   series_out[s] = series ? 1 : 0;
