@@ -10,7 +10,7 @@ alpha guess (the committed MLP) and plain Newton from the previous alpha.
 `value` is the learned arm's MLUPS; the Newton arm is reported beside it.
 
 Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-       [--workload entropic_learned_512|bgk_d3q19_f64_256|bgk_d3q19_f32_256]
+       [--workload entropic_learned_512|bgk_d3q19_f64_256|bgk_d3q19_f32_256|bgk_d3q19_f16_256]
 Under torchrun (N > 1) every rank runs an independent replica of the workload
 on its own GPU (the path has no data exchange on one lattice per GPU); the
 timed region is bracketed by barriers and the max over ranks is used.
@@ -60,6 +60,11 @@ WORKLOADS = {
                               forceAmplitude=(1e-6, 0.0, 0.0), forceWaveLength=(128.0, 1.0, 1.0),
                               kolmogorovAxis=2, globalLength=(256, 256, 256), storage="f32",
                               bytes_per_node=2 * 19 * 4),
+    "bgk_d3q19_f16_256": dict(latticeT="D3Q19", collisionT="BGK", relaxationTime=0.55,
+                              forcingSchemeT="Guo", forceT="Kolmogorov",
+                              forceAmplitude=(1e-6, 0.0, 0.0), forceWaveLength=(128.0, 1.0, 1.0),
+                              kolmogorovAxis=2, globalLength=(256, 256, 256),
+                              storage="f16_shifted", bytes_per_node=2 * 19 * 2),
 }
 
 
@@ -317,18 +322,30 @@ def run_ours(args):
     bpn = w["bytes_per_node"]
     avg_launch_ms = total_ms / args.steps
     achieved = bpn * V / (avg_launch_ms * 1e-3) / 1e9
-    traffic = None
-    tfile = ROOT / "profiles" / "traffic.json"
-    if tfile.exists():
-        tr = json.loads(tfile.read_text()).get(name)
-        if tr:
-            traffic = tr.get("dram_bytes_per_launch")
+    # ncu figures of the dominant kernel (profiles/roofline_inputs.json, each
+    # entry naming the profile summary it comes from): DRAM bytes per node of
+    # one launch and, for the FP64-bound kernels, FP64 instructions per node
+    prof = {}
+    pfile = ROOT / "profiles" / "roofline_inputs.json"
+    if pfile.exists():
+        prof = json.loads(pfile.read_text()).get(name, {})
+    traffic = prof["dram_bytes_per_node"] * V if "dram_bytes_per_node" in prof else None
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
                 "frac": achieved / peaks["hbm_gbs"], "traffic": traffic,
                 "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs, burst copy)"
                 if peak_src == "measured" else "fallback 6.8 TB/s",
                 "bytes_per_node": bpn, "kernel": "elbm_lowp_kernel" if entropic else
-                ("bgk_f64_kernel" if w["storage"] == "f64" else "bgk_lowp_kernel")}
+                ("bgk_f64_kernel" if w["storage"] == "f64" else "bgk_lowp_kernel"),
+                "traffic_source": prof.get("source")}
+    if "fp64_inst_per_node" in prof:
+        # the kernel's binding roof: GB300's FP64 pipe (no FP64 figure in
+        # MEASURED_PEAKS.json; the peak is the DFMA rate measured by
+        # metalbm_gb300/cpp/fp64_throughput.cu on this pool)
+        gops = prof["fp64_inst_per_node"] * V / (avg_launch_ms * 1e-3) / 1e9
+        roofline["fp64_pipe"] = {"achieved": gops, "peak": prof["fp64_peak_gops"],
+                                 "unit": "G FP64 instr/s", "frac": gops / prof["fp64_peak_gops"],
+                                 "instructions_per_node": prof["fp64_inst_per_node"],
+                                 "peak_source": "measured DFMA throughput (profiles/fp64_throughput_gb300.md)"}
 
     # --- end to end through the C ABI with host buffers (rank 0 reports)
     e2e = run_e2e(name, deck_l, rho, u, model if entropic else None, args.steps, torch, dist, world)

@@ -91,13 +91,23 @@ constexpr int DIAG_FIELDS = 5;
 // Source node of the pulled population with velocity (cx, cy, cz): periodic
 // neighbour offsets along each axis, formed once per node.
 struct PullOffsets {
-  long long ox[3];  // index 0: c = -1 (reads x+1), 1: c = 0, 2: c = +1 (reads x-1)
-  long long oy[3];
-  long long oz[3];
-  __device__ __forceinline__ long long at(int cx, int cy, int cz) const {
+  // node-index offsets within one population array (V < 2^31): 32-bit, so a
+  // source address is one 32-bit three-input add and one wide multiply-add
+  // onto the population's base pointer
+  uint32_t ox[3];  // index 0: c = -1 (reads x+1), 1: c = 0, 2: c = +1 (reads x-1)
+  uint32_t oy[3];
+  uint32_t oz[3];
+  __device__ __forceinline__ uint32_t at(int cx, int cy, int cz) const {
     return ox[cx + 1] + oy[cy + 1] + oz[cz + 1];
   }
 };
+
+// Base of population q's array (uniform across the grid) indexed with a
+// 32-bit node index.
+template <class T>
+__device__ __forceinline__ T* pop(T* base, long long V, int q) {
+  return base + (long long)q * V;
+}
 
 __device__ __forceinline__ void node_coords(const StepParams& p, long long idx, uint32_t& x,
                                             uint32_t& y, uint32_t& z) {
@@ -111,12 +121,12 @@ __device__ __forceinline__ void node_coords(const StepParams& p, long long idx, 
 __device__ __forceinline__ PullOffsets pull_offsets(const StepParams& p, uint32_t x, uint32_t y,
                                                     uint32_t z) {
   PullOffsets o;
-  const long long sx = (long long)p.ly * p.lz;
+  const uint32_t sx = p.ly * p.lz;
   const uint32_t xp = (x + 1 == p.lx) ? 0 : x + 1, xm = (x == 0) ? p.lx - 1 : x - 1;
   const uint32_t yp = (y + 1 == p.ly) ? 0 : y + 1, ym = (y == 0) ? p.ly - 1 : y - 1;
   const uint32_t zp = (z + 1 == p.lz) ? 0 : z + 1, zm = (z == 0) ? p.lz - 1 : z - 1;
   o.ox[0] = xp * sx; o.ox[1] = x * sx; o.ox[2] = xm * sx;
-  o.oy[0] = (long long)yp * p.lz; o.oy[1] = (long long)y * p.lz; o.oy[2] = (long long)ym * p.lz;
+  o.oy[0] = yp * p.lz; o.oy[1] = y * p.lz; o.oy[2] = ym * p.lz;
   o.oz[0] = zp; o.oz[1] = z; o.oz[2] = zm;
   return o;
 }

@@ -122,7 +122,7 @@ __device__ __forceinline__ void pull(const double* __restrict__ prev, long long 
   using L = Lattice<LAT>;
 #pragma unroll
   for (int q = 0; q < L::Q; ++q)
-    f[q] = __ldg(prev + (long long)q * V + o.at(L::c(q, 0), L::c(q, 1), L::c(q, 2)));
+    f[q] = __ldg(pop(prev, V, q) + o.at(L::c(q, 0), L::c(q, 1), L::c(q, 2)));
 }
 
 // rho = f0 + f1 + ... ; u_d = sum_q c_qd f_q ; u /= rho (Moment.h:13-47)
@@ -227,7 +227,7 @@ __global__ void __launch_bounds__(256) bgk_f64_kernel(const double* __restrict__
       const double cu3 = cdot<LAT>(q, u) * 3.0;
       double r = p.bgk_a * f[q] + p.bgk_b * feq[q];
       if (FS == FS_GUO || FS == FS_EDM) r = r + source<LAT, FS>(p, q, rho, u, F, cu3, feq[q], fsh);
-      next[(long long)q * p.V + idx] = r;
+      pop(next, p.V, q)[(uint32_t)idx] = r;
     }
     if (!(rho > 0.0) || !isfinite(rho)) atomicOr(p.err_word, ERR_NONFINITE);
     mass = rho;
@@ -343,7 +343,7 @@ __global__ void __launch_bounds__(128) elbm_f64_kernel(const double* __restrict_
       double r = f[q] - inv * fneq[q];
       if (FS == FS_GUO || FS == FS_EDM)
         r = r + source<LAT, FS>(p, q, rho, u, F, cdot<LAT>(q, u) * 3.0, eqq, fsh);
-      next[(long long)q * p.V + idx] = r;
+      pop(next, p.V, q)[(uint32_t)idx] = r;
     }
     p.alpha_field[idx] = alpha;
     if (!(rho > 0.0) || !isfinite(rho)) atomicOr(p.err_word, ERR_NONFINITE);

@@ -43,9 +43,23 @@ __host__ __device__ constexpr int shift_exponent(int q) {
 template <int ST>
 struct Storage;
 
+// Scaled deviations d'_q = S_q (f_q - w_q), S_q = 1 (F32) or 2^k_q (F16):
+// the value a population is stored as, before its rounding to the storage
+// type. The BGK kernel works on d' with the scale folded into its
+// constants, so the FP16 path spends no multiply on either side of memory.
 template <>
 struct Storage<ST_F32> {
   using T = float;
+  template <int LAT>
+  __host__ __device__ static constexpr float scale(int) { return 1.0f; }
+  template <int LAT>
+  __device__ __forceinline__ static float load_scaled(const float* p, int q) {
+    return __ldg(p) - (float)Lattice<LAT>::w(q);
+  }
+  template <int LAT>
+  __device__ __forceinline__ static void store_scaled(float* p, int q, float d) {
+    *p = (float)Lattice<LAT>::w(q) + d;
+  }
   template <int LAT>
   __device__ __forceinline__ static float load(const float* p, int q) {
     return __ldg(p) - (float)Lattice<LAT>::w(q);
@@ -63,6 +77,18 @@ struct Storage<ST_F32> {
 template <>
 struct Storage<ST_F16> {
   using T = __half;
+  template <int LAT>
+  __host__ __device__ static constexpr float scale(int q) {
+    return (float)(1 << shift_exponent<LAT>(q));
+  }
+  template <int LAT>
+  __device__ __forceinline__ static float load_scaled(const __half* p, int) {
+    return __half2float(__ldg(p));
+  }
+  template <int LAT>
+  __device__ __forceinline__ static void store_scaled(__half* p, int, float d) {
+    *p = __float2half_rn(d);
+  }
   template <int LAT>
   __device__ __forceinline__ static float load(const __half* p, int q) {
     return __half2float(__ldg(p)) * (1.0f / (float)(1 << shift_exponent<LAT>(q)));
@@ -185,7 +211,7 @@ __device__ __forceinline__ void pull_dev(const typename Storage<ST>::T* __restri
 #pragma unroll
   for (int q = 0; q < L::Q; ++q)
     d[q] = Storage<ST>::template load<LAT>(
-        prev + (long long)q * V + o.at(L::c(q, 0), L::c(q, 1), L::c(q, 2)), q);
+        pop(prev, V, q) + o.at(L::c(q, 0), L::c(q, 1), L::c(q, 2)), q);
 }
 
 template <int LAT>
@@ -281,13 +307,15 @@ __device__ __forceinline__ void node_force_float(const StepParams& p, uint32_t x
 // with the pair algebra P(+-cu) = E +- O of the TruncationMa3 polynomial and,
 // for Guo (ForcingScheme.h:100-117), S_q = kt w_q [(c_q - u).F + 3 (c_q.u)(c_q.F)]
 // = kt w_q (3 cu cF - u.F +- cF) for the pair; EDM: S_q = w_q rho (P_q(v) - P_q(u)),
-// v = u + F/rho (ForcingScheme.h:183-197).
+// v = u + F/rho (ForcingScheme.h:183-197). Every population is carried in its
+// storage scale (d'_q = S_q d_q, Storage::scale), the factors S_q and 1/S_q
+// folded into the per-population constants.
 template <int LAT, int FS, int ST>
 __global__ void __launch_bounds__(256) bgk_lowp_kernel(const typename Storage<ST>::T* __restrict__ prev,
                                                        typename Storage<ST>::T* __restrict__ next,
                                                        StepParams p) {
   using L = Lattice<LAT>;
-  using T = typename Storage<ST>::T;
+  using S = Storage<ST>;
   const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const bool active = idx < p.V;
   double mass = 0.0, energy = 0.0, mach = 0.0;
@@ -295,10 +323,26 @@ __global__ void __launch_bounds__(256) bgk_lowp_kernel(const typename Storage<ST
     uint32_t x, y, z;
     node_coords(p, idx, x, y, z);
     const PullOffsets o = pull_offsets(p, x, y, z);
-    float d[L::Q];
-    pull_dev<LAT, ST>(prev, p.V, o, d);
-    float rhop, rho, u[3];
-    moments_dev<LAT>(d, rhop, rho, u);
+    float d[L::Q];  // scaled deviations
+#pragma unroll
+    for (int q = 0; q < L::Q; ++q)
+      d[q] = S::template load_scaled<LAT>(pop(prev, p.V, q) + o.at(L::c(q, 0), L::c(q, 1), L::c(q, 2)), q);
+    float rhop = 0.0f, j[3] = {0.0f, 0.0f, 0.0f};
+#pragma unroll
+    for (int q = 0; q < L::Q; ++q) {
+      const float is = 1.0f / S::template scale<LAT>(q);
+      rhop = fmaf(d[q], is, rhop);
+#pragma unroll
+      for (int k = 0; k < L::D; ++k) {
+        if (L::c(q, k) > 0) j[k] = fmaf(d[q], is, j[k]);
+        if (L::c(q, k) < 0) j[k] = fmaf(d[q], -is, j[k]);
+      }
+    }
+    const float rho = 1.0f + rhop;
+    const float irho = 1.0f / rho;
+    float u[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) u[k] = j[k] * irho;
     float F[3] = {0.0f, 0.0f, 0.0f};
     if (FS != FS_NONE) node_force_float<L::D>(p, x, y, z, F);
     const float u2 = u[0] * u[0] + u[1] * u[1] + u[2] * u[2];
@@ -308,47 +352,46 @@ __global__ void __launch_bounds__(256) bgk_lowp_kernel(const typename Storage<ST
     PolyNode nv = n;
     if (FS == FS_GUO) uF = u[0] * F[0] + u[1] * F[1] + u[2] * F[2];
     if (FS == FS_EDM) {
-      const float ir = 1.0f / rho;
 #pragma unroll
-      for (int k = 0; k < 3; ++k) v[k] = fmaf(F[k], ir, u[k]);
+      for (int k = 0; k < 3; ++k) v[k] = fmaf(F[k], irho, u[k]);
       nv = poly_node(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
     }
-    T* out = next + idx;
     {  // rest population
-      const float w = (float)L::w(0);
-      const float deq = w * fmaf(rho, n.common, rhop);
+      const float ws = (float)L::w(0) * S::template scale<LAT>(0);
+      const float deq = ws * fmaf(rho, n.common, rhop);
       float r = fmaf(b, deq - d[0], d[0]);
-      if (FS == FS_GUO) r = fmaf(p.guo_kt_f * w, -uF, r);
-      if (FS == FS_EDM) r = fmaf(w * rho, nv.common - n.common, r);
-      Storage<ST>::template store<LAT>(out, 0, r);
+      if (FS == FS_GUO) r = fmaf(p.guo_kt_f * ws, -uF, r);
+      if (FS == FS_EDM) r = fmaf(ws * rho, nv.common - n.common, r);
+      S::template store_scaled<LAT>(next + (uint32_t)idx, 0, r);
     }
 #pragma unroll
     for (int q = 1; q < L::Q; ++q) {
       if (is_pair_leader<LAT>(q)) {
         const int qb = opposite<LAT>(q);
-        const float w = (float)L::w(q);
+        // opposite populations share w_q and therefore S_q
+        const float ws = (float)L::w(q) * S::template scale<LAT>(q);
         const float cu = cdotf<LAT>(q, u);
         float E, O;
         poly_pair(n, cu, E, O);
-        const float dq = w * fmaf(rho, E + O, rhop), dqb = w * fmaf(rho, E - O, rhop);
+        const float dq = ws * fmaf(rho, E + O, rhop), dqb = ws * fmaf(rho, E - O, rhop);
         float rq = fmaf(b, dq - d[q], d[q]);
         float rqb = fmaf(b, dqb - d[qb], d[qb]);
         if (FS == FS_GUO) {
           const float cF = cdotf<LAT>(q, F);
           const float Es = fmaf(3.0f * cu, cF, -uF);
-          const float kw = p.guo_kt_f * w;
+          const float kw = p.guo_kt_f * ws;
           rq = fmaf(kw, Es + cF, rq);
           rqb = fmaf(kw, Es - cF, rqb);
         }
         if (FS == FS_EDM) {
           float Ev, Ov;
           poly_pair(nv, cdotf<LAT>(q, v), Ev, Ov);
-          const float wr = w * rho;
+          const float wr = ws * rho;
           rq = fmaf(wr, (Ev + Ov) - (E + O), rq);
           rqb = fmaf(wr, (Ev - Ov) - (E - O), rqb);
         }
-        Storage<ST>::template store<LAT>(out + (long long)q * p.V, q, rq);
-        Storage<ST>::template store<LAT>(out + (long long)qb * p.V, qb, rqb);
+        S::template store_scaled<LAT>(pop(next, p.V, q) + (uint32_t)idx, q, rq);
+        S::template store_scaled<LAT>(pop(next, p.V, qb) + (uint32_t)idx, qb, rqb);
       }
     }
     if (!(rho > 0.0f) || !isfinite(rho)) atomicOr(p.err_word, ERR_NONFINITE);
@@ -660,7 +703,7 @@ __device__ __forceinline__ void elbm_node(const typename Storage<ST>::T* __restr
     const PullOffsets o = pull_offsets(p, x, y, z);
 #pragma unroll
     for (int q = 0; q < L::Q; ++q) {
-      const auto* src = prev + (long long)q * p.V + o.at(L::c(q, 0), L::c(q, 1), L::c(q, 2));
+      const auto* src = pop(prev, p.V, q) + o.at(L::c(q, 0), L::c(q, 1), L::c(q, 2));
       if constexpr (ST == ST_F32) P.v[q] = __ldg(src);
       else P.v[q] = __half2float(__ldg(src)) * (1.0f / (float)(1 << shift_exponent<LAT>(q)));
     }
@@ -785,7 +828,7 @@ __device__ __forceinline__ void elbm_node(const typename Storage<ST>::T* __restr
       const float nf = direct ? narrow_rn(n[q] * P.f64(q)) : narrow_rn(n[q]);
       float rr = fmaf(-ab, nf, P.v[q]);  // f (F32) or f - w (F16)
       if (FS == FS_GUO || FS == FS_EDM) rr += src[q];
-      auto* dst = next + (long long)q * p.V + idx;
+      auto* dst = pop(next, p.V, q) + (uint32_t)idx;
       if constexpr (ST == ST_F32) *dst = rr;
       else *dst = __float2half_rn(rr * (float)(1 << shift_exponent<LAT>(q)));
     }
@@ -980,7 +1023,7 @@ __global__ void samples_lowp_kernel(const typename Storage<ST>::T* __restrict__ 
   double f[L::Q], fn[L::Q], rho = 0.0, j[3] = {0.0, 0.0, 0.0}, u[3];
 #pragma unroll
   for (int q = 0; q < L::Q; ++q) {
-    f[q] = load_f64<LAT, ST>(prev + (long long)q * p.V + o.at(L::c(q, 0), L::c(q, 1), L::c(q, 2)), q);
+    f[q] = load_f64<LAT, ST>(pop(prev, p.V, q) + o.at(L::c(q, 0), L::c(q, 1), L::c(q, 2)), q);
     rho += f[q];
 #pragma unroll
     for (int k = 0; k < L::D; ++k) {
