@@ -712,14 +712,15 @@ __device__ __forceinline__ void elbm_node(const typename Storage<ST>::T* __restr
     for (int q = 0; q < L::Q; ++q) P.v[q] = ST == ST_F32 ? (float)L::w(q) : 0.0f;
   }
   // Learned guess: every thread of the block takes part (tile inference), on
-  // features f_neq / rho from the FP32 deviations.
+  // features f_neq / rho from the FP32 deviations (computed before the FP64
+  // part, so that the inference and the FP64 f_neq are not live together)
   float learned = 0.0f;
   if (LEARNED) {
-    float dv[L::Q], rhop, rf, uf[3], deq[L::Q];
+    float dv[L::Q], rhopf, rf, uf[3], deq[L::Q];
 #pragma unroll
     for (int q = 0; q < L::Q; ++q) dv[q] = P.dev(q);
-    moments_dev<LAT>(dv, rhop, rf, uf);
-    eq_dev<LAT>(rhop, rf, uf, uf[0] * uf[0] + uf[1] * uf[1] + uf[2] * uf[2], deq);
+    moments_dev<LAT>(dv, rhopf, rf, uf);
+    eq_dev<LAT>(rhopf, rf, uf, uf[0] * uf[0] + uf[1] * uf[1] + uf[2] * uf[2], deq);
     const float irf = 1.0f / rf;
     float xin[L::Q];
 #pragma unroll
@@ -727,14 +728,15 @@ __device__ __forceinline__ void elbm_node(const typename Storage<ST>::T* __restr
     learned = mlp_guess_block<L::Q>(reinterpret_cast<const MlpDev*>(p.mlp), xin);
   }
   if (!active) return;
+  // rho, u and f_neq in FP64 from the exact stored values
   double rho, rhop, j[3], u[3];
   moments_exact<LAT, ST>(P, rho, rhop, j);
   const double ir = recip_refined(rho, narrow_rn(rho));
 #pragma unroll
   for (int k = 0; k < 3; ++k) u[k] = j[k] * ir;
-  // n_q = f_neq_q; r_q = n_q / f_q in FP32 for the bracket and the tests
   double n[L::Q];
   neq_pairs<LAT, ST>(P, rho, rhop, u, n);
+  // r_q = n_q / f_q in FP32 for the bracket and the tests
   float rpos = 0.0f, rabs = 0.0f;
 #pragma unroll
   for (int q = 0; q < L::Q; ++q) {
