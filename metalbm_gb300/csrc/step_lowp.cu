@@ -512,7 +512,8 @@ __device__ __forceinline__ double series_error_bound(float rabs, double rho) {
 // (direct form).
 template <int LAT, int ST, bool SERIES>
 __device__ __forceinline__ HLowp<LAT, ST, SERIES> make_entropy_eval(const Pulled<LAT, ST>& P,
-                                                                    double n[], float rabs,
+                                                                    double n[], float nfr[],
+                                                                    float rabs,
                                                                     const LogEntry* tab,
                                                                     const LogEntryFine* fine,
                                                                     const double* lnw) {
@@ -528,6 +529,7 @@ __device__ __forceinline__ HLowp<LAT, ST, SERIES> make_entropy_eval(const Pulled
     for (int q = 0; q < L::Q; ++q) {
       const double f = P.f64(q);
       const float nf = narrow_rn(n[q]);
+      nfr[q] = nf;
       // B1 += f_neq ln(f/w): ln(f/w) = C_q(d) + T_j + log1p(r'), r' = m inv_j - 1
       {
         const int64_t bits = __double_as_longlong(f);
@@ -744,14 +746,26 @@ __device__ __forceinline__ void elbm_node(const typename Storage<ST>::T* __restr
     rpos = fmaxf(rpos, rq);
     rabs = fmaxf(rabs, fabsf(rq));
   }
+  // nf_q = f_neq_q rounded to FP32, all the update needs: the series form
+  // fills it in its moment loop, past which the FP64 f_neq is dead
+  float nf[L::Q];
   // alpha_max = min(2.5, 1 / max_q r_q) over r_q > 0 (Collision.h:305-326);
   // the deviation test |f_neq|/f <= threshold (Collision.h:284-303)
   const bool small = !(rabs > p.deviation_threshold_f);
   const double alphaMax = rpos > 0.4f ? widen_exact(__frcp_rn(rpos)) : 2.5;
   double alpha = 2.0;
   bool direct = false;  // n[] holds r_q instead of f_neq_q
-  if (MODE == ELBM_MAIN && small) { ++cnt[CNT_SHORTCUT]; alpha = 2.0; }
-  else if (MODE == ELBM_MAIN && alphaMax < 2.0) { ++cnt[CNT_LIMITED]; alpha = 0.95 * alphaMax; }
+  if (MODE == ELBM_MAIN && small) {
+    ++cnt[CNT_SHORTCUT];
+    alpha = 2.0;
+#pragma unroll
+    for (int q = 0; q < L::Q; ++q) nf[q] = narrow_rn(n[q]);
+  } else if (MODE == ELBM_MAIN && alphaMax < 2.0) {
+    ++cnt[CNT_LIMITED];
+    alpha = 0.95 * alphaMax;
+#pragma unroll
+    for (int q = 0; q < L::Q; ++q) nf[q] = narrow_rn(n[q]);
+  }
   else {
     const bool series = MODE == ELBM_MAIN && rabs <= kSeriesRmax;
     if (MODE == ELBM_MAIN && !series) {
@@ -764,12 +778,12 @@ __device__ __forceinline__ void elbm_node(const typename Storage<ST>::T* __restr
       const double plain = p.guess_mode == GUESS_TWO ? 2.0 : prevA;
       const double guess = LEARNED ? 2.0 + widen_exact(learned) : plain;
       if constexpr (MODE == ELBM_MAIN) {
-        const auto ev = make_entropy_eval<LAT, ST, true>(P, n, rabs, s_log, s_fine, s_lnw);
+        const auto ev = make_entropy_eval<LAT, ST, true>(P, n, nf, rabs, s_log, s_fine, s_lnw);
         const double tol = p.newton_tol - series_error_bound<LAT, ST>(rabs, rho);
         alpha = residual_alpha_solve<decltype(ev), true>(ev, guess, plain, alphaMax, tol,
                                                          p.newton_maxit, cnt);
       } else {
-        const auto ev = make_entropy_eval<LAT, ST, false>(P, n, rabs, s_log, s_fine, s_lnw);
+        const auto ev = make_entropy_eval<LAT, ST, false>(P, n, nf, rabs, s_log, s_fine, s_lnw);
         alpha = residual_alpha_solve<decltype(ev), true>(ev, guess, plain, alphaMax,
                                                          p.newton_tol - 4e-15, p.newton_maxit, cnt);
       }
@@ -827,8 +841,8 @@ __device__ __forceinline__ void elbm_node(const typename Storage<ST>::T* __restr
     }
 #pragma unroll
     for (int q = 0; q < L::Q; ++q) {
-      const float nf = direct ? narrow_rn(n[q] * P.f64(q)) : narrow_rn(n[q]);
-      float rr = fmaf(-ab, nf, P.v[q]);  // f (F32) or f - w (F16)
+      const float nfq = direct ? narrow_rn(n[q] * P.f64(q)) : nf[q];
+      float rr = fmaf(-ab, nfq, P.v[q]);  // f (F32) or f - w (F16)
       if (FS == FS_GUO || FS == FS_EDM) rr += src[q];
       auto* dst = pop(next, p.V, q) + (uint32_t)idx;
       if constexpr (ST == ST_F32) *dst = rr;
@@ -855,13 +869,19 @@ __device__ __forceinline__ void elbm_node(const typename Storage<ST>::T* __restr
   }
 }
 
-// Resident blocks per SM the main pass's register allocation is sized for.
+// Resident blocks per SM the main pass's register allocation is sized for:
+// 3 (no spills) for the plain guess; 4 for the learned guess, whose
+// inference phase gains more from the extra warps than the spills cost
+// (measured on the 512^3 entropic workload: 950 against 909 MLUPS).
 #ifndef MLBM_ELBM_MIN_BLOCKS
 #define MLBM_ELBM_MIN_BLOCKS 3
 #endif
+#ifndef MLBM_ELBM_MIN_BLOCKS_LEARNED
+#define MLBM_ELBM_MIN_BLOCKS_LEARNED 4
+#endif
 
 template <int LAT, int FS, int ST, bool LEARNED>
-__global__ void __launch_bounds__(128, MLBM_ELBM_MIN_BLOCKS) elbm_lowp_kernel(const typename Storage<ST>::T* __restrict__ prev,
+__global__ void __launch_bounds__(128, LEARNED ? MLBM_ELBM_MIN_BLOCKS_LEARNED : MLBM_ELBM_MIN_BLOCKS) elbm_lowp_kernel(const typename Storage<ST>::T* __restrict__ prev,
                                                         typename Storage<ST>::T* __restrict__ next,
                                                         StepParams p) {
   __shared__ LogEntryFine s_fine[LOG_TABLE_FINE];
@@ -940,19 +960,20 @@ __global__ void entropy_test_kernel(const float* __restrict__ f, const double* _
   if (s >= nodes) return;
   Pulled<LAT, ST_F32> P;
   double n[L::Q];
-  float rabs = 0.0f;
+  float rabs = 0.0f, nf[L::Q];
 #pragma unroll
   for (int q = 0; q < L::Q; ++q) {
     P.v[q] = f[s * L::Q + q];
     n[q] = fneq[s * L::Q + q];
-    rabs = fmaxf(rabs, fabsf(narrow_rn(n[q]) * __frcp_rn(P.v[q])));
+    nf[q] = narrow_rn(n[q]);
+    rabs = fmaxf(rabs, fabsf(nf[q] * __frcp_rn(P.v[q])));
   }
   const bool series = mode == 2 || (mode == 0 && rabs <= kSeriesRmax);
   if (series) {
-    const auto ev = make_entropy_eval<LAT, ST_F32, true>(P, n, rabs, s_log, s_fine, s_lnw);
+    const auto ev = make_entropy_eval<LAT, ST_F32, true>(P, n, nf, rabs, s_log, s_fine, s_lnw);
     for (int i = 0; i < nx; ++i) ev(xs[i], Fo[s * nx + i], Do[s * nx + i]);
   } else {
-    const auto ev = make_entropy_eval<LAT, ST_F32, false>(P, n, rabs, s_log, s_fine, s_lnw);
+    const auto ev = make_entropy_eval<LAT, ST_F32, false>(P, n, nf, rabs, s_log, s_fine, s_lnw);
     for (int i = 0; i < nx; ++i) ev(xs[i], Fo[s * nx + i], Do[s * nx + i]);
   }
   series_out[s] = series ? 1 : 0;
