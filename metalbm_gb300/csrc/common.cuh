@@ -186,41 +186,63 @@ __device__ __forceinline__ float narrow_rn(double x) {
   return __uint_as_float(bits | (hi & 0x80000000u));
 }
 
-// Warp + block reduction of the diagnostics, written to partials[blockIdx.x].
+// Order-preserving integer key of a double, so that maxima and minima are
+// integer operations (GB300 runs FP64 compares on its narrow FP64 path):
+// non-negative values keep their bit pattern, negative ones are mirrored.
+__device__ __forceinline__ long long dkey(double x) {
+  const long long b = __double_as_longlong(x);
+  return b >= 0 ? b : b ^ 0x7fffffffffffffffLL;
+}
+__device__ __forceinline__ double dkey_value(long long k) {
+  return __longlong_as_double(k >= 0 ? k : k ^ 0x7fffffffffffffffLL);
+}
+
+// Block reduction of the diagnostics, written to partials[blockIdx.x]
+// (blocks of at most 256 threads). Sums in a fixed order — each lane of warp
+// 0 adds its column of the block's values in warp order, then a shuffle
+// tree — so the result does not depend on scheduling; maxima and minima on
+// integer keys.
 __device__ __forceinline__ void block_reduce_diag(double mass, double energy, double mach,
                                                   double amin, double amax, double* partials) {
-  __shared__ double sh[DIAG_FIELDS][32];
+  __shared__ double sh_sum[2][256];
+  __shared__ long long sh_key[3][8];
+  long long kmach = dkey(mach), kmin = dkey(amin), kmax = dkey(amax);
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
-    mass += __shfl_down_sync(0xffffffffu, mass, o);
-    energy += __shfl_down_sync(0xffffffffu, energy, o);
-    mach = fmax(mach, __shfl_down_sync(0xffffffffu, mach, o));
-    amin = fmin(amin, __shfl_down_sync(0xffffffffu, amin, o));
-    amax = fmax(amax, __shfl_down_sync(0xffffffffu, amax, o));
+    kmach = max(kmach, __shfl_down_sync(0xffffffffu, kmach, o));
+    kmin = min(kmin, __shfl_down_sync(0xffffffffu, kmin, o));
+    kmax = max(kmax, __shfl_down_sync(0xffffffffu, kmax, o));
   }
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  sh_sum[0][threadIdx.x] = mass;
+  sh_sum[1][threadIdx.x] = energy;
   if (lane == 0) {
-    sh[0][warp] = mass; sh[1][warp] = energy; sh[2][warp] = mach;
-    sh[3][warp] = amin; sh[4][warp] = amax;
+    sh_key[0][warp] = kmach; sh_key[1][warp] = kmin; sh_key[2][warp] = kmax;
   }
   __syncthreads();
   if (warp == 0) {
-    mass = lane < nw ? sh[0][lane] : 0.0;
-    energy = lane < nw ? sh[1][lane] : 0.0;
-    mach = lane < nw ? sh[2][lane] : 0.0;
-    amin = lane < nw ? sh[3][lane] : 1e300;
-    amax = lane < nw ? sh[4][lane] : -1e300;
+    double m = 0.0, e = 0.0;
+    for (int w = 0; w < nw; ++w) {
+      m += sh_sum[0][w * 32 + lane];
+      e += sh_sum[1][w * 32 + lane];
+    }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
-      mass += __shfl_down_sync(0xffffffffu, mass, o);
-      energy += __shfl_down_sync(0xffffffffu, energy, o);
-      mach = fmax(mach, __shfl_down_sync(0xffffffffu, mach, o));
-      amin = fmin(amin, __shfl_down_sync(0xffffffffu, amin, o));
-      amax = fmax(amax, __shfl_down_sync(0xffffffffu, amax, o));
+      m += __shfl_down_sync(0xffffffffu, m, o);
+      e += __shfl_down_sync(0xffffffffu, e, o);
+    }
+    kmach = lane < nw ? sh_key[0][lane] : dkey(0.0);
+    kmin = lane < nw ? sh_key[1][lane] : dkey(1e300);
+    kmax = lane < nw ? sh_key[2][lane] : dkey(-1e300);
+#pragma unroll
+    for (int o = 4; o > 0; o >>= 1) {
+      kmach = max(kmach, __shfl_down_sync(0xffffffffu, kmach, o));
+      kmin = min(kmin, __shfl_down_sync(0xffffffffu, kmin, o));
+      kmax = max(kmax, __shfl_down_sync(0xffffffffu, kmax, o));
     }
     if (lane == 0) {
       double* o = partials + (size_t)blockIdx.x * DIAG_FIELDS;
-      o[0] = mass; o[1] = energy; o[2] = mach; o[3] = amin; o[4] = amax;
+      o[0] = m; o[1] = e; o[2] = dkey_value(kmach); o[3] = dkey_value(kmin); o[4] = dkey_value(kmax);
     }
   }
 }

@@ -35,8 +35,12 @@ __global__ void finalize_diag_kernel(const double* __restrict__ partials, int nb
     }
     __syncthreads();
   }
-  if (threadIdx.x == 0)
+  if (threadIdx.x == 0) {
     for (int k = 0; k < DIAG_FIELDS; ++k) out[k] = sh[k][0];
+    // the nodes contribute |u|^2 / c_s^2; sqrt is monotonic and correctly
+    // rounded, so the root of the maximum is the maximum of the roots
+    out[2] = sqrt(sh[2][0]);
+  }
 }
 
 __global__ void fast_log_kernel(const double* __restrict__ x, double* __restrict__ out, long long n,

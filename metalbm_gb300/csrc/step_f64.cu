@@ -195,7 +195,7 @@ __device__ __forceinline__ void store_node_fields(const StepParams& p, long long
     energy = 0.0;
 #pragma unroll
     for (int d = 0; d < L::D; ++d) energy = energy + 0.5 * rho * uh[d] * uh[d];
-    mach = sqrt(3.0 * norm2<LAT>(uh));
+    mach = 3.0 * norm2<LAT>(uh);  // |u|^2 / c_s^2; the square root is taken once, in finalize_diag
   }
 }
 

@@ -243,16 +243,17 @@ __device__ __forceinline__ void node_force_f(const StepParams& p, uint32_t x, ui
   for (int k = 0; k < 3; ++k) Ff[k] = (float)F[k];
 }
 
+// Stored fields and the diagnostics' node terms from FP64 rho and u (the
+// hydrodynamic velocity u + F/(2 rho) for the shifted forcing schemes).
 template <int LAT>
-__device__ __forceinline__ void lowp_store_fields(const StepParams& p, long long idx, float rho,
-                                                  const float u[3], const double F[3], bool shifted,
-                                                  double alpha, double& energy, double& mach,
-                                                  bool write_alpha = true) {
+__device__ __forceinline__ void store_fields_f64(const StepParams& p, long long idx, double r,
+                                                 const double u[3], const double F[3],
+                                                 bool shifted, double alpha, double& energy,
+                                                 double& mach, bool write_alpha = true) {
   using L = Lattice<LAT>;
   double uh[3] = {0.0, 0.0, 0.0};
-  const double r = (double)rho;
 #pragma unroll
-  for (int k = 0; k < L::D; ++k) uh[k] = shifted ? (double)u[k] + F[k] * (0.5 / r) : (double)u[k];
+  for (int k = 0; k < L::D; ++k) uh[k] = shifted ? u[k] + F[k] * (0.5 / r) : u[k];
   if (p.store) {
     p.rho_out[idx] = r;
 #pragma unroll
@@ -270,8 +271,17 @@ __device__ __forceinline__ void lowp_store_fields(const StepParams& p, long long
       s += uh[k] * uh[k];
     }
     energy = e;
-    mach = sqrt(3.0 * s);
+    mach = 3.0 * s;  // |u|^2 / c_s^2; the square root is taken once, in finalize_diag
   }
+}
+
+template <int LAT>
+__device__ __forceinline__ void lowp_store_fields(const StepParams& p, long long idx, float rho,
+                                                  const float u[3], const double F[3], bool shifted,
+                                                  double alpha, double& energy, double& mach,
+                                                  bool write_alpha = true) {
+  const double ud[3] = {(double)u[0], (double)u[1], (double)u[2]};
+  store_fields_f64<LAT>(p, idx, (double)rho, ud, F, shifted, alpha, energy, mach, write_alpha);
 }
 
 // ---- BGK ------------------------------------------------------------------
@@ -862,9 +872,7 @@ __device__ __forceinline__ void elbm_node(const typename Storage<ST>::T* __restr
       mass = rho;
       double F[3] = {0.0, 0.0, 0.0};
       if (FS != FS_NONE) node_force<L::D>(p, x, y, z, F);
-      const float ufl[3] = {narrow_rn(u[0]), narrow_rn(u[1]), narrow_rn(u[2])};
-      lowp_store_fields<LAT>(p, idx, narrow_rn(rho), ufl, F, FS != FS_NONE, alpha, energy, mach,
-                             !defer);
+      store_fields_f64<LAT>(p, idx, rho, u, F, FS != FS_NONE, alpha, energy, mach, !defer);
     }
   }
 }
@@ -980,21 +988,9 @@ __global__ void entropy_test_kernel(const float* __restrict__ f, const double* _
 }
 
 // ---- init and conversions ---------------------------------------------------
-// f_eq(rho, u) is formed in FP64 with the reference polynomial, then encoded.
-template <int LAT>
-__device__ double feq_f64(double rho, const double u[3], int q) {
-  using L = Lattice<LAT>;
-  double cu = 0.0, u2 = 0.0;
-#pragma unroll
-  for (int k = 0; k < L::D; ++k) {
-    cu += L::c(q, k) * u[k];
-    u2 += u[k] * u[k];
-  }
-  const double P = 3.0 * cu - 1.5 * u2 + 4.5 * cu * cu - 4.5 * cu * u2 + 4.5 * cu * cu * cu +
-                   1.125 * u2 * u2 - 6.75 * cu * cu * u2 + 3.375 * cu * cu * cu * cu;
-  return rho * L::w(q) * (1.0 + P);
-}
-
+// f_eq(rho, u) formed in FP64 with the TruncationMa3 polynomial in its pair form
+// (Equilibrium.h:17-33), rounded once into the storage format with integer
+// operations (no FP64 conversion instruction).
 template <int LAT, int ST>
 __global__ void init_lowp_kernel(const double* __restrict__ rho, const double* __restrict__ u,
                                  typename Storage<ST>::T* __restrict__ f, long long V) {
@@ -1004,9 +1000,14 @@ __global__ void init_lowp_kernel(const double* __restrict__ rho, const double* _
   double uu[3] = {0.0, 0.0, 0.0};
 #pragma unroll
   for (int k = 0; k < L::D; ++k) uu[k] = u[(long long)k * V + idx];
+  double feq[L::Q];
+  feq_pairs_f64<LAT>(rho[idx], uu, feq);
 #pragma unroll
-  for (int q = 0; q < L::Q; ++q)
-    f[(long long)q * V + idx] = Storage<ST>::template encode<LAT>(feq_f64<LAT>(rho[idx], uu, q), q);
+  for (int q = 0; q < L::Q; ++q) {
+    auto* dst = pop(f, V, q) + (uint32_t)idx;
+    if constexpr (ST == ST_F32) *dst = narrow_rn(feq[q]);
+    else *dst = __float2half_rn(narrow_rn((feq[q] - L::w(q)) * (double)(1 << shift_exponent<LAT>(q))));
+  }
 }
 
 template <int LAT, int ST>

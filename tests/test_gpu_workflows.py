@@ -98,3 +98,28 @@ def test_sync_gives_up_after_its_timeout():
         lat.sync(-1)
         lat.step(1, diagnostics=True)
         assert lat.diagnostics()["solved_nodes"] > 0
+
+
+@pytest.mark.gpu
+def test_registered_host_buffers_round_trip():
+    """Fields through page-locked, huge-page host arrays equal those through
+    ordinary numpy arrays."""
+    from metalbm_gb300 import InputDeck, Lattice, fields
+    from metalbm_gb300.hostbuf import pinned_array
+    import ctypes as ct
+    shape = (24, 20, 16)
+    V = 24 * 20 * 16
+    rho, u = fields.perturbed_rest(shape, 3, 1e-3, seed=4, rho_amplitude=1e-3)
+    h_rho, h_u = pinned_array((V,)), pinned_array((3, V))
+    h_rho[:] = rho
+    h_u[:] = u
+    deck = InputDeck(latticeT="D3Q19", relaxationTime=0.6, globalLength=shape, storage="f32")
+    with Lattice(deck) as lat:
+        lat.init_equilibrium(h_rho, h_u)
+        lat.step(3, store=True)
+        o_rho, o_u = pinned_array((V,)), pinned_array((3, V))
+        dp = ct.POINTER(ct.c_double)
+        assert lat._lib.mlbm_get_fields(lat.handle, o_rho.ctypes.data_as(dp),
+                                        o_u.ctypes.data_as(dp), None, None, 0) == 0
+        ref = lat.fields()
+    assert np.array_equal(o_rho, ref["rho"]) and np.array_equal(o_u, ref["u"])
