@@ -656,8 +656,9 @@ extern "C" int mlbm_step(mlbm_handle* h, int nsteps, unsigned int flags) {
     count_launches(h->defer_blocks > 0 ? 2 : 1);
     if (e != cudaSuccess) return fail(h, MLBM_ERR_CUDA, "step kernel: %s", cudaGetErrorString(e));
     if (p.diag) {
-      const int bs = collision ? 128 : 256;
-      const int nb = (int)((h->V + bs - 1) / bs) + h->defer_blocks;
+      const int nb = collision ? (int)((h->V + 127) / 128) + h->defer_blocks
+                               : (int)bgk_step_blocks(h->cfg.lattice, h->storage, h->V,
+                                                      (unsigned)h->base.lz);
       e = finalize_diag(h->partials, nb, h->diag_dev, h->stream);
       count_launches(1);
       if (e != cudaSuccess) return fail(h, MLBM_ERR_CUDA, "diagnostics: %s", cudaGetErrorString(e));

@@ -319,7 +319,98 @@ __device__ __forceinline__ void node_force_float(const StepParams& p, uint32_t x
 // = kt w_q (3 cu cF - u.F +- cF) for the pair; EDM: S_q = w_q rho (P_q(v) - P_q(u)),
 // v = u + F/rho (ForcingScheme.h:183-197). Every population is carried in its
 // storage scale (d'_q = S_q d_q, Storage::scale), the factors S_q and 1/S_q
-// folded into the per-population constants.
+// folded into the per-population constants. `d` holds the pulled values on
+// entry and the post-collision values on exit.
+template <int LAT, int FS, int ST>
+__device__ __forceinline__ void bgk_node(const StepParams& p, uint32_t x, uint32_t y, uint32_t z,
+                                         float d[Lattice<LAT>::Q], float& rho_out,
+                                         float u[3]) {
+  using L = Lattice<LAT>;
+  using S = Storage<ST>;
+  float rhop = 0.0f, j[3] = {0.0f, 0.0f, 0.0f};
+#pragma unroll
+  for (int q = 0; q < L::Q; ++q) {
+    const float is = 1.0f / S::template scale<LAT>(q);
+    rhop = fmaf(d[q], is, rhop);
+#pragma unroll
+    for (int k = 0; k < L::D; ++k) {
+      if (L::c(q, k) > 0) j[k] = fmaf(d[q], is, j[k]);
+      if (L::c(q, k) < 0) j[k] = fmaf(d[q], -is, j[k]);
+    }
+  }
+  const float rho = 1.0f + rhop;
+  const float irho = 1.0f / rho;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) u[k] = j[k] * irho;
+  float F[3] = {0.0f, 0.0f, 0.0f};
+  if (FS != FS_NONE) node_force_float<L::D>(p, x, y, z, F);
+  const float u2 = u[0] * u[0] + u[1] * u[1] + u[2] * u[2];
+  const PolyNode n = poly_node(u2);
+  const float b = p.bgk_b_f;
+  float uF = 0.0f, v[3] = {0.0f, 0.0f, 0.0f};
+  PolyNode nv = n;
+  if (FS == FS_GUO) uF = u[0] * F[0] + u[1] * F[1] + u[2] * F[2];
+  if (FS == FS_EDM) {
+#pragma unroll
+    for (int k = 0; k < 3; ++k) v[k] = fmaf(F[k], irho, u[k]);
+    nv = poly_node(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+  }
+  {  // rest population
+    const float ws = (float)L::w(0) * S::template scale<LAT>(0);
+    const float deq = ws * fmaf(rho, n.common, rhop);
+    float r = fmaf(b, deq - d[0], d[0]);
+    if (FS == FS_GUO) r = fmaf(p.guo_kt_f * ws, -uF, r);
+    if (FS == FS_EDM) r = fmaf(ws * rho, nv.common - n.common, r);
+    d[0] = r;
+  }
+#pragma unroll
+  for (int q = 1; q < L::Q; ++q) {
+    if (is_pair_leader<LAT>(q)) {
+      const int qb = opposite<LAT>(q);
+      // opposite populations share w_q and therefore S_q
+      const float ws = (float)L::w(q) * S::template scale<LAT>(q);
+      const float cu = cdotf<LAT>(q, u);
+      float E, O;
+      poly_pair(n, cu, E, O);
+      const float dq = ws * fmaf(rho, E + O, rhop), dqb = ws * fmaf(rho, E - O, rhop);
+      float rq = fmaf(b, dq - d[q], d[q]);
+      float rqb = fmaf(b, dqb - d[qb], d[qb]);
+      if (FS == FS_GUO) {
+        const float cF = cdotf<LAT>(q, F);
+        const float Es = fmaf(3.0f * cu, cF, -uF);
+        const float kw = p.guo_kt_f * ws;
+        rq = fmaf(kw, Es + cF, rq);
+        rqb = fmaf(kw, Es - cF, rqb);
+      }
+      if (FS == FS_EDM) {
+        float Ev, Ov;
+        poly_pair(nv, cdotf<LAT>(q, v), Ev, Ov);
+        const float wr = ws * rho;
+        rq = fmaf(wr, (Ev + Ov) - (E + O), rq);
+        rqb = fmaf(wr, (Ev - Ov) - (E - O), rqb);
+      }
+      d[q] = rq;
+      d[qb] = rqb;
+    }
+  }
+  rho_out = rho;
+}
+
+template <int LAT, int FS, int ST>
+__device__ __forceinline__ void bgk_node_fields(const StepParams& p, long long idx, uint32_t x,
+                                                uint32_t y, uint32_t z, float rho,
+                                                const float u[3], double& mass, double& energy,
+                                                double& mach) {
+  using L = Lattice<LAT>;
+  if (!(rho > 0.0f) || !isfinite(rho)) atomicOr(p.err_word, ERR_NONFINITE);
+  if (p.store || p.diag) {
+    double Fd[3];
+    node_force<L::D>(p, x, y, z, Fd);
+    if (p.diag) mass = (double)rho;
+    lowp_store_fields<LAT>(p, idx, rho, u, Fd, FS != FS_NONE, 2.0, energy, mach);
+  }
+}
+
 template <int LAT, int FS, int ST>
 __global__ void __launch_bounds__(256) bgk_lowp_kernel(const typename Storage<ST>::T* __restrict__ prev,
                                                        typename Storage<ST>::T* __restrict__ next,
@@ -337,80 +428,63 @@ __global__ void __launch_bounds__(256) bgk_lowp_kernel(const typename Storage<ST
 #pragma unroll
     for (int q = 0; q < L::Q; ++q)
       d[q] = S::template load_scaled<LAT>(pop(prev, p.V, q) + o.at(L::c(q, 0), L::c(q, 1), L::c(q, 2)), q);
-    float rhop = 0.0f, j[3] = {0.0f, 0.0f, 0.0f};
+    float rho, u[3];
+    bgk_node<LAT, FS, ST>(p, x, y, z, d, rho, u);
+#pragma unroll
+    for (int q = 0; q < L::Q; ++q) S::template store_scaled<LAT>(pop(next, p.V, q) + (uint32_t)idx, q, d[q]);
+    bgk_node_fields<LAT, FS, ST>(p, idx, x, y, z, rho, u, mass, energy, mach);
+  }
+  if (p.diag) block_reduce_diag(mass, energy, mach, 2.0, 2.0, p.diag_partials);
+}
+
+// FP16-shifted storage, two z-adjacent nodes a thread (z even, Lz even): the
+// populations with c_z = 0 load as one aligned half2 for both nodes, every
+// population stores as one half2, and the node's coordinates and periodic
+// offsets are formed once for the pair.
+template <int LAT, int FS>
+__global__ void __launch_bounds__(256) bgk_f16_pair_kernel(const __half* __restrict__ prev,
+                                                           __half* __restrict__ next,
+                                                           StepParams p) {
+  using L = Lattice<LAT>;
+  const long long idx = 2 * ((long long)blockIdx.x * blockDim.x + threadIdx.x);
+  const bool active = idx < p.V;
+  double mass = 0.0, energy = 0.0, mach = 0.0;
+  if (active) {
+    uint32_t x, y, z;
+    node_coords(p, idx, x, y, z);  // z even
+    const PullOffsets o = pull_offsets(p, x, y, z);
+    // second node's z neighbours: z + 1 reads z + 2 (c_z = -1) and z (c_z = +1)
+    const uint32_t z2p = (z + 2 == p.lz) ? 0 : z + 2;
+    float d0[L::Q], d1[L::Q];
 #pragma unroll
     for (int q = 0; q < L::Q; ++q) {
-      const float is = 1.0f / S::template scale<LAT>(q);
-      rhop = fmaf(d[q], is, rhop);
-#pragma unroll
-      for (int k = 0; k < L::D; ++k) {
-        if (L::c(q, k) > 0) j[k] = fmaf(d[q], is, j[k]);
-        if (L::c(q, k) < 0) j[k] = fmaf(d[q], -is, j[k]);
+      const __half* src = pop(prev, p.V, q);
+      const int cx = L::c(q, 0), cy = L::c(q, 1), cz = L::c(q, 2);
+      const uint32_t xy = o.ox[cx + 1] + o.oy[cy + 1];
+      if (cz == 0) {
+        const __half2 h = __ldg(reinterpret_cast<const __half2*>(src + xy + z));
+        d0[q] = __low2float(h);
+        d1[q] = __high2float(h);
+      } else if (cz > 0) {  // reads z - 1 and z
+        d0[q] = __half2float(__ldg(src + xy + o.oz[2]));
+        d1[q] = __half2float(__ldg(src + xy + z));
+      } else {  // reads z + 1 and z + 2
+        d0[q] = __half2float(__ldg(src + xy + o.oz[0]));
+        d1[q] = __half2float(__ldg(src + xy + z2p));
       }
     }
-    const float rho = 1.0f + rhop;
-    const float irho = 1.0f / rho;
-    float u[3];
+    float rho0, u0[3], rho1, u1[3];
+    bgk_node<LAT, FS, ST_F16>(p, x, y, z, d0, rho0, u0);
+    bgk_node<LAT, FS, ST_F16>(p, x, y, z + 1, d1, rho1, u1);
 #pragma unroll
-    for (int k = 0; k < 3; ++k) u[k] = j[k] * irho;
-    float F[3] = {0.0f, 0.0f, 0.0f};
-    if (FS != FS_NONE) node_force_float<L::D>(p, x, y, z, F);
-    const float u2 = u[0] * u[0] + u[1] * u[1] + u[2] * u[2];
-    const PolyNode n = poly_node(u2);
-    const float b = p.bgk_b_f;
-    float uF = 0.0f, v[3] = {0.0f, 0.0f, 0.0f};
-    PolyNode nv = n;
-    if (FS == FS_GUO) uF = u[0] * F[0] + u[1] * F[1] + u[2] * F[2];
-    if (FS == FS_EDM) {
-#pragma unroll
-      for (int k = 0; k < 3; ++k) v[k] = fmaf(F[k], irho, u[k]);
-      nv = poly_node(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
-    }
-    {  // rest population
-      const float ws = (float)L::w(0) * S::template scale<LAT>(0);
-      const float deq = ws * fmaf(rho, n.common, rhop);
-      float r = fmaf(b, deq - d[0], d[0]);
-      if (FS == FS_GUO) r = fmaf(p.guo_kt_f * ws, -uF, r);
-      if (FS == FS_EDM) r = fmaf(ws * rho, nv.common - n.common, r);
-      S::template store_scaled<LAT>(next + (uint32_t)idx, 0, r);
-    }
-#pragma unroll
-    for (int q = 1; q < L::Q; ++q) {
-      if (is_pair_leader<LAT>(q)) {
-        const int qb = opposite<LAT>(q);
-        // opposite populations share w_q and therefore S_q
-        const float ws = (float)L::w(q) * S::template scale<LAT>(q);
-        const float cu = cdotf<LAT>(q, u);
-        float E, O;
-        poly_pair(n, cu, E, O);
-        const float dq = ws * fmaf(rho, E + O, rhop), dqb = ws * fmaf(rho, E - O, rhop);
-        float rq = fmaf(b, dq - d[q], d[q]);
-        float rqb = fmaf(b, dqb - d[qb], d[qb]);
-        if (FS == FS_GUO) {
-          const float cF = cdotf<LAT>(q, F);
-          const float Es = fmaf(3.0f * cu, cF, -uF);
-          const float kw = p.guo_kt_f * ws;
-          rq = fmaf(kw, Es + cF, rq);
-          rqb = fmaf(kw, Es - cF, rqb);
-        }
-        if (FS == FS_EDM) {
-          float Ev, Ov;
-          poly_pair(nv, cdotf<LAT>(q, v), Ev, Ov);
-          const float wr = ws * rho;
-          rq = fmaf(wr, (Ev + Ov) - (E + O), rq);
-          rqb = fmaf(wr, (Ev - Ov) - (E - O), rqb);
-        }
-        S::template store_scaled<LAT>(pop(next, p.V, q) + (uint32_t)idx, q, rq);
-        S::template store_scaled<LAT>(pop(next, p.V, qb) + (uint32_t)idx, qb, rqb);
-      }
-    }
-    if (!(rho > 0.0f) || !isfinite(rho)) atomicOr(p.err_word, ERR_NONFINITE);
-    if (p.store || p.diag) {
-      double Fd[3];
-      node_force<L::D>(p, x, y, z, Fd);
-      if (p.diag) mass = (double)rho;
-      lowp_store_fields<LAT>(p, idx, rho, u, Fd, FS != FS_NONE, 2.0, energy, mach);
-    }
+    for (int q = 0; q < L::Q; ++q)
+      *reinterpret_cast<__half2*>(pop(next, p.V, q) + (uint32_t)idx) = __floats2half2_rn(d0[q], d1[q]);
+    double m1 = 0.0, e1 = 0.0, a1 = 0.0;
+    bgk_node_fields<LAT, FS, ST_F16>(p, idx, x, y, z, rho0, u0, mass, energy, mach);
+    bgk_node_fields<LAT, FS, ST_F16>(p, idx + 1, x, y, z + 1, rho1, u1, m1, e1, a1);
+    mass += m1;
+    energy += e1;
+    mach = fmax(mach, a1);
   }
   if (p.diag) block_reduce_diag(mass, energy, mach, 2.0, 2.0, p.diag_partials);
 }
@@ -1078,8 +1152,13 @@ static cudaError_t launch_lowp(int collision, const void* prev, void* next, cons
   using T = typename Storage<ST>::T;
   if (collision == 0) {
     const int bs = 256;
-    const unsigned grid = (unsigned)((p.V + bs - 1) / bs);
-    bgk_lowp_kernel<LAT, FS, ST><<<grid, bs, 0, s>>>((const T*)prev, (T*)next, p);
+    if (bgk_pairs(LAT, ST, p.lz)) {
+      const unsigned grid = (unsigned)bgk_step_blocks(LAT, ST, p.V, p.lz);
+      bgk_f16_pair_kernel<LAT, FS><<<grid, bs, 0, s>>>((const __half*)prev, (__half*)next, p);
+    } else {
+      const unsigned grid = (unsigned)((p.V + bs - 1) / bs);
+      bgk_lowp_kernel<LAT, FS, ST><<<grid, bs, 0, s>>>((const T*)prev, (T*)next, p);
+    }
   } else {
     const int bs = 128;
     const unsigned grid = (unsigned)((p.V + bs - 1) / bs);
