@@ -577,7 +577,8 @@ struct HLowp {
 // storage): the FP64 part sum f_neq^2 y0 plus an FP32 correction.
 // The evaluation error of F is bounded per node (F's error sources):
 //   FP32 M3 (tier A):   (2.5^3/6) 2.1e-6 rho rmax^3 (9 roundings a term,
-//                       26 in the sum) = 5.5e-6 rho rmax^3, M4.. smaller;
+//                       26 in the sum, the seeds from the SFU reciprocal) = 6.0e-6 rho rmax^3,
+//                       M4.. smaller;
 //   FP32 M5 (tier B):   (2.5^5/20) 2.3e-6 rho rmax^5;
 //   B1 (fast_log_fine and the FP32 tail sum): 2.5 x 2.4e-13 rho rmax;
 //   FP64 rounding and the k > 8 truncation: < 1e-15.
@@ -585,10 +586,48 @@ struct HLowp {
 // exact function stays within tol.
 constexpr float kSeriesTierA = 0.0025f;
 
+// SFU reciprocal (rcp.approx.ftz.f32, relative error below 2^-22): seeds of
+// the FP64 reciprocals and the FP32 r_q, where an approximation is all that
+// is needed.
+__device__ __forceinline__ float rcp_sfu(float x) {
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+
+// True when every weight of the lattice has the same binary significand
+// (D2Q9: 4/9, 1/9, 1/36; D3Q27: 8/27 4^-k), so that the constants
+// C_q(d) = d ln 2 - ln(m_q) of ln(f_q/w_q) share their second term.
+template <int LAT>
+__host__ __device__ constexpr bool uniform_weight_significand() {
+  using L = Lattice<LAT>;
+  double m0 = L::w(0);
+  for (int e = exponent_of(m0); e > 0; --e) m0 *= 0.5;
+  for (int e = exponent_of(L::w(0)); e < 0; ++e) m0 *= 2.0;
+  for (int q = 1; q < L::Q; ++q) {
+    double m = L::w(q);
+    for (int e = exponent_of(L::w(q)); e > 0; --e) m *= 0.5;
+    for (int e = exponent_of(L::w(q)); e < 0; ++e) m *= 2.0;
+    if (m != m0) return false;
+  }
+  return true;
+}
+
+// v * 2^64 truncated to an integer, |v| < 2^-6 (zero for |v| < 2^-1022).
+__device__ __forceinline__ long long fixed64(double v) {
+  const long long b = __double_as_longlong(v);
+  const int e = (int)((b >> 52) & 0x7ff);
+  const long long m = (b & 0x000fffffffffffffLL) | 0x0010000000000000LL;  // v = m 2^(e - 1075)
+  const int sh = e - 1011;                                                 // v 2^64 = m 2^(e - 1011)
+  long long a = sh >= 0 ? (m << min(sh, 10)) : (sh > -64 ? (m >> -sh) : 0LL);
+  if (e == 0) a = 0;
+  return b < 0 ? -a : a;
+}
+
 template <int LAT, int ST>
 __device__ __forceinline__ double series_error_bound(float rabs, double rho) {
   const float r = rabs, rf = narrow_rn(rho);
-  const float m = r <= kSeriesTierA ? 5.6e-6f * r * r * r : 1.2e-5f * (r * r) * (r * r) * r;
+  const float m = r <= kSeriesTierA ? 6.0e-6f * r * r * r : 1.2e-5f * (r * r) * (r * r) * r;
   return widen_exact(fmaf(rf, fmaf(6.0e-13f, r, m), 1.0e-15f));
 }
 
@@ -609,6 +648,7 @@ __device__ __forceinline__ HLowp<LAT, ST, SERIES> make_entropy_eval(const Pulled
     double M2 = 0.0, M3 = 0.0, M4 = 0.0;
     float B1t = 0.0f, M2c = 0.0f, M3f = 0.0f, M4f = 0.0f, M5 = 0.0f, M6 = 0.0f, M7 = 0.0f,
           M8 = 0.0f;
+    long long nd = 0;  // sum_q f_neq_q d_q 2^64 (lattices with one weight significand)
 #pragma unroll
     for (int q = 0; q < L::Q; ++q) {
       const double f = P.f64(q);
@@ -621,15 +661,24 @@ __device__ __forceinline__ HLowp<LAT, ST, SERIES> make_entropy_eval(const Pulled
         const LogEntryFine t = fine[(bits >> 42) & (LOG_TABLE_FINE - 1)];
         const double m = __longlong_as_double((bits & 0x000fffffffffffffLL) | 0x3ff0000000000000LL);
         const double rp = fma(m, t.inv, -1.0);
-        double C;
-        if (d >= -1 && d <= 1) C = lnw[3 * q + d + 1];
-        else C = fma(exponent_as_double(d), kLn2, lnw[3 * q + 1]);
-        B1 = fma(n[q], (C + t.hi) + rp, B1);
+        if constexpr (uniform_weight_significand<LAT>()) {
+          // sum_q f_neq_q C_q(d_q) = ln 2 sum_q f_neq_q d_q - ln(m) sum_q f_neq_q, and
+          // sum_q f_neq_q = 0: the exponent term accumulates exactly in fixed point
+          B1 = fma(n[q], t.hi + rp, B1);
+          if (d == 1) nd += fixed64(n[q]);
+          else if (d == -1) nd -= fixed64(n[q]);
+          else if (d != 0) B1 = fma(n[q], exponent_as_double(d) * kLn2, B1);
+        } else {
+          double C;
+          if (d >= -1 && d <= 1) C = lnw[3 * q + d + 1];
+          else C = fma(exponent_as_double(d), kLn2, lnw[3 * q + 1]);
+          B1 = fma(n[q], (C + t.hi) + rp, B1);
+        }
         const float rpf = narrow_rn(rp);
         B1t = fmaf(nf, (rpf * rpf) * fmaf(rpf, 1.0f / 3.0f, -0.5f), B1t);
       }
       // moments
-      const float y0f = __frcp_rn(P.f32(q));
+      const float y0f = rcp_sfu(P.f32(q));
       const double y0 = widen_exact(y0f);
       float e;
       if constexpr (ST == ST_F32) e = fmaf(-P.v[q], y0f, 1.0f);
@@ -654,6 +703,8 @@ __device__ __forceinline__ HLowp<LAT, ST, SERIES> make_entropy_eval(const Pulled
       t *= rf; M8 += t;
     }
     B1 += widen_exact(B1t);
+    if constexpr (uniform_weight_significand<LAT>())
+      B1 = fma((double)nd, kLn2 * 0x1p-64, B1);
     M2 += widen_exact(M2c);
     if (!tierB) { M3 = widen_exact(M3f); M4 = widen_exact(M4f); }
     ev.S = HSeries{B1, M2 * 0.5, M3 * (1.0 / 6.0), M4 * (1.0 / 12.0), M2, M3 * 0.5,
@@ -826,7 +877,7 @@ __device__ __forceinline__ void elbm_node(const typename Storage<ST>::T* __restr
   float rpos = 0.0f, rabs = 0.0f;
 #pragma unroll
   for (int q = 0; q < L::Q; ++q) {
-    const float rq = narrow_rn(n[q]) * __frcp_rn(P.f32(q));
+    const float rq = narrow_rn(n[q]) * rcp_sfu(P.f32(q));
     rpos = fmaxf(rpos, rq);
     rabs = fmaxf(rabs, fabsf(rq));
   }
@@ -1048,7 +1099,7 @@ __global__ void entropy_test_kernel(const float* __restrict__ f, const double* _
     P.v[q] = f[s * L::Q + q];
     n[q] = fneq[s * L::Q + q];
     nf[q] = narrow_rn(n[q]);
-    rabs = fmaxf(rabs, fabsf(nf[q] * __frcp_rn(P.v[q])));
+    rabs = fmaxf(rabs, fabsf(nf[q] * rcp_sfu(P.v[q])));
   }
   const bool series = mode == 2 || (mode == 0 && rabs <= kSeriesRmax);
   if (series) {

@@ -24,7 +24,7 @@ def series_bound(rmax, rho):
     """The series form's evaluation-error bound (the kernel's
     series_error_bound): FP32 M3 below rmax = 2.5e-3, FP32 M5 above, the B1
     logarithms and FP64 rounding."""
-    m = np.where(rmax <= 0.0025, 5.6e-6 * rmax ** 3, 1.2e-5 * rmax ** 5)
+    m = np.where(rmax <= 0.0025, 6.0e-6 * rmax ** 3, 1.2e-5 * rmax ** 5)
     return rho * (m + 6e-13 * rmax) + 1e-15
 
 
