@@ -1003,11 +1003,13 @@ __device__ __forceinline__ void elbm_node(const typename Storage<ST>::T* __restr
 }
 
 // Resident blocks per SM the main pass's register allocation is sized for:
-// 3 (no spills) for the plain guess; 4 for the learned guess, whose
-// inference phase gains more from the extra warps than the spills cost
-// (measured on the 512^3 entropic workload: 950 against 909 MLUPS).
+// 4 blocks of 128 threads (128 registers, a few spills). Measured on the 512^3
+// entropic workload, 4 blocks beat 3 (156 registers, no spills) for both
+// variants: 1177 against 1078 MLUPS with the previous-alpha guess, 1096
+// against 1004 with the learned guess; the extra warps hide the phases in
+// which the FP64 pipe would otherwise idle (loads, inference).
 #ifndef MLBM_ELBM_MIN_BLOCKS
-#define MLBM_ELBM_MIN_BLOCKS 3
+#define MLBM_ELBM_MIN_BLOCKS 4
 #endif
 #ifndef MLBM_ELBM_MIN_BLOCKS_LEARNED
 #define MLBM_ELBM_MIN_BLOCKS_LEARNED 4

@@ -71,11 +71,14 @@ def test_tensor_core_inference_matches_bf16_restatement(lat, n_in):
     got = lat.alpha_model_predict(m, X)
     ref = mlp_oracle.predict_bf16(m, X)
     err = np.abs(got - ref) / m.output_scale
-    # FP32 accumulation order can move a hidden activation across a bfloat16
-    # rounding boundary (one bf16 ulp = 2^-8 relative): rare outliers are
-    # bounded by that, the bulk agrees to float rounding.
-    assert np.quantile(err, 0.99) <= 2e-5
-    assert err.max() <= 2e-3
+    # The kernel's tanh is the hardware approximation (absolute error below
+    # 2^-10) and its FP32 accumulation order differs, which can move a hidden
+    # activation across a bfloat16 rounding boundary (2^-8 relative): the
+    # output stays within a few 1e-3 of the BF16 restatement (relative to
+    # output_scale), where a layout or indexing error gives O(1).
+    assert np.quantile(err, 0.5) <= 1e-3
+    assert np.quantile(err, 0.99) <= 5e-3
+    assert err.max() <= 2e-2
 
 
 @pytest.mark.gpu
