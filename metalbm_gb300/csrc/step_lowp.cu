@@ -482,9 +482,11 @@ __global__ void __launch_bounds__(256) bgk_f16_pair_kernel(const __half* __restr
     double m1 = 0.0, e1 = 0.0, a1 = 0.0;
     bgk_node_fields<LAT, FS, ST_F16>(p, idx, x, y, z, rho0, u0, mass, energy, mach);
     bgk_node_fields<LAT, FS, ST_F16>(p, idx + 1, x, y, z + 1, rho1, u1, m1, e1, a1);
-    mass += m1;
-    energy += e1;
-    mach = fmax(mach, a1);
+    if (p.diag) {  // FP64 only on diagnostics steps
+      mass += m1;
+      energy += e1;
+      mach = fmax(mach, a1);
+    }
   }
   if (p.diag) block_reduce_diag(mass, energy, mach, 2.0, 2.0, p.diag_partials);
 }
