@@ -24,6 +24,12 @@ int mlbm_testing_fast_log(const double* x, double* out, long long n);
 int mlbm_testing_entropy(int lattice, const float* f, const double* fneq, long long nodes,
                          const double* x, int nx, int mode, double* F, double* D, int* series);
 
+/* f_neq[nodes][Q] of nodes given as FP32 populations f[nodes][Q] (the stored
+ * values of FP32 storage), formed as the FP32-storage entropic step forms it:
+ * exact fixed-point density and momentum, then the TruncationMa3 equilibrium
+ * in double-float arithmetic (dfloat = 1) or FP64 (dfloat = 0). Host arrays. */
+int mlbm_testing_neq(int lattice, const float* f, long long nodes, int dfloat, double* fneq);
+
 #ifdef __cplusplus
 }
 #endif

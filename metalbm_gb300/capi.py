@@ -34,7 +34,7 @@ EXPORTS = [
     "mlbm_last_error", "mlbm_kernel_launch_count", "mlbm_step_f64_noalloc",
     "mlbm_get_alpha", "mlbm_set_alpha",
 ]
-TESTING_EXPORTS = ["mlbm_testing_fast_log", "mlbm_testing_entropy"]
+TESTING_EXPORTS = ["mlbm_testing_fast_log", "mlbm_testing_entropy", "mlbm_testing_neq"]
 
 
 class Config(ct.Structure):
@@ -119,6 +119,7 @@ def load(path: Path | str | None = None):
         "mlbm_testing_fast_log": ([dp, dp, ct.c_longlong], ct.c_int),
         "mlbm_testing_entropy": ([ct.c_int, fp, dp, ct.c_longlong, dp, ct.c_int, ct.c_int, dp,
                                   dp, ct.POINTER(ct.c_int)], ct.c_int),
+        "mlbm_testing_neq": ([ct.c_int, fp, ct.c_longlong, ct.c_int, dp], ct.c_int),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)

@@ -1013,3 +1013,24 @@ extern "C" int mlbm_testing_entropy(int lattice, const float* f, const double* f
   if (e != cudaSuccess) return fail(nullptr, MLBM_ERR_CUDA, "entropy test: %s", cudaGetErrorString(e));
   return MLBM_OK;
 }
+
+extern "C" int mlbm_testing_neq(int lattice, const float* f, long long nodes, int dfloat,
+                                double* fneq) {
+  if (lattice < 0 || lattice > 2 || !f || !fneq || nodes <= 0) return MLBM_ERR_INVALID;
+  const int Q = lattice == 0 ? 9 : (lattice == 1 ? 19 : 27);
+  void *df = nullptr, *dn = nullptr;
+  if (cudaMalloc(&df, sizeof(float) * Q * nodes) != cudaSuccess ||
+      cudaMalloc(&dn, sizeof(double) * Q * nodes) != cudaSuccess) {
+    cudaFree(df); cudaFree(dn);
+    cudaGetLastError();
+    return fail(nullptr, MLBM_ERR_ALLOC, "testing buffers");
+  }
+  cudaError_t e = cudaMemcpy(df, f, sizeof(float) * Q * nodes, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = neq_test(lattice, (const float*)df, nodes, dfloat, (double*)dn, 0);
+  count_launches(1);
+  if (e == cudaSuccess) e = cudaDeviceSynchronize();
+  if (e == cudaSuccess) e = cudaMemcpy(fneq, dn, sizeof(double) * Q * nodes, cudaMemcpyDeviceToHost);
+  cudaFree(df); cudaFree(dn);
+  if (e != cudaSuccess) return fail(nullptr, MLBM_ERR_CUDA, "neq test: %s", cudaGetErrorString(e));
+  return MLBM_OK;
+}

@@ -54,6 +54,13 @@ cudaError_t entropy_test_L2(const float* f, const double* fneq, long long nodes,
                             int nx, int mode, const void* table, const void* table_fine, double* F, double* D,
                             int* series, cudaStream_t s);
 
+// f_neq as the FP32-storage entropic main pass forms it (tests).
+cudaError_t neq_test(int lattice, const float* f, long long nodes, int dfloat, double* out,
+                     cudaStream_t s);
+cudaError_t neq_test_L0(const float* f, long long nodes, int dfloat, double* out, cudaStream_t s);
+cudaError_t neq_test_L1(const float* f, long long nodes, int dfloat, double* out, cudaStream_t s);
+cudaError_t neq_test_L2(const float* f, long long nodes, int dfloat, double* out, cudaStream_t s);
+
 // Diagnostics: sum the per-block partials in a fixed order (deterministic).
 cudaError_t finalize_diag(const double* partials, int nblocks, double* out, cudaStream_t s);
 

@@ -81,6 +81,12 @@ cudaError_t entropy_test(int lattice, const float* f, const double* fneq, long l
               entropy_test_L2(f, fneq, nodes, x, nx, mode, table, table_fine, F, D, series, s))
 }
 
+cudaError_t neq_test(int lattice, const float* f, long long nodes, int dfloat, double* out,
+                     cudaStream_t s) {
+  MLBM_BY_LAT(lattice, neq_test_L0(f, nodes, dfloat, out, s), neq_test_L1(f, nodes, dfloat, out, s),
+              neq_test_L2(f, nodes, dfloat, out, s))
+}
+
 cudaError_t step_f64(int lattice, int collision, int forcing, const double* prev, double* next,
                      const StepParams& p, cudaStream_t s) {
   MLBM_BY_LAT(lattice, step_f64_L0(collision, forcing, prev, next, p, s),

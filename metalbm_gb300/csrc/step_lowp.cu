@@ -23,10 +23,17 @@
 #include "entropy.cuh"
 #include "fastlog.cuh"
 #include "solver.cuh"
+#include "dfloat.cuh"
 
 namespace mlbm {
 
 enum : int { ST_F32 = 1, ST_F16 = 2 };
+
+// f_neq of the FP32-storage entropic main pass in double-float arithmetic
+// (1) or in FP64 (0).
+#ifndef MLBM_NEQ_DFLOAT
+#define MLBM_NEQ_DFLOAT 1
+#endif
 
 template <int LAT>
 __host__ __device__ constexpr int shift_exponent(int q) {
@@ -626,11 +633,18 @@ __device__ __forceinline__ long long fixed64(double v) {
   return b < 0 ? -a : a;
 }
 
+// With f_neq from double-float arithmetic (FP32 storage), each f_neq_q is off
+// by at most 8 2^-48 rho w_q (1 + |P_q|) (eight roundings of 2^-48 on the
+// operands' scale), so sum_q |delta f_neq_q| <= 8 2^-48 1.6 rho; through
+// x (B1 + sum f_neq) with |ln(f/w)| <= 1: at most 2.5 x 2 x 4.6e-14 rho.
+constexpr float kNeqDflBound = 2.3e-13f;
+
 template <int LAT, int ST>
 __device__ __forceinline__ double series_error_bound(float rabs, double rho) {
   const float r = rabs, rf = narrow_rn(rho);
   const float m = r <= kSeriesTierA ? 6.0e-6f * r * r * r : 1.2e-5f * (r * r) * (r * r) * r;
-  return widen_exact(fmaf(rf, fmaf(6.0e-13f, r, m), 1.0e-15f));
+  const float dfl_term = (ST == ST_F32 && MLBM_NEQ_DFLOAT) ? kNeqDflBound : 0.0f;
+  return widen_exact(fmaf(rf, fmaf(6.0e-13f, r, m) + dfl_term, 1.0e-15f));
 }
 
 // B1 and the moments (series form), or r_q in place of f_neq_q in n[]
@@ -816,6 +830,59 @@ __device__ __forceinline__ void neq_pairs(const Pulled<LAT, ST>& P, double rho, 
   }
 }
 
+// f_neq in double-float arithmetic (dfloat.cuh) for FP32 storage: the same
+// pair form as neq_pairs, each operation on (hi, lo) float pairs, the result
+// rounded once to FP64. Error: a few 2^-48 of rho w_q (1 + |P_q|) a
+// population (bounded in series_error_bound), from ~20x fewer FP64-pipe
+// cycles than the FP64 form.
+template <int LAT>
+__device__ __forceinline__ void neq_pairs_dfl(const Pulled<LAT, ST_F32>& P, double rho,
+                                              const double u[3], double n[]) {
+  using L = Lattice<LAT>;
+  const dfl r = dfl_from(rho);
+  const dfl ux = dfl_from(u[0]), uy = dfl_from(u[1]), uz = dfl_from(u[2]);
+  const dfl uv[3] = {ux, uy, uz};
+  dfl u2 = dfl_mul(ux, ux);
+  if (L::D > 1) u2 = dfl_add(u2, dfl_mul(uy, uy));
+  if (L::D > 2) u2 = dfl_add(u2, dfl_mul(uz, uz));
+  const dfl common = dfl_mul(u2, dfl_add_f(dfl_mul_f(u2, 1.125f), -1.5f));
+  const dfl A = dfl_add_f(dfl_mul_f(u2, -6.75f), 4.5f);
+  const dfl B = dfl_add_f(dfl_mul_f(u2, -4.5f), 3.0f);
+  auto rw_of = [&](int q) {
+    const float wh = (float)L::w(q);
+    const float wl = (float)(L::w(q) - (double)wh);
+    return dfl_mul(r, dfl{wh, wl});
+  };
+  {
+    const dfl rw = rw_of(0);
+    const dfl feq = dfl_add(rw, dfl_mul(rw, common));
+    n[0] = dfl_to_double(dfl_add_f(dfl_neg(feq), P.v[0]));
+  }
+#pragma unroll
+  for (int q = 1; q < L::Q; ++q) {
+    if (is_pair_leader<LAT>(q)) {
+      const int qb = opposite<LAT>(q);
+      dfl cu{0.0f, 0.0f};
+      bool first = true;
+#pragma unroll
+      for (int k = 0; k < L::D; ++k) {
+        if (L::c(q, k) == 0) continue;
+        const dfl t = L::c(q, k) > 0 ? uv[k] : dfl_neg(uv[k]);
+        cu = first ? t : dfl_add(cu, t);
+        first = false;
+      }
+      const dfl c2 = dfl_mul(cu, cu);
+      const dfl E = dfl_add(dfl_mul(c2, dfl_add(dfl_mul_f(c2, 3.375f), A)), common);
+      const dfl O = dfl_mul(cu, dfl_add(dfl_mul_f(c2, 4.5f), B));
+      const dfl rw = rw_of(q);
+      const dfl A1 = dfl_add(rw, dfl_mul(rw, E));  // rho w (1 + E)
+      const dfl B1 = dfl_mul(rw, O);               // rho w O
+      n[q] = dfl_to_double(dfl_sub(dfl_add_f(dfl_neg(A1), P.v[q]), B1));
+      n[qb] = dfl_to_double(dfl_add(dfl_add_f(dfl_neg(A1), P.v[qb]), B1));
+    }
+  }
+}
+
 // The entropic step runs as two kernels. The main pass completes every node
 // whose deviations allow the moment-series entropy function (all of them on
 // resolved flows), the alpha = 2 shortcut and the alpha_max-limited nodes,
@@ -874,7 +941,8 @@ __device__ __forceinline__ void elbm_node(const typename Storage<ST>::T* __restr
 #pragma unroll
   for (int k = 0; k < 3; ++k) u[k] = j[k] * ir;
   double n[L::Q];
-  neq_pairs<LAT, ST>(P, rho, rhop, u, n);
+  if constexpr (MODE == ELBM_MAIN && ST == ST_F32 && MLBM_NEQ_DFLOAT) neq_pairs_dfl<LAT>(P, rho, u, n);
+  else neq_pairs<LAT, ST>(P, rho, rhop, u, n);
   // r_q = n_q / f_q in FP32 for the bracket and the tests
   float rpos = 0.0f, rabs = 0.0f;
 #pragma unroll
@@ -1116,6 +1184,29 @@ __global__ void entropy_test_kernel(const float* __restrict__ f, const double* _
   series_out[s] = series ? 1 : 0;
 }
 
+// f_neq of nodes given as FP32 populations [nodes][Q], as the FP32-storage
+// entropic main pass forms it (exact fixed-point moments, then double-float
+// or FP64 pair form), for accuracy tests.
+template <int LAT>
+__global__ void neq_test_kernel(const float* __restrict__ f, long long nodes, int dfloat,
+                                double* __restrict__ out) {
+  using L = Lattice<LAT>;
+  const long long s = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= nodes) return;
+  Pulled<LAT, ST_F32> P;
+#pragma unroll
+  for (int q = 0; q < L::Q; ++q) P.v[q] = f[s * L::Q + q];
+  double rho, rhop, j[3], u[3], n[L::Q];
+  moments_exact<LAT, ST_F32>(P, rho, rhop, j);
+  const double ir = recip_refined(rho, narrow_rn(rho));
+#pragma unroll
+  for (int k = 0; k < 3; ++k) u[k] = j[k] * ir;
+  if (dfloat) neq_pairs_dfl<LAT>(P, rho, u, n);
+  else neq_pairs<LAT, ST_F32>(P, rho, rhop, u, n);
+#pragma unroll
+  for (int q = 0; q < L::Q; ++q) out[s * L::Q + q] = n[q];
+}
+
 // ---- init and conversions ---------------------------------------------------
 // f_eq(rho, u) formed in FP64 with the TruncationMa3 polynomial in its pair form
 // (Equilibrium.h:17-33), rounded once into the storage format with integer
@@ -1266,6 +1357,12 @@ cudaError_t MLBM_FN(f64_to_lowp_L)(const double* in, int q, void* f, long long V
 }
 
 #if MLBM_ST == 1
+cudaError_t MLBM_CAT(neq_test_L, MLBM_LAT, , )(const float* f, long long nodes, int dfloat,
+                                              double* out, cudaStream_t s) {
+  neq_test_kernel<MLBM_LAT><<<(unsigned)((nodes + 127) / 128), 128, 0, s>>>(f, nodes, dfloat, out);
+  return cudaGetLastError();
+}
+
 cudaError_t MLBM_CAT(entropy_test_L, MLBM_LAT, , )(const float* f, const double* fneq, long long nodes,
                                                   const double* x, int nx, int mode,
                                                   const void* table, const void* table_fine,

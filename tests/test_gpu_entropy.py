@@ -126,3 +126,32 @@ def test_entropy_forms_match_definition(lattice):
     assert (np.abs(Fs - Fr[:small.size]) <= bound[:small.size]).all()
     # the bound stays a small part of the tolerance it is taken from
     assert series_bound(0.0125, 1.03) < 0.1e-12 and series_bound(0.0025, 1.03) < 0.1e-12
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("lattice", ["D3Q27", "D3Q19", "D2Q9"])
+def test_neq_double_float_within_bound(lattice):
+    """f_neq of the FP32 entropic main pass (exact fixed-point moments, then the
+    equilibrium in double-float arithmetic) against a long-double evaluation:
+    sum_q |delta f_neq_q| within the 8 2^-48 1.6 rho that its error bound
+    assumes, and the FP64 form within FP64 rounding."""
+    from metalbm_gb300 import capi
+    c, w = lattice_tables(lattice)
+    Q = w.size
+    rmax = np.geomspace(1e-5, 0.3, 3000)
+    f32, fneq_ref, wl = make_nodes(lattice, rmax, seed=7)
+    lib = capi.load()
+    fp, dp = ct.POINTER(ct.c_float), ct.POINTER(ct.c_double)
+    f32 = np.ascontiguousarray(f32)
+    out = {}
+    for mode in (0, 1):
+        n = np.empty((f32.shape[0], Q))
+        assert lib.mlbm_testing_neq({"D2Q9": 0, "D3Q19": 1, "D3Q27": 2}[lattice],
+                                    f32.ctypes.data_as(fp), f32.shape[0], mode,
+                                    n.ctypes.data_as(dp)) == 0
+        out[mode] = n
+    rho = f32.astype(np.float64).sum(1)
+    err_dfl = np.abs(out[1] - fneq_ref).sum(1)
+    err_f64 = np.abs(out[0] - fneq_ref).sum(1)
+    assert (err_dfl <= 8 * 2.0 ** -48 * 1.6 * rho).all(), (err_dfl / rho).max()
+    assert (err_f64 <= 64 * 2.0 ** -53 * rho).all(), (err_f64 / rho).max()
