@@ -42,7 +42,22 @@ enum {
 /* ---- template axes of the reference, as runtime enums -------------------
  * Names and order follow include/metaLBM/Options.h:12-43. */
 enum { MLBM_D2Q9 = 0, MLBM_D3Q19 = 1, MLBM_D3Q27 = 2 };             /* LatticeType */
-enum { MLBM_BGK = 0, MLBM_ELBM = 1, MLBM_FORCED_BNR_ELBM = 2 };     /* CollisionType */
+/* CollisionType (Options.h:33-36). Every entropic type from 2 on runs as
+ * MLBM_ELBM: in the reference they only redefine the non-virtual
+ * calculateAlpha, which ELBM::calculateRelaxationTime never reaches
+ * (Collision.h:227-241), so their populations equal ELBM's bit for bit.
+ * ForcedNR_ELBM_Forcing (subtracts f_eq from the pulled source in place) and
+ * GenericSRT / GenericMRT (abstract) have no value. */
+enum {
+  MLBM_BGK = 0,
+  MLBM_ELBM = 1,
+  MLBM_FORCED_BNR_ELBM = 2,
+  MLBM_APPROACHED_ELBM = 3,
+  MLBM_MALASPINAS_ELBM = 4,
+  MLBM_ESSENTIALLY1_ELBM = 5,
+  MLBM_ESSENTIALLY2_ELBM = 6,
+  MLBM_FORCED_NR_ELBM = 7
+};
 enum { MLBM_FORCING_NONE = 0, MLBM_FORCING_GUO = 1, MLBM_FORCING_SHAN_CHEN = 2,
        MLBM_FORCING_EXACT_DIFFERENCE = 3 };                         /* ForcingSchemeType */
 enum { MLBM_FORCE_NONE = 0, MLBM_FORCE_CONSTANT = 1, MLBM_FORCE_SINUSOIDAL = 2,

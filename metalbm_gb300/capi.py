@@ -16,6 +16,7 @@ OK, ERR_INVALID, ERR_CUDA, ERR_ALLOC, ERR_TIMEOUT, ERR_NUMERIC, ERR_STATE, ERR_N
 # enums (Options.h:12-43)
 D2Q9, D3Q19, D3Q27 = 0, 1, 2
 BGK, ELBM, FORCED_BNR_ELBM = 0, 1, 2
+APPROACHED_ELBM, MALASPINAS_ELBM, ESSENTIALLY1_ELBM, ESSENTIALLY2_ELBM, FORCED_NR_ELBM = range(3, 8)
 FORCING_NONE, FORCING_GUO, FORCING_SHAN_CHEN, FORCING_EXACT_DIFFERENCE = 0, 1, 2, 3
 FORCE_NONE, FORCE_CONSTANT, FORCE_SINUSOIDAL, FORCE_KOLMOGOROV = 0, 1, 2, 3
 STORAGE_F64, STORAGE_F32, STORAGE_F16_SHIFTED = 0, 1, 2

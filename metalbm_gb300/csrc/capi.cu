@@ -334,7 +334,7 @@ extern "C" int mlbm_create(const mlbm_config* cfg, mlbm_handle** out) {
   *out = nullptr;
   const mlbm_config& c = *cfg;
   if (c.lattice < 0 || c.lattice > 2) return fail(nullptr, MLBM_ERR_INVALID, "bad lattice %d", c.lattice);
-  if (c.collision < 0 || c.collision > 2)
+  if (c.collision < MLBM_BGK || c.collision > MLBM_FORCED_NR_ELBM)
     return fail(nullptr, MLBM_ERR_INVALID, "bad collision %d", c.collision);
   if (c.forcing_scheme < 0 || c.forcing_scheme > 3)
     return fail(nullptr, MLBM_ERR_INVALID, "bad forcing scheme %d", c.forcing_scheme);
@@ -372,7 +372,7 @@ extern "C" int mlbm_create(const mlbm_config* cfg, mlbm_handle** out) {
   mlbm_handle* h = new (std::nothrow) mlbm_handle();
   if (!h) return fail(nullptr, MLBM_ERR_ALLOC, "host allocation failed");
   h->cfg = c;
-  if (h->cfg.collision == MLBM_FORCED_BNR_ELBM) h->cfg.collision = MLBM_ELBM;
+  if (h->cfg.collision >= MLBM_FORCED_BNR_ELBM) h->cfg.collision = MLBM_ELBM;
   h->Q = kQ[c.lattice];
   h->D = D;
   h->lx = (uint32_t)L[0];

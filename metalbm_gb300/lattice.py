@@ -10,7 +10,18 @@ from . import capi
 from .capi import MlbmError
 
 _LATTICES = {"D2Q9": capi.D2Q9, "D3Q19": capi.D3Q19, "D3Q27": capi.D3Q27}
-_COLLISIONS = {"BGK": capi.BGK, "ELBM": capi.ELBM, "ForcedBNR_ELBM": capi.FORCED_BNR_ELBM}
+# The entropic variants other than ELBM run as ELBM, as they do in the
+# reference: their calculateAlpha overrides are never called from
+# ELBM::calculateRelaxationTime (Collision.h:227-241).
+_COLLISIONS = {"BGK": capi.BGK, "ELBM": capi.ELBM, "ForcedBNR_ELBM": capi.FORCED_BNR_ELBM,
+               "Approached_ELBM": capi.APPROACHED_ELBM, "Malaspinas_ELBM": capi.MALASPINAS_ELBM,
+               "Essentially1_ELBM": capi.ESSENTIALLY1_ELBM,
+               "Essentially2_ELBM": capi.ESSENTIALLY2_ELBM, "ForcedNR_ELBM": capi.FORCED_NR_ELBM}
+_UNSUPPORTED_COLLISIONS = {
+    "ForcedNR_ELBM_Forcing": "subtracts the equilibrium from the pulled source populations in "
+                             "place (Collision.h:757-775), so its result depends on the sweep "
+                             "order",
+    "GenericSRT": "abstract base of the SRT collisions", "GenericMRT": "abstract, no implementation"}
 _FORCINGS = {"None": capi.FORCING_NONE, "Guo": capi.FORCING_GUO,
              "ShanChen": capi.FORCING_SHAN_CHEN,
              "ExactDifferenceMethod": capi.FORCING_EXACT_DIFFERENCE}
@@ -71,6 +82,9 @@ class InputDeck:
         c = capi.Config()
         capi.load().mlbm_config_init(ct.byref(c))
         c.lattice = _LATTICES[self.latticeT]
+        if self.collisionT in _UNSUPPORTED_COLLISIONS:
+            raise ValueError(f"collisionT {self.collisionT!r} is not supported: "
+                             f"{_UNSUPPORTED_COLLISIONS[self.collisionT]}")
         c.collision = _COLLISIONS[self.collisionT]
         c.forcing_scheme = _FORCINGS[self.forcingSchemeT]
         c.force = _FORCES[self.forceT]

@@ -31,7 +31,7 @@ OUT = HERE / "_ref"
 @dataclass(frozen=True)
 class RefCase:
     lattice: str          # D2Q9 | D3Q19 | D3Q27
-    collision: str        # BGK | ELBM | ForcedBNR_ELBM
+    collision: str        # BGK | ELBM | ForcedBNR_ELBM | Approached_ELBM | ... (CollisionType)
     forcing: str          # None | Guo | ShanChen | ExactDifferenceMethod
     force: str            # None | Constant | Sinusoidal | Kolmogorov
     tau: float
@@ -77,6 +77,23 @@ CASES: dict[str, RefCase] = {
                                          (1.0, 1.0, 1.0), (12, 10, 8)),
     "d3q19_elbm_edm_constant": RefCase("D3Q19", "ELBM", "ExactDifferenceMethod", "Constant",
                                        0.53, (1e-4, -1e-4, 2e-4), (1.0, 1.0, 1.0), (8, 9, 10)),
+    # the other entropic collision types, same parameters as d3q27_elbm_none_none
+    # (they inherit ELBM::calculateRelaxationTime, Collision.h:227-241)
+    "d3q27_approached_none_none": RefCase("D3Q27", "Approached_ELBM", "None", "None",
+                                          0.500250125062531, (0.0, 0.0, 0.0),
+                                          (1.0, 1.0, 1.0), (12, 10, 8)),
+    "d3q27_malaspinas_none_none": RefCase("D3Q27", "Malaspinas_ELBM", "None", "None",
+                                          0.500250125062531, (0.0, 0.0, 0.0),
+                                          (1.0, 1.0, 1.0), (12, 10, 8)),
+    "d3q27_essentially1_none_none": RefCase("D3Q27", "Essentially1_ELBM", "None", "None",
+                                            0.500250125062531, (0.0, 0.0, 0.0),
+                                            (1.0, 1.0, 1.0), (12, 10, 8)),
+    "d3q27_essentially2_none_none": RefCase("D3Q27", "Essentially2_ELBM", "None", "None",
+                                            0.500250125062531, (0.0, 0.0, 0.0),
+                                            (1.0, 1.0, 1.0), (12, 10, 8)),
+    "d3q27_forcednr_none_none": RefCase("D3Q27", "ForcedNR_ELBM", "None", "None",
+                                        0.500250125062531, (0.0, 0.0, 0.0),
+                                        (1.0, 1.0, 1.0), (12, 10, 8)),
     # CPU-baseline timing cases (sizes of the benchmark workloads, run for a
     # bounded number of steps).
     "time_d3q19_bgk_guo_kolmogorov_128": RefCase("D3Q19", "BGK", "Guo", "Kolmogorov", 0.55,

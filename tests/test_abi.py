@@ -71,3 +71,28 @@ def test_create_reports_errors_without_aborting(lib):
     assert lib.mlbm_create(ct.byref(c), ct.byref(h)) == capi.ERR_INVALID
     assert b"relaxation time" in lib.mlbm_last_error(None)
     assert lib.mlbm_create(None, ct.byref(h)) == capi.ERR_INVALID
+
+
+def test_collision_enum_matches_header_and_deck(lib):
+    """Every entropic CollisionType of Options.h:33-36 that the reference can
+    run is accepted (they run as ELBM); an out-of-range code is rejected, and
+    the deck refuses ForcedNR_ELBM_Forcing with the reason."""
+    from metalbm_gb300 import capi
+    from metalbm_gb300.lattice import InputDeck
+    text = (ROOT / "include" / "mlbm" / "mlbm.h").read_text()
+    for name, value in [("BGK", 0), ("ELBM", 1), ("FORCED_BNR_ELBM", 2), ("APPROACHED_ELBM", 3),
+                        ("MALASPINAS_ELBM", 4), ("ESSENTIALLY1_ELBM", 5),
+                        ("ESSENTIALLY2_ELBM", 6), ("FORCED_NR_ELBM", 7)]:
+        assert re.search(rf"\bMLBM_{name} = {value}\b", text), name
+        assert getattr(capi, name) == value
+    for coll in ["ForcedBNR_ELBM", "Approached_ELBM", "Malaspinas_ELBM", "Essentially1_ELBM",
+                 "Essentially2_ELBM", "ForcedNR_ELBM"]:
+        assert InputDeck(latticeT="D3Q27", collisionT=coll).to_c().collision >= capi.ELBM
+    with pytest.raises(ValueError, match="sweep order"):
+        InputDeck(collisionT="ForcedNR_ELBM_Forcing").to_c()
+    c = capi.Config()
+    lib.mlbm_config_init(ct.byref(c))
+    c.collision = 8
+    h = ct.c_void_p()
+    assert lib.mlbm_create(ct.byref(c), ct.byref(h)) == capi.ERR_INVALID
+    assert b"collision" in lib.mlbm_last_error(None)
