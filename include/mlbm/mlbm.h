@@ -41,7 +41,16 @@ enum {
 
 /* ---- template axes of the reference, as runtime enums -------------------
  * Names and order follow include/metaLBM/Options.h:12-43. */
-enum { MLBM_D2Q9 = 0, MLBM_D3Q19 = 1, MLBM_D3Q27 = 2 };             /* LatticeType */
+/* LatticeType (Options.h:12-13). D3Q15, D2Q13 and D3Q33 run with FP64
+ * storage only; D2Q13 and D3Q33 reach two nodes (the reference's halo 2). */
+enum {
+  MLBM_D2Q9 = 0,
+  MLBM_D3Q19 = 1,
+  MLBM_D3Q27 = 2,
+  MLBM_D3Q15 = 3,
+  MLBM_D2Q13 = 4,
+  MLBM_D3Q33 = 5
+};
 /* CollisionType (Options.h:33-36). Every entropic type from 2 on runs as
  * MLBM_ELBM: in the reference they only redefine the non-virtual
  * calculateAlpha, which ELBM::calculateRelaxationTime never reaches

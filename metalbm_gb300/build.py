@@ -37,7 +37,7 @@ def units() -> list[tuple[Path, list[str], str]]:
     for src in sorted(CSRC.glob("*.cu")):
         extra = PER_FILE.get(src.name, [])
         if src.name == "step_f64.cu":
-            out += [(src, extra + [f"-DMLBM_LAT={l}"], f"{src.stem}_L{l}") for l in range(3)]
+            out += [(src, extra + [f"-DMLBM_LAT={l}"], f"{src.stem}_L{l}") for l in range(6)]
         elif src.name == "step_lowp.cu":
             out += [(src, extra + [f"-DMLBM_LAT={l}", f"-DMLBM_ST={st}"], f"{src.stem}_L{l}_S{st}")
                     for l in range(3) for st in (1, 2)]

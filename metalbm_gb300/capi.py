@@ -14,7 +14,7 @@ LIB_PATH = Path(__file__).resolve().parent / "libmlbm.so"
 # status codes
 OK, ERR_INVALID, ERR_CUDA, ERR_ALLOC, ERR_TIMEOUT, ERR_NUMERIC, ERR_STATE, ERR_NO_DEVICE = range(8)
 # enums (Options.h:12-43)
-D2Q9, D3Q19, D3Q27 = 0, 1, 2
+D2Q9, D3Q19, D3Q27, D3Q15, D2Q13, D3Q33 = 0, 1, 2, 3, 4, 5
 BGK, ELBM, FORCED_BNR_ELBM = 0, 1, 2
 APPROACHED_ELBM, MALASPINAS_ELBM, ESSENTIALLY1_ELBM, ESSENTIALLY2_ELBM, FORCED_NR_ELBM = range(3, 8)
 FORCING_NONE, FORCING_GUO, FORCING_SHAN_CHEN, FORCING_EXACT_DIFFERENCE = 0, 1, 2, 3

@@ -5,7 +5,7 @@
 // reference's padded FieldList layout, f = f_eq(rho, u), `steps` iterations
 // with isStored on the last one, then pack and storeFields.
 //
-// Usage: routine_gpu <in.bin> <out.bin> <steps> <lattice 0|1|2> <collision 0|1|2>
+// Usage: routine_gpu <in.bin> <out.bin> <steps> <lattice 0..5> <collision 0..7>
 //                    <forcing 0..3> <force 0..3> <tau> <ax> <ay> <az> <lx> <ly> <lz>
 //                    <Lx> <Ly> <Lz>
 //   in.bin : float64 rho[V], u[D][V] dense (index (x*Ly+y)*Lz+z)
@@ -34,8 +34,13 @@ int main(int argc, char** argv) {
     cfg.force_wavelength[d] = std::atof(argv[12 + d]);
     cfg.length[d] = std::atoi(argv[15 + d]);
   }
-  const int Q = cfg.lattice == MLBM_D2Q9 ? 9 : (cfg.lattice == MLBM_D3Q19 ? 19 : 27);
-  const int D = cfg.lattice == MLBM_D2Q9 ? 2 : 3;
+  if (cfg.lattice < MLBM_D2Q9 || cfg.lattice > MLBM_D3Q33) {
+    std::fprintf(stderr, "bad lattice %d\n", cfg.lattice);
+    return 2;
+  }
+  static const int kQ[6] = {9, 19, 27, 15, 13, 33};
+  const int Q = kQ[cfg.lattice];
+  const int D = (cfg.lattice == MLBM_D2Q9 || cfg.lattice == MLBM_D2Q13) ? 2 : 3;
   const long lx = cfg.length[0], ly = cfg.length[1], lz = D == 2 ? 1 : cfg.length[2];
   const long V = lx * ly * lz;
   // reference local layout: last active dimension padded to 2*(N/2+1)

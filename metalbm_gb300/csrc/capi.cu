@@ -37,8 +37,8 @@ std::atomic<unsigned long long> g_launches{0};
 std::mutex g_create_error_mutex;
 std::string g_create_error;
 
-const int kQ[3] = {9, 19, 27};
-const int kD[3] = {2, 3, 3};
+const int kQ[6] = {9, 19, 27, 15, 13, 33};
+const int kD[6] = {2, 3, 3, 3, 2, 3};
 const double kPi = 3.14159265358979323846;
 
 }  // namespace
@@ -251,27 +251,25 @@ static void release(mlbm_handle* h) {
 // Table of the FP64 logarithm (fastlog.cuh): for the centre c_j of each of
 // the 128 mantissa intervals, inv_j = RN(1/c_j) and -ln(inv_j) split into a
 // double-double, evaluated in the host's extended precision.
-// Lattice weights in the reference's population order (Lattice.h:145-210,
-// 535-612, 614-703).
-static const double* lattice_weights(int lattice) {
-  static const double w9[9] = {4.0 / 9.0, 1.0 / 36.0, 1.0 / 9.0, 1.0 / 36.0, 1.0 / 36.0,
-                               1.0 / 9.0, 1.0 / 36.0, 1.0 / 9.0, 1.0 / 9.0};
-  static const double w19[19] = {1.0 / 3.0,  1.0 / 18.0, 1.0 / 36.0, 1.0 / 36.0, 1.0 / 36.0,
-                                 1.0 / 36.0, 1.0 / 18.0, 1.0 / 36.0, 1.0 / 36.0, 1.0 / 36.0,
-                                 1.0 / 36.0, 1.0 / 18.0, 1.0 / 18.0, 1.0 / 36.0, 1.0 / 36.0,
-                                 1.0 / 18.0, 1.0 / 18.0, 1.0 / 36.0, 1.0 / 36.0};
-  static double w27[27];
-  static std::once_flag once;
-  std::call_once(once, [] {
-    const double v[4] = {8.0 / 27.0, 2.0 / 27.0, 1.0 / 54.0, 1.0 / 216.0};
-    for (int q = 0; q < 27; ++q) {
-      const int cls = (q == 0) ? 0 : ((q == 1 || q == 10 || q == 19 || q == 20 || q == 23 || q == 24) ? 1
-                        : ((q >= 6 && q <= 9) || (q >= 15 && q <= 18)) ? 3 : 2);
-      w27[q] = v[cls];
-    }
-  });
-  return lattice == MLBM_D2Q9 ? w9 : (lattice == MLBM_D3Q19 ? w19 : w27);
+// Host copy of a lattice's weights (reference population order) and
+// inv_cs2, from the same compile-time tables the kernels use (lattice.cuh).
+struct HostLattice {
+  double w[kMaxQ];
+  double ics;
+};
+template <int LAT>
+static HostLattice host_lattice_of() {
+  HostLattice h{};
+  for (int q = 0; q < Lattice<LAT>::Q; ++q) h.w[q] = Lattice<LAT>::w(q);
+  h.ics = Lattice<LAT>::ics;
+  return h;
 }
+static const HostLattice& host_lattice(int lattice) {
+  static const HostLattice t[6] = {host_lattice_of<0>(), host_lattice_of<1>(), host_lattice_of<2>(),
+                                   host_lattice_of<3>(), host_lattice_of<4>(), host_lattice_of<5>()};
+  return t[lattice];
+}
+static const double* lattice_weights(int lattice) { return host_lattice(lattice).w; }
 
 // Fine log table (1024 x {RN(1/c_j), RN(ln(1/inv_j))}) followed by the
 // lattice's constants C_q(d) = d ln 2 - ln(m_q), w_q = m_q 2^e_q.
@@ -287,7 +285,7 @@ static void make_log_table_fine(FineTable* ft, int lattice) {
     ft->t[j].hi = (double)(-std::log((long double)inv));
   }
   const double* wl = lattice_weights(lattice);
-  const int Q = lattice == MLBM_D2Q9 ? 9 : (lattice == MLBM_D3Q19 ? 19 : 27);
+  const int Q = kQ[lattice];
   for (int q = 0; q < 27; ++q) {
     const double wq = q < Q ? wl[q] : 1.0;
     int ew = 0;
@@ -333,13 +331,17 @@ extern "C" int mlbm_create(const mlbm_config* cfg, mlbm_handle** out) {
   if (!cfg || !out) return fail(nullptr, MLBM_ERR_INVALID, "null argument");
   *out = nullptr;
   const mlbm_config& c = *cfg;
-  if (c.lattice < 0 || c.lattice > 2) return fail(nullptr, MLBM_ERR_INVALID, "bad lattice %d", c.lattice);
+  if (c.lattice < 0 || c.lattice > MLBM_D3Q33) return fail(nullptr, MLBM_ERR_INVALID, "bad lattice %d", c.lattice);
   if (c.collision < MLBM_BGK || c.collision > MLBM_FORCED_NR_ELBM)
     return fail(nullptr, MLBM_ERR_INVALID, "bad collision %d", c.collision);
   if (c.forcing_scheme < 0 || c.forcing_scheme > 3)
     return fail(nullptr, MLBM_ERR_INVALID, "bad forcing scheme %d", c.forcing_scheme);
   if (c.force < 0 || c.force > 3) return fail(nullptr, MLBM_ERR_INVALID, "bad force %d", c.force);
   if (c.storage < 0 || c.storage > 2) return fail(nullptr, MLBM_ERR_INVALID, "bad storage %d", c.storage);
+  if (c.storage != MLBM_STORAGE_F64 && c.lattice > MLBM_D3Q27)
+    return fail(nullptr, MLBM_ERR_INVALID,
+                "FP32 / FP16 storage supports D2Q9, D3Q19 and D3Q27; lattice %d runs with FP64 storage",
+                c.lattice);
   if (!(c.relaxation_time > 0.5) || !std::isfinite(c.relaxation_time))
     return fail(nullptr, MLBM_ERR_INVALID, "relaxation time must be > 0.5 (got %g)", c.relaxation_time);
   if (c.alpha_mode < 0 || c.alpha_mode > 1) return fail(nullptr, MLBM_ERR_INVALID, "bad alpha mode");
@@ -496,23 +498,9 @@ extern "C" int mlbm_create(const mlbm_config* cfg, mlbm_handle** out) {
   p.bgk_a = 1. - 2. * p.beta;                            // Collision.h:145
   p.bgk_b = 2. * p.beta;                                 // Collision.h:147
   {
-    double w[27];
-    const double* wl = nullptr;
-    static const double w9[9] = {4.0 / 9.0, 1.0 / 36.0, 1.0 / 9.0, 1.0 / 36.0, 1.0 / 36.0,
-                                 1.0 / 9.0, 1.0 / 36.0, 1.0 / 9.0, 1.0 / 9.0};
-    static const double w19[19] = {1.0 / 3.0,  1.0 / 18.0, 1.0 / 36.0, 1.0 / 36.0, 1.0 / 36.0,
-                                   1.0 / 36.0, 1.0 / 18.0, 1.0 / 36.0, 1.0 / 36.0, 1.0 / 36.0,
-                                   1.0 / 36.0, 1.0 / 18.0, 1.0 / 18.0, 1.0 / 36.0, 1.0 / 36.0,
-                                   1.0 / 18.0, 1.0 / 18.0, 1.0 / 36.0, 1.0 / 36.0};
-    for (int q = 0; q < 27; ++q) {
-      const int cls = (q == 0) ? 0 : ((q == 1 || q == 10 || q == 19 || q == 20 || q == 23 || q == 24) ? 1
-                        : ((q >= 6 && q <= 9) || (q >= 15 && q <= 18)) ? 3 : 2);
-      const double v[4] = {8.0 / 27.0, 2.0 / 27.0, 1.0 / 54.0, 1.0 / 216.0};
-      w[q] = v[cls];
-    }
-    wl = c.lattice == MLBM_D2Q9 ? w9 : (c.lattice == MLBM_D3Q19 ? w19 : w);
+    const HostLattice& hl = host_lattice(c.lattice);
     for (int q = 0; q < h->Q; ++q)  // ForcingScheme.h:115-116
-      p.guo_k[q] = (1.0 - 1.0 / (2.0 * c.relaxation_time)) * wl[q] * 3.0;
+      p.guo_k[q] = (1.0 - 1.0 / (2.0 * c.relaxation_time)) * hl.w[q] * hl.ics;
   }
   p.force_type = c.force;
   p.kol_axis = c.kolmogorov_axis;

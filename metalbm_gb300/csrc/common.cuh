@@ -41,7 +41,7 @@ struct StepParams {
   // relaxation
   double tau, beta;
   double bgk_a, bgk_b;       // (1 - 2 beta), 2 beta  (Collision.h:145-149)
-  double guo_k[27];          // ((1 - 1/(2 tau)) w_q) 3  (ForcingScheme.h:115-116)
+  double guo_k[kMaxQ];       // ((1 - 1/(2 tau)) w_q) inv_cs2  (ForcingScheme.h:115-116)
   // force
   int force_type;
   int kol_axis, kol_comp;
@@ -90,17 +90,20 @@ constexpr int DIAG_FIELDS = 5;
 
 // Source node of the pulled population with velocity (cx, cy, cz): periodic
 // neighbour offsets along each axis, formed once per node.
-struct PullOffsets {
+template <int R>
+struct PullOffsetsR {
   // node-index offsets within one population array (V < 2^31): 32-bit, so a
   // source address is one 32-bit three-input add and one wide multiply-add
-  // onto the population's base pointer
-  uint32_t ox[3];  // index 0: c = -1 (reads x+1), 1: c = 0, 2: c = +1 (reads x-1)
-  uint32_t oy[3];
-  uint32_t oz[3];
+  // onto the population's base pointer. Index c + R holds the offset of the
+  // node x - c (periodic) for a velocity component c in [-R, R].
+  uint32_t ox[2 * R + 1];
+  uint32_t oy[2 * R + 1];
+  uint32_t oz[2 * R + 1];
   __device__ __forceinline__ uint32_t at(int cx, int cy, int cz) const {
-    return ox[cx + 1] + oy[cy + 1] + oz[cz + 1];
+    return ox[cx + R] + oy[cy + R] + oz[cz + R];
   }
 };
+using PullOffsets = PullOffsetsR<1>;
 
 // Base of population q's array (uniform across the grid) indexed with a
 // 32-bit node index.
@@ -129,6 +132,28 @@ __device__ __forceinline__ PullOffsets pull_offsets(const StepParams& p, uint32_
   o.oy[0] = yp * p.lz; o.oy[1] = y * p.lz; o.oy[2] = ym * p.lz;
   o.oz[0] = zp; o.oz[1] = z; o.oz[2] = zm;
   return o;
+}
+
+// Offsets for lattices that reach R > 1 nodes (D2Q13, D3Q33; the reference's
+// halo of width R, Lattice.h:225-228, 719-722): (x - c) mod L by integer
+// division, valid for any length >= 1. Those lattices run only in the FP64
+// kernels, where the divisions are a small share of the node's work.
+template <int R>
+__device__ __forceinline__ PullOffsetsR<R> pull_offsets_r(const StepParams& p, uint32_t x,
+                                                        uint32_t y, uint32_t z) {
+  if constexpr (R == 1) {
+    return pull_offsets(p, x, y, z);
+  } else {
+    PullOffsetsR<R> o;
+    const uint32_t sx = p.ly * p.lz;
+#pragma unroll
+    for (int c = -R; c <= R; ++c) {
+      o.ox[c + R] = ((x + R * p.lx - c) % p.lx) * sx;
+      o.oy[c + R] = ((y + R * p.ly - c) % p.ly) * p.lz;
+      o.oz[c + R] = (z + R * p.lz - c) % p.lz;
+    }
+    return o;
+  }
 }
 
 // Per-node body force (Force.h:137-292). The sine profiles are tabulated on

@@ -67,6 +67,13 @@ cudaError_t finalize_diag(const double* partials, int nblocks, double* out, cuda
 #define MLBM_BY_LAT(L, CALL0, CALL1, CALL2) \
   switch (L) { case 0: return CALL0; case 1: return CALL1; case 2: return CALL2; } \
   return cudaErrorInvalidValue;
+// the FP64 units exist for all six lattices (0..5)
+#define MLBM_BY_LAT6(L, F, ARGS) \
+  switch (L) { \
+    case 0: return F##_L0 ARGS; case 1: return F##_L1 ARGS; case 2: return F##_L2 ARGS; \
+    case 3: return F##_L3 ARGS; case 4: return F##_L4 ARGS; case 5: return F##_L5 ARGS; \
+  } \
+  return cudaErrorInvalidValue;
 #define MLBM_BY_LAT_ST(L, S, F, ARGS) \
   if (S == 1) { MLBM_BY_LAT(L, F##_L0_S1 ARGS, F##_L1_S1 ARGS, F##_L2_S1 ARGS) } \
   if (S == 2) { MLBM_BY_LAT(L, F##_L0_S2 ARGS, F##_L1_S2 ARGS, F##_L2_S2 ARGS) } \
@@ -89,15 +96,12 @@ cudaError_t neq_test(int lattice, const float* f, long long nodes, int dfloat, d
 
 cudaError_t step_f64(int lattice, int collision, int forcing, const double* prev, double* next,
                      const StepParams& p, cudaStream_t s) {
-  MLBM_BY_LAT(lattice, step_f64_L0(collision, forcing, prev, next, p, s),
-              step_f64_L1(collision, forcing, prev, next, p, s),
-              step_f64_L2(collision, forcing, prev, next, p, s))
+  MLBM_BY_LAT6(lattice, step_f64, (collision, forcing, prev, next, p, s))
 }
 
 cudaError_t init_f64(int lattice, const double* rho, const double* u, double* f, long long V,
                      cudaStream_t s) {
-  MLBM_BY_LAT(lattice, init_f64_L0(rho, u, f, V, s), init_f64_L1(rho, u, f, V, s),
-              init_f64_L2(rho, u, f, V, s))
+  MLBM_BY_LAT6(lattice, init_f64, (rho, u, f, V, s))
 }
 
 cudaError_t step_lowp(int lattice, int collision, int forcing, int storage, const void* prev,
@@ -124,10 +128,8 @@ cudaError_t log_samples(int lattice, int storage, const void* prev, const StepPa
                         const long long* nodes, long long n, double* features, double* alpha,
                         int* solved, cudaStream_t s) {
   if (storage == 0) {
-    MLBM_BY_LAT(lattice,
-                log_samples_f64_L0((const double*)prev, p, nodes, n, features, alpha, solved, s),
-                log_samples_f64_L1((const double*)prev, p, nodes, n, features, alpha, solved, s),
-                log_samples_f64_L2((const double*)prev, p, nodes, n, features, alpha, solved, s))
+    MLBM_BY_LAT6(lattice, log_samples_f64,
+                 ((const double*)prev, p, nodes, n, features, alpha, solved, s))
   }
   MLBM_BY_LAT_ST(lattice, storage, log_samples_lowp,
                  (prev, p, nodes, n, features, alpha, solved, s))

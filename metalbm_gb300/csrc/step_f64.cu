@@ -31,7 +31,8 @@ __device__ __forceinline__ double cdot(int q, const double v[3]) {
   for (int d = 0; d < L::D; ++d) {
     const int c = L::c(q, d);
     if (c != 0) {
-      const double t = c > 0 ? v[d] : -v[d];
+      // c v with c = +-1 is a sign change, with c = +-2 an exact doubling
+      const double t = c == 1 ? v[d] : (c == -1 ? -v[d] : (double)c * v[d]);
       r = any ? r + t : t;
       any = true;
     }
@@ -43,28 +44,33 @@ __device__ __forceinline__ double cdot(int q, const double v[3]) {
 struct EqNode {
   double rho, u2, t2, t6;
 };
+template <int LAT>
 __device__ __forceinline__ EqNode eq_node(double rho, double u2) {
+  using K = EqConst<LAT>;
   EqNode e;
   e.rho = rho;
   e.u2 = u2;
-  e.t2 = 0.5 * u2 * 3.0;
-  e.t6 = 0.125 * u2 * u2 * 9.0;
+  e.t2 = 0.5 * u2 * K::ics;
+  e.t6 = 0.125 * u2 * u2 * K::p2;
   return e;
 }
 
-// Equilibrium of the pair (q, -q) from cu = c_q . u:
-//   fEq = 1 + 3cu - 1.5u2 + 4.5cu^2 - 4.5cu u2 + 4.5cu^3 + 1.125u2^2
-//         - 6.75cu^2 u2 + 3.375cu^4, each term as the reference forms it.
+// Equilibrium of the pair (q, -q) from cu = c_q . u, with k = inv_cs2:
+//   fEq = 1 + k cu - k/2 u2 + k^2/2 cu^2 - k^2/2 cu u2 + k^3/6 cu^3
+//         + k^2/8 u2^2 - k^3/4 cu^2 u2 + k^4/24 cu^4,
+// each term as the reference forms it (k = 3: 4.5, 27/6, 6.75, 81/24).
+template <int LAT>
 __device__ __forceinline__ void eq_pair(const EqNode& e, double cu, double rw_plus,
                                         double rw_minus, double& feq_plus, double& feq_minus) {
-  const double t1 = cu * 3.0;
-  const double a = 4.5 * cu;
+  using K = EqConst<LAT>;
+  const double t1 = cu * K::ics;
+  const double a = K::half_p2 * cu;
   const double t3 = a * cu;
   const double t4 = a * e.u2;
   const double c3 = cu * cu * cu;
-  const double t5 = c3 * 27.0 / 6.0;
-  const double t7 = 0.25 * cu * cu * e.u2 * 27.0;
-  const double t8 = c3 * cu * 81.0 / 24.0;
+  const double t5 = c3 * K::p3 / 6.0;
+  const double t7 = 0.25 * cu * cu * e.u2 * K::p3;
+  const double t8 = c3 * cu * K::p4 / 24.0;
   const double sp = 1.0 + t1 - e.t2 + t3 - t4 + t5 + e.t6 - t7 + t8;
   const double sm = 1.0 - t1 - e.t2 + t3 + t4 - t5 + e.t6 - t7 + t8;
   feq_plus = rw_plus * sp;
@@ -80,13 +86,13 @@ template <int LAT>
 __device__ __forceinline__ void equilibria(double rho, const double u[3], double u2,
                                            double feq[Lattice<LAT>::Q]) {
   using L = Lattice<LAT>;
-  const EqNode e = eq_node(rho, u2);
+  const EqNode e = eq_node<LAT>(rho, u2);
   feq[0] = eq_rest(e, rho * L::w(0));
 #pragma unroll
   for (int q = 1; q < L::Q; ++q) {
     if (is_pair_leader<LAT>(q)) {
       const int qb = opposite<LAT>(q);
-      eq_pair(e, cdot<LAT>(q, u), rho * L::w(q), rho * L::w(qb), feq[q], feq[qb]);
+      eq_pair<LAT>(e, cdot<LAT>(q, u), rho * L::w(q), rho * L::w(qb), feq[q], feq[qb]);
     }
   }
 }
@@ -98,13 +104,14 @@ __device__ __forceinline__ double source(const StepParams& p, int q, double rho,
                                          const double* feq_shift) {
   using L = Lattice<LAT>;
   if (FS == FS_GUO) {
-    // ((c - u) + c (3 c.u)) . F, then ((1 - 1/(2 tau)) w) 3 * R
+    // ((c - u) + (inv_cs2 c.u) c) . F, then ((1 - 1/(2 tau)) w) inv_cs2 * R;
+    // cu3 = inv_cs2 c.u, and (cu3) c is exact for c = +-1, +-2
     double v[3];
 #pragma unroll
     for (int d = 0; d < L::D; ++d) {
       const int c = L::c(q, d);
-      const double cmu = c > 0 ? 1.0 - u[d] : (c < 0 ? -1.0 - u[d] : -u[d]);
-      v[d] = c == 0 ? cmu : cmu + (c > 0 ? cu3 : -cu3);
+      const double cmu = c == 0 ? -u[d] : (double)c - u[d];
+      v[d] = c == 0 ? cmu : cmu + (c == 1 ? cu3 : (c == -1 ? -cu3 : (double)c * cu3));
     }
     double R = v[0] * F[0];
 #pragma unroll
@@ -118,7 +125,8 @@ __device__ __forceinline__ double source(const StepParams& p, int q, double rho,
 
 template <int LAT>
 __device__ __forceinline__ void pull(const double* __restrict__ prev, long long V,
-                                     const PullOffsets& o, double f[Lattice<LAT>::Q]) {
+                                     const PullOffsetsR<Lattice<LAT>::R>& o,
+                                     double f[Lattice<LAT>::Q]) {
   using L = Lattice<LAT>;
 #pragma unroll
   for (int q = 0; q < L::Q; ++q)
@@ -143,7 +151,7 @@ __device__ __forceinline__ void moments(const double f[Lattice<LAT>::Q], double&
     for (int q = 1; q < L::Q; ++q) {
       const int c = L::c(q, d);
       if (c != 0) {
-        const double t = c > 0 ? f[q] : -f[q];
+        const double t = c == 1 ? f[q] : (c == -1 ? -f[q] : (double)c * f[q]);
         s = any ? s + t : t;
         any = true;
       }
@@ -195,7 +203,7 @@ __device__ __forceinline__ void store_node_fields(const StepParams& p, long long
     energy = 0.0;
 #pragma unroll
     for (int d = 0; d < L::D; ++d) energy = energy + 0.5 * rho * uh[d] * uh[d];
-    mach = 3.0 * norm2<LAT>(uh);  // |u|^2 / c_s^2; the square root is taken once, in finalize_diag
+    mach = L::ics * norm2<LAT>(uh);  // |u|^2 / c_s^2; the square root is taken once, in finalize_diag
   }
 }
 
@@ -210,7 +218,7 @@ __global__ void __launch_bounds__(256) bgk_f64_kernel(const double* __restrict__
   if (active) {
     uint32_t x, y, z;
     node_coords(p, idx, x, y, z);
-    const PullOffsets o = pull_offsets(p, x, y, z);
+    const auto o = pull_offsets_r<L::R>(p, x, y, z);
     double f[L::Q];
     pull<LAT>(prev, p.V, o, f);
     double rho, u[3];
@@ -224,7 +232,7 @@ __global__ void __launch_bounds__(256) bgk_f64_kernel(const double* __restrict__
     shifted_equilibria<LAT, FS>(rho, u, F, fsh);
 #pragma unroll
     for (int q = 0; q < L::Q; ++q) {
-      const double cu3 = cdot<LAT>(q, u) * 3.0;
+      const double cu3 = cdot<LAT>(q, u) * L::ics;
       double r = p.bgk_a * f[q] + p.bgk_b * feq[q];
       if (FS == FS_GUO || FS == FS_EDM) r = r + source<LAT, FS>(p, q, rho, u, F, cu3, feq[q], fsh);
       pop(next, p.V, q)[(uint32_t)idx] = r;
@@ -319,7 +327,7 @@ __global__ void __launch_bounds__(128) elbm_f64_kernel(const double* __restrict_
   if (active) {
     uint32_t x, y, z;
     node_coords(p, idx, x, y, z);
-    const PullOffsets o = pull_offsets(p, x, y, z);
+    const auto o = pull_offsets_r<L::R>(p, x, y, z);
     double f[L::Q];
     pull<LAT>(prev, p.V, o, f);
     double rho, u[3];
@@ -342,7 +350,7 @@ __global__ void __launch_bounds__(128) elbm_f64_kernel(const double* __restrict_
       const double eqq = f[q] - fneq[q];
       double r = f[q] - inv * fneq[q];
       if (FS == FS_GUO || FS == FS_EDM)
-        r = r + source<LAT, FS>(p, q, rho, u, F, cdot<LAT>(q, u) * 3.0, eqq, fsh);
+        r = r + source<LAT, FS>(p, q, rho, u, F, cdot<LAT>(q, u) * L::ics, eqq, fsh);
       pop(next, p.V, q)[(uint32_t)idx] = r;
     }
     p.alpha_field[idx] = alpha;
@@ -385,7 +393,7 @@ __global__ void samples_f64_kernel(const double* __restrict__ prev, StepParams p
   const long long idx = nodes[s];
   uint32_t x, y, z;
   node_coords(p, idx, x, y, z);
-  const PullOffsets o = pull_offsets(p, x, y, z);
+  const auto o = pull_offsets_r<L::R>(p, x, y, z);
   double f[L::Q], rho, u[3], fneq[L::Q];
   pull<LAT>(prev, p.V, o, f);
   moments<LAT>(f, rho, u);
@@ -443,10 +451,10 @@ static cudaError_t dispatch_fs(int collision, int fs, const double* prev, double
   return cudaErrorInvalidValue;
 }
 
-// This file is compiled once per lattice (MLBM_LAT = 0, 1, 2) so the three
-// sets of kernels build in parallel; misc.cu dispatches on the lattice.
+// This file is compiled once per lattice (MLBM_LAT = 0..5) so the six sets
+// of kernels build in parallel; misc.cu dispatches on the lattice.
 #ifndef MLBM_LAT
-#error "compile step_f64.cu with -DMLBM_LAT=<0|1|2>"
+#error "compile step_f64.cu with -DMLBM_LAT=<0..5>"
 #endif
 #define MLBM_CAT2(a, b) a##b
 #define MLBM_CAT(a, b) MLBM_CAT2(a, b)

@@ -9,7 +9,8 @@ import numpy as np
 from . import capi
 from .capi import MlbmError
 
-_LATTICES = {"D2Q9": capi.D2Q9, "D3Q19": capi.D3Q19, "D3Q27": capi.D3Q27}
+_LATTICES = {"D2Q9": capi.D2Q9, "D3Q19": capi.D3Q19, "D3Q27": capi.D3Q27,
+             "D3Q15": capi.D3Q15, "D2Q13": capi.D2Q13, "D3Q33": capi.D3Q33}
 # The entropic variants other than ELBM run as ELBM, as they do in the
 # reference: their calculateAlpha overrides are never called from
 # ELBM::calculateRelaxationTime (Collision.h:227-241).
@@ -31,8 +32,8 @@ _STORAGES = {"f64": capi.STORAGE_F64, "f32": capi.STORAGE_F32,
              "f16_shifted": capi.STORAGE_F16_SHIFTED}
 _ALPHA = {"reference": capi.ALPHA_REFERENCE, "residual": capi.ALPHA_RESIDUAL}
 _GUESS = {"previous": capi.GUESS_PREVIOUS, "two": capi.GUESS_TWO, "learned": capi.GUESS_LEARNED}
-Q_OF = {"D2Q9": 9, "D3Q19": 19, "D3Q27": 27}
-D_OF = {"D2Q9": 2, "D3Q19": 3, "D3Q27": 3}
+Q_OF = {"D2Q9": 9, "D3Q19": 19, "D3Q27": 27, "D3Q15": 15, "D2Q13": 13, "D3Q33": 33}
+D_OF = {"D2Q9": 2, "D3Q19": 3, "D3Q27": 3, "D3Q15": 3, "D2Q13": 2, "D3Q33": 3}
 
 
 @dataclass

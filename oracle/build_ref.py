@@ -30,7 +30,7 @@ OUT = HERE / "_ref"
 
 @dataclass(frozen=True)
 class RefCase:
-    lattice: str          # D2Q9 | D3Q19 | D3Q27
+    lattice: str          # D2Q9 | D3Q19 | D3Q27 | D3Q15 | D2Q13 | D3Q33
     collision: str        # BGK | ELBM | ForcedBNR_ELBM | Approached_ELBM | ... (CollisionType)
     forcing: str          # None | Guo | ShanChen | ExactDifferenceMethod
     force: str            # None | Constant | Sinusoidal | Kolmogorov
@@ -94,6 +94,28 @@ CASES: dict[str, RefCase] = {
     "d3q27_forcednr_none_none": RefCase("D3Q27", "ForcedNR_ELBM", "None", "None",
                                         0.500250125062531, (0.0, 0.0, 0.0),
                                         (1.0, 1.0, 1.0), (12, 10, 8)),
+    # the other lattices of Lattice.h:213-533, 706-802 (D2Q13 and D3Q33 reach
+    # two nodes away: halo 2)
+    "d3q15_bgk_guo_kolmogorov": RefCase("D3Q15", "BGK", "Guo", "Kolmogorov", 0.57,
+                                        (1e-3, 0.0, 0.0), (5.0, 1.0, 1.0), (12, 10, 8)),
+    "d3q15_bgk_shanchen_constant": RefCase("D3Q15", "BGK", "ShanChen", "Constant", 0.7,
+                                           (2e-4, -1e-4, 1e-4), (1.0, 1.0, 1.0), (9, 8, 10)),
+    "d3q15_elbm_edm_sinusoidal": RefCase("D3Q15", "ELBM", "ExactDifferenceMethod", "Sinusoidal",
+                                         0.51, (1e-4, -2e-4, 1e-4), (6.0, 5.0, 7.0), (10, 9, 8)),
+    "d2q13_bgk_none_none": RefCase("D2Q13", "BGK", "None", "None", 0.8, (0.0, 0.0, 0.0),
+                                   (1.0, 1.0, 1.0), (16, 20, 1)),
+    "d2q13_bgk_guo_kolmogorov": RefCase("D2Q13", "BGK", "Guo", "Kolmogorov", 0.6,
+                                        (1e-3, 0.0, 0.0), (6.0, 1.0, 1.0), (20, 12, 1)),
+    "d2q13_bgk_edm_sinusoidal": RefCase("D2Q13", "BGK", "ExactDifferenceMethod", "Sinusoidal",
+                                        0.75, (1e-3, -2e-3, 0.0), (7.0, 5.0, 1.0), (14, 10, 1)),
+    "d2q13_elbm_guo_kolmogorov": RefCase("D2Q13", "ELBM", "Guo", "Kolmogorov", 0.52,
+                                         (1e-4, 0.0, 0.0), (8.0, 1.0, 1.0), (24, 16, 1)),
+    "d3q33_bgk_guo_kolmogorov": RefCase("D3Q33", "BGK", "Guo", "Kolmogorov", 0.58,
+                                        (1e-3, 0.0, 0.0), (5.0, 1.0, 1.0), (12, 10, 8)),
+    "d3q33_bgk_shanchen_constant": RefCase("D3Q33", "BGK", "ShanChen", "Constant", 0.66,
+                                           (2e-4, 1e-4, -1e-4), (1.0, 1.0, 1.0), (8, 10, 9)),
+    "d3q33_elbm_none_none": RefCase("D3Q33", "ELBM", "None", "None", 0.500250125062531,
+                                    (0.0, 0.0, 0.0), (1.0, 1.0, 1.0), (12, 10, 8)),
     # CPU-baseline timing cases (sizes of the benchmark workloads, run for a
     # bounded number of steps).
     "time_d3q19_bgk_guo_kolmogorov_128": RefCase("D3Q19", "BGK", "Guo", "Kolmogorov", 0.55,

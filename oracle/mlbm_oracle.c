@@ -22,9 +22,11 @@
 #define M_PI 3.14159265358979323846
 #endif
 
-/* ---- Lattice tables (Lattice.h:145-210, 535-612, 614-703) ---------------
- * Velocity order: rest, the faceQ populations with c_x = -1, the faceQ with
- * c_x = +1, then c_x = 0. Weights written as the reference's (T)a/(T)b. */
+/* ---- Lattice tables (Lattice.h:146-210, 214-288, 461-533, 536-612,
+ * 615-703, 707-802) ----------------------------------------------------------
+ * Velocity order: rest, the populations with c_x < 0, those with c_x > 0,
+ * then c_x = 0, in the reference's order. Weights written as the reference's
+ * (T)a/(T)b, or its decimal literals for D3Q33. */
 static const int C_D2Q9[9][3] = {{0, 0, 0},  {-1, 1, 0}, {-1, 0, 0}, {-1, -1, 0}, {1, -1, 0},
                                  {1, 0, 0},  {1, 1, 0},  {0, -1, 0}, {0, 1, 0}};
 static const int C_D3Q19[19][3] = {
@@ -37,6 +39,19 @@ static const int C_D3Q27[27][3] = {
     {1, 0, -1},  {1, 1, 1},   {1, 1, -1},  {1, -1, 1}, {1, -1, -1}, {0, -1, 0},  {0, 0, -1},
     {0, -1, -1}, {0, -1, 1},  {0, 1, 0},   {0, 0, 1},  {0, 1, 1},   {0, 1, -1}};
 
+static const int C_D3Q15[15][3] = {
+    {0, 0, 0},  {-1, 0, 0}, {-1, -1, -1}, {-1, -1, 1}, {-1, 1, -1}, {-1, 1, 1}, {1, 0, 0}, {1, 1, 1},
+    {1, 1, -1}, {1, -1, 1}, {1, -1, -1},  {0, -1, 0},  {0, 0, -1},  {0, 1, 0},  {0, 0, 1}};
+static const int C_D2Q13[13][3] = {{0, 0, 0}, {-1, 0, 0}, {-1, -1, 0}, {-1, 1, 0}, {-2, 0, 0},
+                                   {1, 0, 0}, {1, -1, 0}, {1, 1, 0},   {2, 0, 0},  {0, -1, 0},
+                                   {0, 1, 0}, {0, -2, 0}, {0, 2, 0}};
+static const int C_D3Q33[33][3] = {
+    {0, 0, 0},   {-1, 0, 0},  {-1, -1, 0}, {-1, 1, 0},  {-1, 0, -1}, {-1, 0, 1}, {-1, -1, -1},
+    {-1, -1, 1}, {-1, 1, -1}, {-1, 1, 1},  {-2, 0, 0},  {1, 0, 0},   {1, 1, 0},  {1, -1, 0},
+    {1, 0, 1},   {1, 0, -1},  {1, 1, 1},   {1, 1, -1},  {1, -1, 1},  {1, -1, -1}, {2, 0, 0},
+    {0, -1, 0},  {0, 0, -1},  {0, -1, -1}, {0, -1, 1},  {0, 1, 0},   {0, 0, 1},  {0, 1, 1},
+    {0, 1, -1},  {0, 2, 0},   {0, -2, 0},  {0, 0, 2},   {0, 0, -2}};
+
 static void weights(int lattice, double* w) {
   if (lattice == ORACLE_D2Q9) {
     const double a = 4.0 / 9.0, b = 1.0 / 36.0, c = 1.0 / 9.0;
@@ -46,21 +61,51 @@ static void weights(int lattice, double* w) {
     const double a = 1.0 / 3.0, b = 1.0 / 18.0, c = 1.0 / 36.0;
     const double t[19] = {a, b, c, c, c, c, b, c, c, c, c, b, b, c, c, b, b, c, c};
     memcpy(w, t, sizeof t);
-  } else {
+  } else if (lattice == ORACLE_D3Q27) {
     const double a = 8.0 / 27.0, b = 2.0 / 27.0, c = 1.0 / 54.0, d = 1.0 / 216.0;
     const double t[27] = {a, b, c, c, c, c, d, d, d, d, b, c, c, c,
                           c, d, d, d, d, b, b, c, c, b, b, c, c};
+    memcpy(w, t, sizeof t);
+  } else if (lattice == ORACLE_D3Q15) {
+    const double a = 2.0 / 9.0, b = 1.0 / 9.0, c = 1.0 / 72.0;
+    const double t[15] = {a, b, c, c, c, c, b, c, c, c, c, b, b, b, b};
+    memcpy(w, t, sizeof t);
+  } else if (lattice == ORACLE_D2Q13) {
+    const double w0 = 1.0 / 2.0, w1 = 4.0 / 45.0, w2 = 1.0 / 30.0, w4 = 1.0 / 360.0;
+    const double t[13] = {w0, w1, w2, w2, w4, w1, w2, w2, w4, w1, w1, w4, w4};
+    memcpy(w, t, sizeof t);
+  } else {
+    const double w0 = 0.177627658370520295649084, w1 = 0.103315974899246818673111,
+                 w2 = 0.000513472406731114352456, w3 = 0.021333928148672240120078,
+                 w4 = 0.004273899693974583187026;
+    const double t[33] = {w0, w1, w2, w2, w2, w2, w3, w3, w3, w3, w4, w1, w2, w2, w2, w2, w3,
+                          w3, w3, w3, w4, w1, w1, w2, w2, w1, w1, w2, w2, w4, w4, w4, w4};
     memcpy(w, t, sizeof t);
   }
 }
 
 int oracle_lattice_q(int lattice) {
-  return lattice == ORACLE_D2Q9 ? 9 : (lattice == ORACLE_D3Q19 ? 19 : 27);
+  static const int q[6] = {9, 19, 27, 15, 13, 33};
+  return q[lattice];
 }
-int oracle_lattice_d(int lattice) { return lattice == ORACLE_D2Q9 ? 2 : 3; }
+int oracle_lattice_d(int lattice) {
+  return (lattice == ORACLE_D2Q9 || lattice == ORACLE_D2Q13) ? 2 : 3;
+}
+
+/* inv_cs2 (Lattice.h): 3, except D3Q33 with cs2 = 0.4156023517935171 */
+static double lattice_ics(int lattice) {
+  return lattice == ORACLE_D3Q33 ? 1.0 / 0.4156023517935171 : 3.0;
+}
 
 static const int (*celerity(int lattice))[3] {
-  return lattice == ORACLE_D2Q9 ? C_D2Q9 : (lattice == ORACLE_D3Q19 ? C_D3Q19 : C_D3Q27);
+  switch (lattice) {
+    case ORACLE_D2Q9: return C_D2Q9;
+    case ORACLE_D3Q19: return C_D3Q19;
+    case ORACLE_D3Q27: return C_D3Q27;
+    case ORACLE_D3Q15: return C_D3Q15;
+    case ORACLE_D2Q13: return C_D2Q13;
+    default: return C_D3Q33;
+  }
 }
 
 void oracle_lattice_tables(int lattice, double* c, double* w) {
@@ -71,12 +116,15 @@ void oracle_lattice_tables(int lattice, double* c, double* w) {
   weights(lattice, w);
 }
 
-#define QMAX 27
+#define QMAX 33
 
 typedef struct {
   int D, Q;
   double c[QMAX][3];
   double w[QMAX];
+  /* inv_cs2 and the Power<T, n>::Do(inv_cs2) of the equilibrium, left-folded
+   * products (Helpers.h:93-113) */
+  double ics, p2, p3, p4;
 } lattice_t;
 
 static void lattice_init(lattice_t* L, int lattice) {
@@ -86,6 +134,10 @@ static void lattice_init(lattice_t* L, int lattice) {
   for (int q = 0; q < L->Q; ++q)
     for (int d = 0; d < 3; ++d) L->c[q][d] = (double)ci[q][d];
   weights(lattice, L->w);
+  L->ics = lattice_ics(lattice);
+  L->p2 = L->ics * L->ics;
+  L->p3 = L->ics * L->ics * L->ics;
+  L->p4 = L->ics * L->ics * L->ics * L->ics;
 }
 
 /* MathVector::dot (MathVector.h:45-53): a0*b0, then += ai*bi. */
@@ -95,15 +147,17 @@ static inline double dotD(const double* a, const double* b, int D) {
   return r;
 }
 
-/* Equilibrium<TruncationMa3>::calculate (Equilibrium.h:14-33), inv_cs2 = 3,
- * Power<T,n> = left-folded products (Helpers.h:93-113). */
+/* Equilibrium<TruncationMa3>::calculate (Equilibrium.h:14-33) with
+ * k = inv_cs2 and its powers; Power<T,n> = left-folded products
+ * (Helpers.h:93-113). */
 static inline double equilibrium(const lattice_t* L, double rho, const double* u, double u2,
                                  int q) {
   const double cu = dotD(L->c[q], u, L->D);
-  const double fEq = 1.0 + cu * 3.0 - 0.5 * u2 * 3.0 + 0.5 * 9.0 * cu * cu -
-                     0.5 * 9.0 * cu * u2 + (cu * cu * cu) * 27.0 / 6.0 +
-                     0.125 * u2 * u2 * 9.0 - 0.25 * cu * cu * u2 * 27.0 +
-                     (cu * cu * cu * cu) * 81.0 / 24.0;
+  const double k = L->ics;
+  const double fEq = 1.0 + cu * k - 0.5 * u2 * k + 0.5 * L->p2 * cu * cu -
+                     0.5 * L->p2 * cu * u2 + (cu * cu * cu) * L->p3 / 6.0 +
+                     0.125 * u2 * u2 * L->p2 - 0.25 * cu * cu * u2 * L->p3 +
+                     (cu * cu * cu * cu) * L->p4 / 24.0;
   return rho * L->w[q] * fEq;
 }
 
@@ -169,9 +223,9 @@ static inline double collision_source(const oracle_state* s, const double* F, do
     case ORACLE_FS_GUO: { /* ForcingScheme.h:100-117 */
       const double cu = dotD(L->c[q], u, D);
       double v[3] = {0.0, 0.0, 0.0};
-      for (int d = 0; d < D; ++d) v[d] = L->c[q][d] - u[d] + L->c[q][d] * (3.0 * cu);
+      for (int d = 0; d < D; ++d) v[d] = L->c[q][d] - u[d] + (L->ics * cu) * L->c[q][d];
       const double R = dotD(v, F, D);
-      return (1.0 - 1.0 / (2.0 * s->cfg.tau)) * L->w[q] * 3.0 * R;
+      return (1.0 - 1.0 / (2.0 * s->cfg.tau)) * L->w[q] * L->ics * R;
     }
     case ORACLE_FS_EDM: { /* ForcingScheme.h:183-197 */
       const double inv = 1.0 / rho;
@@ -469,9 +523,9 @@ static void node_update(oracle_state* s, unsigned x, unsigned y, unsigned z, int
   double f[QMAX] = {0.0};
   for (int q = 0; q < Q; ++q) {
     const int* cq = celerity(c->lattice)[q];
-    const long sx = ((long)x - cq[0] + lx) % lx;
-    const long sy = ((long)y - cq[1] + ly) % ly;
-    const long sz = ((long)z - cq[2] + lz) % lz;
+    const long sx = ((long)x - cq[0] + 2 * (long)lx) % lx;
+    const long sy = ((long)y - cq[1] + 2 * (long)ly) % ly;
+    const long sz = ((long)z - cq[2] + 2 * (long)lz) % lz;
     f[q] = s->prev[(long)q * V + (sx * ly + sy) * lz + sz];
   }
 

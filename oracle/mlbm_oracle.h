@@ -19,7 +19,8 @@
 extern "C" {
 #endif
 
-enum { ORACLE_D2Q9 = 0, ORACLE_D3Q19 = 1, ORACLE_D3Q27 = 2 };
+enum { ORACLE_D2Q9 = 0, ORACLE_D3Q19 = 1, ORACLE_D3Q27 = 2, ORACLE_D3Q15 = 3, ORACLE_D2Q13 = 4,
+       ORACLE_D3Q33 = 5 };
 enum { ORACLE_BGK = 0, ORACLE_ELBM = 1 };
 enum { ORACLE_FS_NONE = 0, ORACLE_FS_GUO = 1, ORACLE_FS_SHANCHEN = 2, ORACLE_FS_EDM = 3 };
 enum { ORACLE_F_NONE = 0, ORACLE_F_CONSTANT = 1, ORACLE_F_SINUSOIDAL = 2, ORACLE_F_KOLMOGOROV = 3 };

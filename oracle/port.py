@@ -18,14 +18,14 @@ HERE = Path(__file__).resolve().parent
 BUILD = HERE / "_build"
 LIB_PATH = BUILD / "liboracle.so"
 
-LATTICES = {"D2Q9": 0, "D3Q19": 1, "D3Q27": 2}
+LATTICES = {"D2Q9": 0, "D3Q19": 1, "D3Q27": 2, "D3Q15": 3, "D2Q13": 4, "D3Q33": 5}
 COLLISIONS = {"BGK": 0, "ELBM": 1}
 FORCINGS = {"None": 0, "Guo": 1, "ShanChen": 2, "ExactDifferenceMethod": 3}
 FORCES = {"None": 0, "Constant": 1, "Sinusoidal": 2, "Kolmogorov": 3}
 ALPHA_REFERENCE, ALPHA_RESIDUAL = 0, 1
 GUESS_PREVIOUS, GUESS_TWO = 0, 1
-_Q = {"D2Q9": 9, "D3Q19": 19, "D3Q27": 27}
-_D = {"D2Q9": 2, "D3Q19": 3, "D3Q27": 3}
+_Q = {"D2Q9": 9, "D3Q19": 19, "D3Q27": 27, "D3Q15": 15, "D2Q13": 13, "D3Q33": 33}
+_D = {"D2Q9": 2, "D3Q19": 3, "D3Q27": 3, "D3Q15": 3, "D2Q13": 2, "D3Q33": 3}
 
 _lock = threading.Lock()
 

@@ -14,8 +14,8 @@ import numpy as np
 
 from .build_ref import CASES, OUT, compile_case
 
-_Q = {"D2Q9": 9, "D3Q19": 19, "D3Q27": 27}
-_D = {"D2Q9": 2, "D3Q19": 3, "D3Q27": 3}
+_Q = {"D2Q9": 9, "D3Q19": 19, "D3Q27": 27, "D3Q15": 15, "D2Q13": 13, "D3Q33": 33}
+_D = {"D2Q9": 2, "D3Q19": 3, "D3Q27": 3, "D3Q15": 3, "D2Q13": 2, "D3Q33": 3}
 
 
 def run_reference(case: str, rho: np.ndarray, u: np.ndarray, steps: int) -> dict:

@@ -36,7 +36,7 @@ def case_inputs(name: str):
     """Seeded inputs: BGK cases get |u| ~ 2e-2, entropic cases ~ 5e-2 so the
     Newton solve is active on a good share of nodes."""
     c = CASES[name]
-    dims = 2 if c.lattice == "D2Q9" else 3
+    dims = 2 if c.lattice.startswith("D2") else 3
     shape = (c.size[0], c.size[1], 1 if dims == 2 else c.size[2])
     if c.collision == "BGK":
         seed, amp, ramp = 7, 0.02, 0.01
@@ -46,8 +46,8 @@ def case_inputs(name: str):
     return rho, u, {"seed": seed, "u_amplitude": amp, "rho_amplitude": ramp}
 
 
-def main() -> None:
-    names = [n for n in CASES if not n.startswith("time_")]
+def main(only=None) -> None:
+    names = [n for n in CASES if not n.startswith("time_") and (not only or n in only)]
     build(names)
     for name in names:
         rho, u, gen = case_inputs(name)
@@ -60,4 +60,4 @@ def main() -> None:
 
 
 if __name__ == "__main__":
-    main()
+    main(sys.argv[1:] or None)

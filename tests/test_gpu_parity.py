@@ -101,13 +101,13 @@ def test_reference_layout_roundtrip_and_algorithm_surface():
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("lattice", ["D2Q9", "D3Q19", "D3Q27"])
+@pytest.mark.parametrize("lattice", ["D2Q9", "D3Q19", "D3Q27", "D3Q15", "D2Q13", "D3Q33"])
 def test_kolmogorov_axis_parameter_matches_port(lattice):
     """F_x(z) (force along the contiguous axis), not expressible in the
     reference, against the port with the same axis parameter."""
     from metalbm_gb300 import InputDeck, Lattice, fields
     from oracle import OracleConfig, OraclePort
-    D = 2 if lattice == "D2Q9" else 3
+    D = 2 if lattice.startswith("D2") else 3
     shape = (8, 6, 10) if D == 3 else (8, 10, 1)
     axis = D - 1
     rho, u = fields.perturbed_rest(shape, D, 0.02, seed=5, rho_amplitude=0.01)
@@ -156,14 +156,14 @@ def test_residual_solver_matches_port(lattice, guess):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("lattice", ["D3Q27", "D2Q9"])
+@pytest.mark.parametrize("lattice", ["D3Q27", "D2Q9", "D3Q15", "D2Q13", "D3Q33"])
 def test_residual_solver_bit_exact(lattice):
     """The FP64 residual-mode step evaluates its logarithms with the same
     table-driven method and series tiers as the oracle, in the same operation
     order: populations and alpha agree bit for bit."""
     from metalbm_gb300 import InputDeck, Lattice, fields
     from oracle import ALPHA_RESIDUAL, OracleConfig, OraclePort
-    D = 2 if lattice == "D2Q9" else 3
+    D = 2 if lattice.startswith("D2") else 3
     shape = (10, 8, 6) if D == 3 else (16, 12, 1)
     rho, u = fields.perturbed_rest(shape, D, 0.06, seed=5, rho_amplitude=0.03)
     with Lattice(InputDeck(latticeT=lattice, collisionT="ELBM", relaxationTime=0.5005,
@@ -326,7 +326,8 @@ def test_error_word_and_timeout_paths():
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("case", ["d2q9_bgk_guo_kolmogorov", "d3q19_bgk_edm_sinusoidal",
-                                  "d3q27_bgk_guo_kolmogorov", "d3q27_elbm_none_none"])
+                                  "d3q27_bgk_guo_kolmogorov", "d3q27_elbm_none_none",
+                                  "d2q13_bgk_guo_kolmogorov", "d3q33_elbm_none_none"])
 def test_cpp_routine_drop_in(case, tmp_path):
     """The C++ Routine-shaped host loop on include/mlbm/Algorithm_gpu.h
     (initialize, iterate with isStored on the last step, pack, storeFields in
@@ -337,7 +338,7 @@ def test_cpp_routine_drop_in(case, tmp_path):
     exe = build.build_routine()
     inp = np.concatenate([g["rho0"].ravel(), g["u0"].ravel()])
     inp.tofile(tmp_path / "in.bin")
-    codes = {"D2Q9": 0, "D3Q19": 1, "D3Q27": 2}
+    codes = {"D2Q9": 0, "D3Q19": 1, "D3Q27": 2, "D3Q15": 3, "D2Q13": 4, "D3Q33": 5}
     coll = {"BGK": 0, "ELBM": 1, "ForcedBNR_ELBM": 2}[meta["collision"]]
     fs = {"None": 0, "Guo": 1, "ShanChen": 2, "ExactDifferenceMethod": 3}[meta["forcing"]]
     fo = {"None": 0, "Constant": 1, "Sinusoidal": 2, "Kolmogorov": 3}[meta["force"]]

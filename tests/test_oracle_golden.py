@@ -72,35 +72,58 @@ def test_entropic_variants_equal_elbm_in_reference(variant):
     assert np.array_equal(a["f"], b["f"]) and np.array_equal(a["alpha"], b["alpha"])
 
 
-@pytest.mark.parametrize("lattice", ["D2Q9", "D3Q19", "D3Q27"])
+# c_s^2 of each lattice and the coefficient of its isotropic fourth moment
+# sum w c_a c_b c_c c_d = m4 (dd + dd + dd): m4 = cs2^2 except on D2Q13
+LATTICE_MOMENTS = {"D2Q9": (1 / 3, 1 / 9), "D3Q19": (1 / 3, 1 / 9), "D3Q27": (1 / 3, 1 / 9),
+                   "D3Q15": (1 / 3, 1 / 9), "D2Q13": (1 / 3, 2 / 15),
+                   "D3Q33": (0.4156023517935171, 0.4156023517935171 ** 2)}
+
+
+@pytest.mark.parametrize("lattice", list(LATTICE_MOMENTS))
 def test_lattice_isotropy(lattice):
     """Known answers of TestLattice.cpp (re-derived): sum w = 1, sum w c = 0,
-    sum w c c = cs2 delta, third moment 0, fourth = cs2^2 (dd + dd + dd)."""
+    sum w c c = cs2 delta, third moment 0, fourth isotropic. D2Q13's fourth
+    moment is 2/15 (dd + dd + dd), not cs2^2 = 1/9."""
     c, w = lattice_tables(lattice)
-    D = 2 if lattice == "D2Q9" else 3
+    D = 2 if lattice.startswith("D2") else 3
     c = c[:, :D]
-    cs2 = 1.0 / 3.0
+    cs2, m4 = LATTICE_MOMENTS[lattice]
     assert abs(w.sum() - 1.0) < 1e-15
     assert np.abs(np.einsum("q,qa->a", w, c)).max() < 1e-15
     assert np.abs(np.einsum("q,qa,qb->ab", w, c, c) - cs2 * np.eye(D)).max() < 1e-15
     assert np.abs(np.einsum("q,qa,qb,qc->abc", w, c, c, c)).max() < 1e-15
     I = np.eye(D)
-    iso4 = cs2 ** 2 * (np.einsum("ab,cd->abcd", I, I) + np.einsum("ac,bd->abcd", I, I)
-                       + np.einsum("ad,bc->abcd", I, I))
+    iso4 = m4 * (np.einsum("ab,cd->abcd", I, I) + np.einsum("ac,bd->abcd", I, I)
+                 + np.einsum("ad,bc->abcd", I, I))
     assert np.abs(np.einsum("q,qa,qb,qc,qd->abcd", w, c, c, c, c) - iso4).max() < 1e-15
     # opposite velocities: faceQ populations with c_x=-1 then their +1 mirrors
     assert (c[0] == 0).all()
 
 
-@pytest.mark.parametrize("lattice", ["D2Q9", "D3Q19", "D3Q27"])
+@pytest.mark.parametrize("lattice", ["D2Q9", "D3Q19", "D3Q27", "D3Q15", "D3Q33"])
 def test_equilibrium_moments(lattice):
     """TestMoment.cpp:68-95 idea: moments of f_eq(rho,u) give back rho and rho u."""
     c, w = lattice_tables(lattice)
-    D = 2 if lattice == "D2Q9" else 3
+    D = 2 if lattice.startswith("D2") else 3
     rho, u = 1.037, np.array([0.011, -0.02, 0.007])[:D]
     feq = np.array([equilibrium(lattice, rho, u, q) for q in range(len(w))])
     assert abs(feq.sum() - rho) < 1e-14
     assert np.abs(feq @ c[:, :D] - rho * u).max() < 1e-14
+
+
+def test_d2q13_equilibrium_moment_excess():
+    """On D2Q13 the TruncationMa3 equilibrium with inv_cs2 = 3
+    (Equilibrium.h:14-33) conserves neither mass nor momentum exactly: the
+    lattice's fourth moment is 2/15 (dd + dd + dd) instead of cs2^2 = 1/9, so
+    sum f_eq = rho (1 + (9/8 - 27/12 + 81/24 * 2/5) |u|^4) = rho (1 + 0.225 |u|^4)
+    and sum c f_eq = rho u (1 + (27/6 * 2/5 - 9/2 * 1/3) |u|^2) = rho u (1 + 0.3 |u|^2).
+    The reference's D2Q13 runs drift in mass accordingly (goldens d2q13_*)."""
+    c, w = lattice_tables("D2Q13")
+    rho, u = 1.037, np.array([0.031, -0.02])
+    feq = np.array([equilibrium("D2Q13", rho, u, q) for q in range(13)])
+    u2 = u @ u
+    assert abs((feq.sum() - rho) / (rho * u2 * u2) - 0.225) < 1e-6
+    assert np.abs((feq @ c[:, :2] - rho * u) / (rho * u * u2) - 0.3).max() < 1e-6
 
 
 def test_density_known_answer():
