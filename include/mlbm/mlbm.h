@@ -69,8 +69,22 @@ enum {
 };
 enum { MLBM_FORCING_NONE = 0, MLBM_FORCING_GUO = 1, MLBM_FORCING_SHAN_CHEN = 2,
        MLBM_FORCING_EXACT_DIFFERENCE = 3 };                         /* ForcingSchemeType */
-enum { MLBM_FORCE_NONE = 0, MLBM_FORCE_CONSTANT = 1, MLBM_FORCE_SINUSOIDAL = 2,
-       MLBM_FORCE_KOLMOGOROV = 3 };                                 /* ForceType */
+/* ForceType (Options.h:39-41). The spectral forces (Force.h:294-626) run with
+ * FP64 storage; their shells use force_kmin/force_kmax and, for the removal
+ * part, removal_amplitude / removal_kmin / removal_kmax:
+ *   CONSTANT_SHELL  time-independent solenoidal forcing on the shell
+ *                   kmin <= |k| <= kmax (curl of a constant-amplitude spectrum)
+ *   ENERGY_REMOVAL  F = -A P_shell(rho u) from the last stored fields, every step
+ *   TURBULENT_2D    CONSTANT_SHELL + ENERGY_REMOVAL (any dimension) */
+enum {
+  MLBM_FORCE_NONE = 0,
+  MLBM_FORCE_CONSTANT = 1,
+  MLBM_FORCE_SINUSOIDAL = 2,
+  MLBM_FORCE_KOLMOGOROV = 3,
+  MLBM_FORCE_CONSTANT_SHELL = 4,
+  MLBM_FORCE_ENERGY_REMOVAL = 5,
+  MLBM_FORCE_TURBULENT_2D = 6
+};
 
 /* Population storage in HBM. F64 is the reference's dataT = double;
  * F32 stores f in float; F16_SHIFTED stores (f_q - w_q) * 2^k_q in binary16
@@ -131,7 +145,13 @@ typedef struct {
   int newton_max_iterations;  /* reference 50 (Collision.h:337) */
   double deviation_threshold; /* reference 1e-3 (Collision.h:357); 0 disables */
   int device;             /* CUDA device ordinal */
-  int reserved[7];
+  /* spectral forces (Input_prod_3d.in:50-58): integer wavenumber shells */
+  int force_kmin;             /* forcekMin, reference 1 */
+  int force_kmax;             /* forcekMax, reference 2 */
+  int removal_kmin;           /* removalForcekMin, reference 1 */
+  int removal_kmax;           /* removalForcekMax, reference 2 */
+  double removal_amplitude[3]; /* removalForceAmplitude, reference 1e-6 */
+  int reserved[4];
 } mlbm_config;
 
 typedef struct {

@@ -102,8 +102,9 @@ def build(force: bool = False, verbose: bool = False) -> Path:
         results = list(ex.map(_compile, todo))
     (BUILD / "ptxas.log").write_text("\n".join(log for _, log in results))
     tmp = LIB.with_suffix(f".so.{os.getpid()}.tmp")
+    # cuFFT: the plain forward/backward transforms of the spectral forces
     cmd = [nvcc(), *ARCH, "-shared", "-o", str(tmp), *[str(o) for o, _ in results],
-           "-Xcompiler", "-fPIC"]
+           "-Xcompiler", "-fPIC", "-lcufft"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stderr[-4000:]}")

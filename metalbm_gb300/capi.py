@@ -19,6 +19,7 @@ BGK, ELBM, FORCED_BNR_ELBM = 0, 1, 2
 APPROACHED_ELBM, MALASPINAS_ELBM, ESSENTIALLY1_ELBM, ESSENTIALLY2_ELBM, FORCED_NR_ELBM = range(3, 8)
 FORCING_NONE, FORCING_GUO, FORCING_SHAN_CHEN, FORCING_EXACT_DIFFERENCE = 0, 1, 2, 3
 FORCE_NONE, FORCE_CONSTANT, FORCE_SINUSOIDAL, FORCE_KOLMOGOROV = 0, 1, 2, 3
+FORCE_CONSTANT_SHELL, FORCE_ENERGY_REMOVAL, FORCE_TURBULENT_2D = 4, 5, 6
 STORAGE_F64, STORAGE_F32, STORAGE_F16_SHIFTED = 0, 1, 2
 ALPHA_REFERENCE, ALPHA_RESIDUAL = 0, 1
 GUESS_PREVIOUS, GUESS_TWO, GUESS_LEARNED = 0, 1, 2
@@ -46,7 +47,9 @@ class Config(ct.Structure):
                 ("length", ct.c_int * 3), ("storage", ct.c_int), ("alpha_mode", ct.c_int),
                 ("alpha_guess", ct.c_int), ("newton_tolerance", ct.c_double),
                 ("newton_max_iterations", ct.c_int), ("deviation_threshold", ct.c_double),
-                ("device", ct.c_int), ("reserved", ct.c_int * 7)]
+                ("device", ct.c_int), ("force_kmin", ct.c_int), ("force_kmax", ct.c_int),
+                ("removal_kmin", ct.c_int), ("removal_kmax", ct.c_int),
+                ("removal_amplitude", ct.c_double * 3), ("reserved", ct.c_int * 4)]
 
 
 class Diag(ct.Structure):

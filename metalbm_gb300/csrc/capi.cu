@@ -94,6 +94,7 @@ struct mlbm_handle {
   bool diag_valid = false;
   bool fields_valid = false;
   StepParams base{};
+  SpectralForce* spectral = nullptr;  // spectral forces (FP64 storage)
   std::string error;
 };
 
@@ -231,6 +232,11 @@ extern "C" int mlbm_config_init(mlbm_config* c) {
   c->newton_max_iterations = 50;
   c->deviation_threshold = 1e-3;
   c->device = 0;
+  c->force_kmin = 1;  // Input_prod_3d.in:52-58
+  c->force_kmax = 2;
+  c->removal_kmin = 1;
+  c->removal_kmax = 2;
+  for (int d = 0; d < 3; ++d) c->removal_amplitude[d] = 1e-6;
   return MLBM_OK;
 }
 
@@ -244,6 +250,7 @@ static void release(mlbm_handle* h) {
                   h->sample_feat, h->sample_alpha, h->sample_solved};
   for (void* p : ptrs)
     if (p) cudaFree(p);
+  spectral_force_destroy(h->spectral);
   if (h->own_stream) cudaStreamDestroy(h->own_stream);
   delete h;
 }
@@ -336,7 +343,8 @@ extern "C" int mlbm_create(const mlbm_config* cfg, mlbm_handle** out) {
     return fail(nullptr, MLBM_ERR_INVALID, "bad collision %d", c.collision);
   if (c.forcing_scheme < 0 || c.forcing_scheme > 3)
     return fail(nullptr, MLBM_ERR_INVALID, "bad forcing scheme %d", c.forcing_scheme);
-  if (c.force < 0 || c.force > 3) return fail(nullptr, MLBM_ERR_INVALID, "bad force %d", c.force);
+  if (c.force < 0 || c.force > MLBM_FORCE_TURBULENT_2D)
+    return fail(nullptr, MLBM_ERR_INVALID, "bad force %d", c.force);
   if (c.storage < 0 || c.storage > 2) return fail(nullptr, MLBM_ERR_INVALID, "bad storage %d", c.storage);
   if (c.storage != MLBM_STORAGE_F64 && c.lattice > MLBM_D3Q27)
     return fail(nullptr, MLBM_ERR_INVALID,
@@ -363,6 +371,20 @@ extern "C" int mlbm_create(const mlbm_config* cfg, mlbm_handle** out) {
   if (c.force == MLBM_FORCE_SINUSOIDAL || c.force == MLBM_FORCE_KOLMOGOROV)
     for (int d = 0; d < D; ++d)
       if (c.force_wavelength[d] == 0.0) return fail(nullptr, MLBM_ERR_INVALID, "zero force wavelength");
+
+  const bool spectral = c.force >= MLBM_FORCE_CONSTANT_SHELL;
+  if (spectral) {
+    if (c.storage != MLBM_STORAGE_F64)
+      return fail(nullptr, MLBM_ERR_INVALID, "the spectral forces run with FP64 storage");
+    long long lmin = L[0];
+    for (int d = 1; d < D; ++d) lmin = std::min(lmin, L[d]);
+    const bool inj = c.force != MLBM_FORCE_ENERGY_REMOVAL, rem = c.force != MLBM_FORCE_CONSTANT_SHELL;
+    if ((inj && (c.force_kmin < 0 || c.force_kmax < c.force_kmin || 2LL * c.force_kmax >= lmin)) ||
+        (rem && (c.removal_kmin < 0 || c.removal_kmax < c.removal_kmin ||
+                 2LL * c.removal_kmax >= lmin)))
+      return fail(nullptr, MLBM_ERR_INVALID,
+                  "bad spectral shell: need 0 <= kmin <= kmax and 2 kmax < the shortest length");
+  }
 
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
@@ -464,6 +486,21 @@ extern "C" int mlbm_create(const mlbm_config* cfg, mlbm_handle** out) {
   cudaMemsetAsync(h->err_word, 0, sizeof(unsigned), h->stream);
   cudaMemsetAsync(h->mlp, 0, sizeof(MlpDev), h->stream);
 
+  // Spectral forces: the force field on the device (spectral_force.cu).
+  if (spectral) {
+    char msg[256] = {0};
+    if (spectral_force_create(&h->spectral, c.force, D, (int)L[0], (int)L[1], (int)L[2],
+                              c.force_amplitude, c.force_kmin, c.force_kmax, c.removal_amplitude,
+                              c.removal_kmin, c.removal_kmax, h->stream, msg, sizeof msg)) {
+      h->error = std::string("spectral force: ") + msg;
+      return bail(MLBM_ERR_CUDA);
+    }
+  }
+  // EnergyRemoval reads the stored fields before the first store: zero until
+  // mlbm_init_equilibrium fills them.
+  cudaMemsetAsync(h->rho, 0, sizeof(double) * V, h->stream);
+  cudaMemsetAsync(h->u, 0, sizeof(double) * V * D, h->stream);
+
   // Force profiles tabulated on the host (Force.h:208-215, 262-267).
   if (c.force == MLBM_FORCE_SINUSOIDAL || c.force == MLBM_FORCE_KOLMOGOROV) {
     const int ntab = c.force == MLBM_FORCE_SINUSOIDAL ? D : 1;
@@ -502,7 +539,8 @@ extern "C" int mlbm_create(const mlbm_config* cfg, mlbm_handle** out) {
     for (int q = 0; q < h->Q; ++q)  // ForcingScheme.h:115-116
       p.guo_k[q] = (1.0 - 1.0 / (2.0 * c.relaxation_time)) * hl.w[q] * hl.ics;
   }
-  p.force_type = c.force;
+  p.force_type = spectral ? FORCE_FIELD : c.force;
+  p.force_field = spectral ? spectral_force_field(h->spectral) : nullptr;
   p.kol_axis = c.kolmogorov_axis;
   p.kol_comp = c.kolmogorov_component;
   for (int d = 0; d < 3; ++d) p.amp[d] = d < D ? c.force_amplitude[d] : 0.0;
@@ -636,6 +674,13 @@ extern "C" int mlbm_step(mlbm_handle* h, int nsteps, unsigned int flags) {
     p.diag = last && (flags & MLBM_STEP_DIAGNOSTICS) ? 1 : 0;
     const void* prev = h->f[h->cur];
     void* next = h->f[1 - h->cur];
+    if (h->spectral && spectral_force_time_dependent(h->spectral)) {
+      // Collision::update before the sweep (Algorithm.h:338): the force field
+      // from the last stored fields
+      char msg[256] = {0};
+      if (spectral_force_update(h->spectral, h->rho, h->u, h->stream, msg, sizeof msg))
+        return fail(h, MLBM_ERR_CUDA, "spectral force: %s", msg);
+    }
     cudaError_t e = h->storage == MLBM_STORAGE_F64
                         ? step_f64(h->cfg.lattice, collision, h->cfg.forcing_scheme,
                                    (const double*)prev, (double*)next, p, h->stream)

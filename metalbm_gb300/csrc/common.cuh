@@ -9,7 +9,10 @@
 namespace mlbm {
 
 enum : int { FS_NONE = 0, FS_GUO = 1, FS_SHANCHEN = 2, FS_EDM = 3 };
-enum : int { FORCE_NONE = 0, FORCE_CONSTANT = 1, FORCE_SINUSOIDAL = 2, FORCE_KOLMOGOROV = 3 };
+// FORCE_FIELD: the per-node force read from force_field [D][V] (the spectral
+// forces, Force.h:294-626, computed into that array before each step)
+enum : int { FORCE_NONE = 0, FORCE_CONSTANT = 1, FORCE_SINUSOIDAL = 2, FORCE_KOLMOGOROV = 3,
+             FORCE_FIELD = 7 };
 enum : int { ALPHA_REFERENCE = 0, ALPHA_RESIDUAL = 1 };
 enum : int { GUESS_PREVIOUS = 0, GUESS_TWO = 1, GUESS_LEARNED = 2 };
 
@@ -47,6 +50,7 @@ struct StepParams {
   int kol_axis, kol_comp;
   double amp[3];
   const double* force_table[3];  // per-axis host-computed sin profiles (device)
+  const double* force_field;     // [D][V] per-node force of FORCE_FIELD (device)
   // float copies for the low-precision kernels, which execute no FP64
   // instruction on their common path (a double->float conversion runs on
   // GB300's narrow FP64 pipe)
@@ -179,6 +183,12 @@ __device__ __forceinline__ void node_force(const StepParams& p, uint32_t x, uint
       F[0] = p.kol_comp == 0 ? v : 0.0;
       F[1] = p.kol_comp == 1 ? v : 0.0;
       F[2] = p.kol_comp == 2 ? v : 0.0;
+      break;
+    }
+    case FORCE_FIELD: {  // Force<Generic>::setForce (Force.h:36-45)
+      const uint32_t i = (x * p.ly + y) * p.lz + z;
+#pragma unroll
+      for (int d = 0; d < D; ++d) F[d] = __ldg(p.force_field + (long long)d * p.V + i);
       break;
     }
     default:

@@ -76,6 +76,21 @@ cudaError_t log_samples(int lattice, int storage, const void* prev, const StepPa
                         const long long* nodes, long long n, double* features, double* alpha,
                         int* solved, cudaStream_t s);
 
+// Spectral forces (spectral_force.cu): a force field [D][V] on the device,
+// computed once (ConstantShell) or before every step from the stored fields
+// (EnergyRemoval, Turbulent2D). Functions return 0 on success, else write a
+// message to err.
+void count_launches(unsigned n);
+struct SpectralForce;
+int spectral_force_create(SpectralForce** out, int force, int D, int lx, int ly, int lz,
+                          const double amp[3], int kmin, int kmax, const double ramp[3],
+                          int rkmin, int rkmax, cudaStream_t s, char* err, size_t errlen);
+int spectral_force_update(SpectralForce* sf, const double* rho, const double* u, cudaStream_t s,
+                          char* err, size_t errlen);
+const double* spectral_force_field(const SpectralForce* sf);
+bool spectral_force_time_dependent(const SpectralForce* sf);
+void spectral_force_destroy(SpectralForce* sf);
+
 // Per-lattice (and per-storage) entry points, one translation unit each.
 cudaError_t step_f64_L0(int collision, int forcing, const double* prev, double* next, const StepParams& p, cudaStream_t s);
 cudaError_t init_f64_L0(const double* rho, const double* u, double* f, long long V, cudaStream_t s);

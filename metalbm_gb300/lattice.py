@@ -27,7 +27,9 @@ _FORCINGS = {"None": capi.FORCING_NONE, "Guo": capi.FORCING_GUO,
              "ShanChen": capi.FORCING_SHAN_CHEN,
              "ExactDifferenceMethod": capi.FORCING_EXACT_DIFFERENCE}
 _FORCES = {"None": capi.FORCE_NONE, "Constant": capi.FORCE_CONSTANT,
-           "Sinusoidal": capi.FORCE_SINUSOIDAL, "Kolmogorov": capi.FORCE_KOLMOGOROV}
+           "Sinusoidal": capi.FORCE_SINUSOIDAL, "Kolmogorov": capi.FORCE_KOLMOGOROV,
+           "ConstantShell": capi.FORCE_CONSTANT_SHELL, "EnergyRemoval": capi.FORCE_ENERGY_REMOVAL,
+           "Turbulent2D": capi.FORCE_TURBULENT_2D}
 _STORAGES = {"f64": capi.STORAGE_F64, "f32": capi.STORAGE_F32,
              "f16_shifted": capi.STORAGE_F16_SHIFTED}
 _ALPHA = {"reference": capi.ALPHA_REFERENCE, "residual": capi.ALPHA_RESIDUAL}
@@ -52,6 +54,12 @@ class InputDeck:
     # reference is axis = 1 (y), component = 0 (x), Force.h:262-267.
     kolmogorovAxis: int = 1
     kolmogorovComponent: int = 0
+    # spectral forces (src/Input_prod_3d.in:50-58): integer wavenumber shells
+    forcekMin: int = 1
+    forcekMax: int = 2
+    removalForceAmplitude: tuple = (1e-6, 1e-6, 1e-6)
+    removalForcekMin: int = 1
+    removalForcekMax: int = 2
     # GB300 build options
     storage: str = "f64"
     alphaSolver: str = "reference"
@@ -65,6 +73,7 @@ class InputDeck:
         self.forceAmplitude = tuple(self.forceAmplitude)
         self.forceWaveLength = tuple(self.forceWaveLength)
         self.globalLength = tuple(self.globalLength)
+        self.removalForceAmplitude = tuple(self.removalForceAmplitude)
 
     @property
     def Q(self) -> int:
@@ -96,6 +105,10 @@ class InputDeck:
             c.length[d] = int(self.globalLength[d])
         c.kolmogorov_axis = int(self.kolmogorovAxis)
         c.kolmogorov_component = int(self.kolmogorovComponent)
+        c.force_kmin, c.force_kmax = int(self.forcekMin), int(self.forcekMax)
+        c.removal_kmin, c.removal_kmax = int(self.removalForcekMin), int(self.removalForcekMax)
+        for d in range(3):
+            c.removal_amplitude[d] = float(self.removalForceAmplitude[d])
         c.storage = _STORAGES[self.storage]
         c.alpha_mode = _ALPHA[self.alphaSolver]
         c.alpha_guess = _GUESS[self.alphaGuess]

@@ -178,6 +178,7 @@ struct oracle_state {
   double* rho;   /* stored fields (Algorithm.h:150-194) */
   double* u;
   double* force;
+  double* force_field; /* [D][V], ORACLE_F_FIELD */
   long long* newton_iterations;
   long long* fallbacks;
   long long* bisections;
@@ -198,6 +199,11 @@ static void node_force(const oracle_state* s, const unsigned* pos, double* F) {
   const int D = s->L.D;
   for (int d = 0; d < 3; ++d) F[d] = 0.0;
   switch (c->force) {
+    case ORACLE_F_FIELD: { /* Force<Generic>::setForce (Force.h:36-45) */
+      const long idx = ((long)pos[0] * c->ly + pos[1]) * c->lz + pos[2];
+      for (int d = 0; d < D; ++d) F[d] = s->force_field[(long)d * s->V + idx];
+      break;
+    }
     case ORACLE_F_CONSTANT:
       for (int d = 0; d < D; ++d) F[d] = c->amplitude[d];
       break;
@@ -597,10 +603,11 @@ oracle_state* oracle_create(const oracle_config* cfg) {
   s->rho = (double*)calloc((size_t)V, sizeof(double));
   s->u = (double*)calloc((size_t)(D * V), sizeof(double));
   s->force = (double*)calloc((size_t)(D * V), sizeof(double));
+  s->force_field = (double*)calloc((size_t)(D * V), sizeof(double));
   s->newton_iterations = (long long*)calloc((size_t)s->cfg.threads, sizeof(long long));
   s->fallbacks = (long long*)calloc((size_t)s->cfg.threads, sizeof(long long));
   s->bisections = (long long*)calloc((size_t)s->cfg.threads, sizeof(long long));
-  if (!s->prev || !s->next || !s->alpha || !s->rho || !s->u || !s->force ||
+  if (!s->prev || !s->next || !s->alpha || !s->rho || !s->u || !s->force || !s->force_field ||
       !s->newton_iterations || !s->fallbacks || !s->bisections) {
     oracle_destroy(s);
     return NULL;
@@ -617,6 +624,7 @@ void oracle_destroy(oracle_state* s) {
   free(s->rho);
   free(s->u);
   free(s->force);
+  free(s->force_field);
   free(s->newton_iterations);
   free(s->fallbacks);
   free(s->bisections);
@@ -697,6 +705,10 @@ void oracle_get_fields(const oracle_state* s, double* rho, double* u, double* al
   if (u) memcpy(u, s->u, sizeof(double) * (size_t)(D * V));
   if (alpha) memcpy(alpha, s->alpha, sizeof(double) * (size_t)V);
   if (force) memcpy(force, s->force, sizeof(double) * (size_t)(D * V));
+}
+
+void oracle_set_force_field(oracle_state* s, const double* force) {
+  memcpy(s->force_field, force, sizeof(double) * (size_t)(s->L.D * s->V));
 }
 
 void oracle_get_counters(const oracle_state* s, long long* newton_iterations,

@@ -23,7 +23,12 @@ enum { ORACLE_D2Q9 = 0, ORACLE_D3Q19 = 1, ORACLE_D3Q27 = 2, ORACLE_D3Q15 = 3, OR
        ORACLE_D3Q33 = 5 };
 enum { ORACLE_BGK = 0, ORACLE_ELBM = 1 };
 enum { ORACLE_FS_NONE = 0, ORACLE_FS_GUO = 1, ORACLE_FS_SHANCHEN = 2, ORACLE_FS_EDM = 3 };
-enum { ORACLE_F_NONE = 0, ORACLE_F_CONSTANT = 1, ORACLE_F_SINUSOIDAL = 2, ORACLE_F_KOLMOGOROV = 3 };
+/* ORACLE_F_FIELD: the per-node force is read from a D x V array set with
+ * oracle_set_force_field (Force<Generic>::setForce, Force.h:36-45), the
+ * mechanism of the reference's array forces (ConstantShell, EnergyRemoval,
+ * Turbulent2D, Force.h:294-626). */
+enum { ORACLE_F_NONE = 0, ORACLE_F_CONSTANT = 1, ORACLE_F_SINUSOIDAL = 2, ORACLE_F_KOLMOGOROV = 3,
+       ORACLE_F_FIELD = 4 };
 /* Entropic alpha solver.
  * REFERENCE: Collision.h:284-375 + EntropicStep.h:111-140 exactly: alpha = 2
  *   when every |f_neq|/f <= deviation_threshold; 0.95*alpha_max when
@@ -72,6 +77,8 @@ void oracle_get_populations(const oracle_state* s, double* f);
 void oracle_step(oracle_state* s, int nsteps, int store_last);
 void oracle_get_fields(const oracle_state* s, double* rho, double* u, double* alpha,
                        double* force);
+/* Force field [D][V] (dense node order) read by ORACLE_F_FIELD; copied. */
+void oracle_set_force_field(oracle_state* s, const double* force);
 /* Sum of Newton iterations and count of alpha=2 fallbacks over the last step. */
 void oracle_get_counters(const oracle_state* s, long long* newton_iterations,
                          long long* fallbacks, long long* bisections);

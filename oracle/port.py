@@ -21,7 +21,8 @@ LIB_PATH = BUILD / "liboracle.so"
 LATTICES = {"D2Q9": 0, "D3Q19": 1, "D3Q27": 2, "D3Q15": 3, "D2Q13": 4, "D3Q33": 5}
 COLLISIONS = {"BGK": 0, "ELBM": 1}
 FORCINGS = {"None": 0, "Guo": 1, "ShanChen": 2, "ExactDifferenceMethod": 3}
-FORCES = {"None": 0, "Constant": 1, "Sinusoidal": 2, "Kolmogorov": 3}
+# "Field": the per-node force read from an array set with set_force_field
+FORCES = {"None": 0, "Constant": 1, "Sinusoidal": 2, "Kolmogorov": 3, "Field": 4}
 ALPHA_REFERENCE, ALPHA_RESIDUAL = 0, 1
 GUESS_PREVIOUS, GUESS_TWO = 0, 1
 _Q = {"D2Q9": 9, "D3Q19": 19, "D3Q27": 27, "D3Q15": 15, "D2Q13": 13, "D3Q33": 33}
@@ -72,6 +73,7 @@ def _load():
         lib.oracle_get_populations.argtypes = [ct.c_void_p, dp]
         lib.oracle_step.argtypes = [ct.c_void_p, ct.c_int, ct.c_int]
         lib.oracle_get_fields.argtypes = [ct.c_void_p, dp, dp, dp, dp]
+        lib.oracle_set_force_field.argtypes = [ct.c_void_p, dp]
         lib.oracle_get_counters.argtypes = [ct.c_void_p] + [ct.POINTER(ct.c_longlong)] * 3
         lib.oracle_equilibrium.restype = ct.c_double
         lib.oracle_equilibrium.argtypes = [ct.c_int, ct.c_double, dp, ct.c_int]
@@ -162,6 +164,11 @@ class OraclePort:
 
     def step(self, n: int, store_last: bool = True):
         self._lib.oracle_step(self._h, int(n), int(bool(store_last)))
+
+    def set_force_field(self, force: np.ndarray):
+        """Per-node force [D, V] for force "Field" (Force.h:36-45)."""
+        force = np.ascontiguousarray(force, dtype=np.float64).reshape(self.D * self.V)
+        self._lib.oracle_set_force_field(self._h, _ptr(force))
 
     def fields(self) -> dict[str, np.ndarray]:
         rho = np.empty(self.V)

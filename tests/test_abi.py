@@ -116,3 +116,27 @@ def test_new_lattices_run_with_fp64_storage_only(lib):
     h = ct.c_void_p()
     assert lib.mlbm_create(ct.byref(c), ct.byref(h)) == capi.ERR_INVALID
     assert b"bad lattice" in lib.mlbm_last_error(None)
+
+
+def test_spectral_force_configurations_are_checked(lib):
+    """Spectral forces: FP64 storage only, shells 0 <= kmin <= kmax with
+    2 kmax below the shortest length; refused before any device work."""
+    from metalbm_gb300 import capi
+    h = ct.c_void_p()
+    cases = [(dict(storage=capi.STORAGE_F32), b"FP64 storage"),
+             (dict(force_kmax=8), b"spectral shell"),
+             (dict(force_kmin=3, force_kmax=2), b"spectral shell")]
+    for kw, msg in cases:
+        c = capi.Config()
+        lib.mlbm_config_init(ct.byref(c))
+        c.lattice, c.force = capi.D3Q19, capi.FORCE_TURBULENT_2D
+        c.length[0] = c.length[1] = c.length[2] = 16
+        for k, v in kw.items():
+            setattr(c, k, v)
+        assert lib.mlbm_create(ct.byref(c), ct.byref(h)) == capi.ERR_INVALID
+        assert msg in lib.mlbm_last_error(None), lib.mlbm_last_error(None)
+    c = capi.Config()
+    lib.mlbm_config_init(ct.byref(c))
+    c.force = 7
+    assert lib.mlbm_create(ct.byref(c), ct.byref(h)) == capi.ERR_INVALID
+    assert c.removal_kmin == 1 and c.removal_kmax == 2 and c.removal_amplitude[0] == 1e-6
