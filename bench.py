@@ -65,7 +65,18 @@ WORKLOADS = {
                               forceAmplitude=(1e-6, 0.0, 0.0), forceWaveLength=(128.0, 1.0, 1.0),
                               kolmogorovAxis=2, globalLength=(256, 256, 256),
                               storage="f16_shifted", bytes_per_node=2 * 19 * 2),
+    # the 3-D production deck's lattice and scheme (Input_prod_3d.in: D3Q27, BGK,
+    # exact-difference forcing) with the time-dependent spectral force: the
+    # force field from two batched FFTs and a shell filter before every step
+    "turbulent_d3q27_f64_256": dict(latticeT="D3Q27", collisionT="BGK", relaxationTime=0.55,
+                                    forcingSchemeT="ExactDifferenceMethod", forceT="Turbulent2D",
+                                    forceAmplitude=(1e-6, 1e-6, 1e-6), forcekMin=1, forcekMax=2,
+                                    removalForceAmplitude=(1e-6, 1e-6, 1e-6), removalForcekMin=1,
+                                    removalForcekMax=2, globalLength=(256, 256, 256),
+                                    storage="f64", bytes_per_node=2 * 27 * 8 + 3 * 8),
 }
+
+SPECTRAL_FORCES = ("ConstantShell", "EnergyRemoval", "Turbulent2D")
 
 
 def initial_field(name: str, shape):
@@ -206,35 +217,72 @@ def load_or_train_model(deck, torch):
     return model, "trained in bench setup (64^3, 100 steps)"
 
 
+class PortRun:
+    """The oracle port on a sample of a workload. Spectral forces: the force
+    field restated with numpy FFTs before every step from the stored fields,
+    which stay the initial ones (no step stores, as in the timed GPU steps)."""
+
+    def __init__(self, name: str, shape, threads: int):
+        from oracle import ALPHA_REFERENCE, OracleConfig, OraclePort
+        w = WORKLOADS[name]
+        self.w, self.shape = w, shape
+        self.spectral = w.get("forceT") in SPECTRAL_FORCES
+        self.rho, self.u = initial_field(name, shape)
+        cfg = OracleConfig(lattice=w["latticeT"],
+                           collision="ELBM" if w["collisionT"] != "BGK" else "BGK",
+                           forcing=w.get("forcingSchemeT", "None"),
+                           force="Field" if self.spectral else w.get("forceT", "None"),
+                           tau=w["relaxationTime"], amplitude=w.get("forceAmplitude", (0, 0, 0)),
+                           wavelength=w.get("forceWaveLength", (1, 1, 1)),
+                           kolmogorov_axis=w.get("kolmogorovAxis", 1), size=shape,
+                           alpha_mode=ALPHA_REFERENCE, threads=threads)
+        self.port = OraclePort(cfg)
+        self.port.init_equilibrium(self.rho, self.u)
+
+    def step(self, n: int):
+        if not self.spectral:
+            self.port.step(n, store_last=False)
+            return
+        from oracle import spectral_force as sf
+        w, D = self.w, 3
+        for _ in range(n):
+            if w["forceT"] == "ConstantShell":
+                F = sf.constant_shell_field(self.shape, D, w["forceAmplitude"], w["forcekMin"],
+                                            w["forcekMax"])
+            elif w["forceT"] == "EnergyRemoval":
+                F = sf.energy_removal_field(self.rho, self.u, self.shape, D,
+                                            w["removalForceAmplitude"], w["removalForcekMin"],
+                                            w["removalForcekMax"])
+            else:
+                F = sf.turbulent_field(self.rho, self.u, self.shape, D, w["forceAmplitude"],
+                                       w["forcekMin"], w["forcekMax"],
+                                       w["removalForceAmplitude"], w["removalForcekMin"],
+                                       w["removalForcekMax"])
+            self.port.set_force_field(F)
+            self.port.step(1, store_last=False)
+
+
 def cpu_baseline_port(name: str, threads: int, seconds_budget: float = 20.0) -> dict:
     """The oracle port (C restatement of the reference path) on the host
     cores, on a bounded sample of the same workload."""
-    from oracle import ALPHA_REFERENCE, OracleConfig, OraclePort
     w = WORKLOADS[name]
     lat = w["latticeT"]
     side = 64 if lat == "D3Q27" else 96
     shape = (side, side, side)
-    rho, u = initial_field(name, shape)
-    cfg = OracleConfig(lattice=lat, collision="ELBM" if w["collisionT"] != "BGK" else "BGK",
-                       forcing=w.get("forcingSchemeT", "None"), force=w.get("forceT", "None"),
-                       tau=w["relaxationTime"], amplitude=w.get("forceAmplitude", (0, 0, 0)),
-                       wavelength=w.get("forceWaveLength", (1, 1, 1)),
-                       kolmogorov_axis=w.get("kolmogorovAxis", 1), size=shape,
-                       alpha_mode=ALPHA_REFERENCE, threads=threads)
-    port = OraclePort(cfg)
-    port.init_equilibrium(rho, u)
-    port.step(1, store_last=False)
+    run = PortRun(name, shape, threads)
+    run.step(1)
     steps, t0 = 0, time.perf_counter()
     while True:
-        port.step(1, store_last=False)
+        run.step(1)
         steps += 1
         dt = time.perf_counter() - t0
         if dt > seconds_budget or steps >= 50:
             break
     V = int(np.prod(shape))
+    extra = ", force field by numpy FFTs each step (1 thread)" if run.spectral else ""
     return {"value": V * steps / dt / 1e6, "unit": "MLUPS", "cores": threads, "kind": "port",
             "sample": f"{lat} {w['collisionT']} FP64, reference alpha solver, {side}^3, "
-                      f"{steps} steps after 1 warm-up, {threads} threads"}
+                      f"{steps} steps after 1 warm-up, {threads} threads{extra}"}
 
 
 # ---------------------------------------------------------------------------
@@ -315,12 +363,31 @@ def run_ours(args):
             "solver_stats_over": f"the {args.steps} timed steps",
         }
 
+    # --- spectral workloads: the same step kernel with the time-independent
+    # ConstantShell field (no per-step transforms) times the kernel alone;
+    # the difference is the per-step force update (momentum, D2Z, filter, Z2D)
+    kernel_ms = total_ms
+    if w.get("forceT") in SPECTRAL_FORCES and w["forceT"] != "ConstantShell":
+        lat = Lattice(deck_for(name, device=local, forceT="ConstantShell", **grid_over))
+        lat.init_equilibrium(rho, u)
+        lat.step(args.warmup)
+        kernel_ms, _ = time_steps(lat, args.steps, torch, dist)
+        lat.close()
+        kernel_ms = max_over_ranks(kernel_ms, dist, f"cuda:{local}")
+        extra["spectral_force"] = {
+            "force": w["forceT"],
+            "step_kernel_ms": kernel_ms / args.steps,
+            "force_update_ms": (total_ms - kernel_ms) / args.steps,
+            "what": "step kernel timed alone with the ConstantShell field (no per-step "
+                    "transforms); force_update_ms = ms_per_step - step_kernel_ms: momentum "
+                    "kernel, batched cuFFT D2Z, shell filter, batched Z2D"}
+
     value = job_value(V, args.steps, world, total_ms)
     pop_gb = V * {"D2Q9": 9, "D3Q19": 19, "D3Q27": 27}[deck.latticeT] * \
         {"f64": 8, "f32": 4, "f16_shifted": 2}[deck.storage] * 2 / 1e9
     peaks, peak_src = measured_peaks()
     bpn = w["bytes_per_node"]
-    avg_launch_ms = total_ms / args.steps
+    avg_launch_ms = kernel_ms / args.steps
     achieved = bpn * V / (avg_launch_ms * 1e-3) / 1e9
     # ncu figures of the dominant kernel (profiles/roofline_inputs.json, each
     # entry naming the profile summary it comes from): DRAM bytes per node of
@@ -460,21 +527,12 @@ def run_reference(args):
     name = args.workload
     w = WORKLOADS[name]
     threads = os.cpu_count() or 1
-    from oracle import ALPHA_REFERENCE, OracleConfig, OraclePort
     side = 96 if w["latticeT"] == "D3Q27" else 128
     shape = (side, side, side)
-    rho, u = initial_field(name, shape)
-    cfg = OracleConfig(lattice=w["latticeT"], collision="ELBM" if w["collisionT"] != "BGK" else "BGK",
-                       forcing=w.get("forcingSchemeT", "None"), force=w.get("forceT", "None"),
-                       tau=w["relaxationTime"], amplitude=w.get("forceAmplitude", (0, 0, 0)),
-                       wavelength=w.get("forceWaveLength", (1, 1, 1)),
-                       kolmogorov_axis=w.get("kolmogorovAxis", 1), size=shape,
-                       alpha_mode=ALPHA_REFERENCE, threads=threads)
-    port = OraclePort(cfg)
-    port.init_equilibrium(rho, u)
-    port.step(args.warmup, store_last=False)
+    run = PortRun(name, shape, threads)
+    run.step(args.warmup)
     t0 = time.perf_counter()
-    port.step(args.steps, store_last=False)
+    run.step(args.steps)
     dt = time.perf_counter() - t0
     V = int(np.prod(shape))
     value = V * args.steps / dt / 1e6
