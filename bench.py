@@ -413,10 +413,10 @@ def run_ours(args):
                                  "unit": "G FP64 instr/s", "frac": gops / prof["fp64_peak_gops"],
                                  "instructions_per_node": prof["fp64_inst_per_node"],
                                  "peak_source": "measured DFMA throughput (profiles/fp64_throughput_gb300.md)"}
-        if "fp64_pipe_busy_pct" in prof:
-            # ncu's FP64-pipe occupancy also counts the compares, conversions
-            # and reciprocal seeds that run on the pipe besides the arithmetic
-            roofline["fp64_pipe"]["pipe_busy_ncu"] = prof["fp64_pipe_busy_pct"] / 100.0
+    if "fp64_pipe_busy_pct" in prof:
+        # ncu's FP64-pipe occupancy also counts the compares, conversions
+        # and reciprocal seeds that run on the pipe besides the arithmetic
+        roofline.setdefault("fp64_pipe", {})["pipe_busy_ncu"] = prof["fp64_pipe_busy_pct"] / 100.0
 
     # --- end to end through the C ABI with host buffers (rank 0 reports)
     e2e = run_e2e(name, deck_l, rho, u, model if entropic else None, args.steps, args.warmup, torch,
