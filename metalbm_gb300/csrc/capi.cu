@@ -95,6 +95,9 @@ struct mlbm_handle {
   bool fields_valid = false;
   StepParams base{};
   SpectralForce* spectral = nullptr;  // spectral forces (FP64 storage)
+  // the stored fields changed since the time-dependent force was computed
+  // from them (its only inputs): recompute before the next step
+  bool force_stale = true;
   std::string error;
 };
 
@@ -479,6 +482,8 @@ extern "C" int mlbm_create(const mlbm_config* cfg, mlbm_handle** out) {
   }
   cudaMemsetAsync(h->f[0], 0, popBytes, h->stream);
   cudaMemsetAsync(h->f[1], 0, popBytes, h->stream);
+  // the stored fields start at zero (EnergyRemoval reads them before the
+  // first store or mlbm_init_equilibrium)
   cudaMemsetAsync(h->rho, 0, sizeof(double) * V, h->stream);
   cudaMemsetAsync(h->u, 0, sizeof(double) * V * D, h->stream);
   cudaMemsetAsync(h->force, 0, sizeof(double) * V * D, h->stream);
@@ -496,11 +501,6 @@ extern "C" int mlbm_create(const mlbm_config* cfg, mlbm_handle** out) {
       return bail(MLBM_ERR_CUDA);
     }
   }
-  // EnergyRemoval reads the stored fields before the first store: zero until
-  // mlbm_init_equilibrium fills them.
-  cudaMemsetAsync(h->rho, 0, sizeof(double) * V, h->stream);
-  cudaMemsetAsync(h->u, 0, sizeof(double) * V * D, h->stream);
-
   // Force profiles tabulated on the host (Force.h:208-215, 262-267).
   if (c.force == MLBM_FORCE_SINUSOIDAL || c.force == MLBM_FORCE_KOLMOGOROV) {
     const int ntab = c.force == MLBM_FORCE_SINUSOIDAL ? D : 1;
@@ -608,6 +608,7 @@ extern "C" int mlbm_init_equilibrium(mlbm_handle* h, const double* rho, const do
   if ((rc = fill_alpha(h, 2.0))) return rc;  // Initialize.h:82-89
   MLBM_CUDA(h, cudaStreamSynchronize(h->stream));
   h->fields_valid = false;
+  h->force_stale = true;
   return MLBM_OK;
 }
 
@@ -674,12 +675,14 @@ extern "C" int mlbm_step(mlbm_handle* h, int nsteps, unsigned int flags) {
     p.diag = last && (flags & MLBM_STEP_DIAGNOSTICS) ? 1 : 0;
     const void* prev = h->f[h->cur];
     void* next = h->f[1 - h->cur];
-    if (h->spectral && spectral_force_time_dependent(h->spectral)) {
+    if (h->spectral && spectral_force_time_dependent(h->spectral) && h->force_stale) {
       // Collision::update before the sweep (Algorithm.h:338): the force field
-      // from the last stored fields
+      // from the last stored fields. The reference recomputes it every step;
+      // between stores its inputs do not change, so neither does the field.
       char msg[256] = {0};
       if (spectral_force_update(h->spectral, h->rho, h->u, h->stream, msg, sizeof msg))
         return fail(h, MLBM_ERR_CUDA, "spectral force: %s", msg);
+      h->force_stale = false;
     }
     cudaError_t e = h->storage == MLBM_STORAGE_F64
                         ? step_f64(h->cfg.lattice, collision, h->cfg.forcing_scheme,
@@ -704,7 +707,10 @@ extern "C" int mlbm_step(mlbm_handle* h, int nsteps, unsigned int flags) {
     }
     h->cur = 1 - h->cur;  // std::swap(prev, next), Algorithm.h:336
     ++h->steps;
-    if (p.store) h->fields_valid = true;
+    if (p.store) {
+      h->fields_valid = true;
+      h->force_stale = true;
+    }
     if (p.diag) h->diag_valid = true;
   }
   return MLBM_OK;

@@ -24,8 +24,10 @@
 
 #include <cufft.h>
 
+#include <cmath>
 #include <cstdio>
 #include <new>
+#include <vector>
 
 #include "common.cuh"
 #include "kernels.h"
@@ -111,17 +113,205 @@ __global__ void removal_filter_kernel(SpecGrid g, cufftDoubleComplex* __restrict
   }
 }
 
+// ---- Removal on a small shell: separable partial transforms ----------------
+// The removal shell is a handful of modes (|k| <= K, K <= kSparseMaxK), so
+// instead of two full FP64 FFTs of D components (FP64-bound on GB300) the
+// momentum spectrum is formed only on the box [-KA, KA] x [-K, K] x [0, K]:
+// sums along the contiguous axis first (one warp per line), then along the
+// two others; the filtered modes go back the same way. The lattice is seen as
+// A x B x C with the halved axis C last: 3-D (lx, ly, lz), 2-D (1, lx, ly)
+// with KA = 0. Per node: D (K + 1) complex multiply-adds each way.
+constexpr int kSparseMaxK = 5;
+
+struct SepGrid {
+  int A, B, C, D, K, KA;
+  long long V;
+  const double2* twA;  // (cos, sin)(2 pi j / n), j < n
+  const double2* twB;
+  const double2* twC;
+};
+
+// e^{+2 pi i k j / n}
+__device__ __forceinline__ double2 twiddle(const double2* t, int k, int j, int n) {
+  const long long km = ((long long)k % n + n) % n;
+  return __ldg(t + (km * j) % n);
+}
+
+__device__ __forceinline__ double2 cmul(double2 a, double2 b) {
+  return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+__device__ __forceinline__ double2 cmul_conj(double2 a, double2 b) {  // a * conj(b)
+  return make_double2(a.x * b.x + a.y * b.y, a.y * b.x - a.x * b.y);
+}
+
+// P1[line][kc][d] = sum_c rho u_d e^{-2 pi i kc c / C}, one warp per line
+template <int K>
+__global__ void __launch_bounds__(256) sep_forward_c(SepGrid g, const double* __restrict__ rho,
+                                                     const double* __restrict__ u,
+                                                     double2* __restrict__ P1) {
+  const int lane = threadIdx.x & 31;
+  const long long line = (long long)blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5);
+  if (line >= (long long)g.A * g.B) return;  // uniform across the warp
+  double ar[3][K + 1], ai[3][K + 1];
+#pragma unroll
+  for (int d = 0; d < 3; ++d)
+#pragma unroll
+    for (int k = 0; k <= K; ++k) ar[d][k] = ai[d][k] = 0.0;
+  for (int c = lane; c < g.C; c += 32) {
+    const long long i = line * g.C + c;
+    const double r = rho[i];
+    double m[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) m[d] = d < g.D ? r * u[(long long)d * g.V + i] : 0.0;
+#pragma unroll
+    for (int k = 0; k <= K; ++k) {
+      const double2 w = twiddle(g.twC, k, c, g.C);
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        ar[d][k] += m[d] * w.x;
+        ai[d][k] -= m[d] * w.y;
+      }
+    }
+  }
+#pragma unroll
+  for (int d = 0; d < 3; ++d)
+#pragma unroll
+    for (int k = 0; k <= K; ++k)
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        ar[d][k] += __shfl_down_sync(0xffffffffu, ar[d][k], o);
+        ai[d][k] += __shfl_down_sync(0xffffffffu, ai[d][k], o);
+      }
+  if (lane == 0) {
+#pragma unroll
+    for (int k = 0; k <= K; ++k)
+#pragma unroll
+      for (int d = 0; d < 3; ++d)
+        if (d < g.D) P1[(line * (K + 1) + k) * g.D + d] = make_double2(ar[d][k], ai[d][k]);
+  }
+}
+
+// P2[a][kb][kc][d] = sum_b P1[a][b][kc][d] e^{-2 pi i kb b / B}
+__global__ void sep_forward_b(SepGrid g, const double2* __restrict__ P1, double2* __restrict__ P2) {
+  const int nk = 2 * g.K + 1, nc = g.K + 1;
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long long)g.A * nk * nc * g.D) return;
+  const int d = (int)(t % g.D);
+  const int kc = (int)((t / g.D) % nc);
+  const int kbi = (int)((t / ((long long)g.D * nc)) % nk);
+  const long long a = t / ((long long)g.D * nc * nk);
+  double2 acc = make_double2(0.0, 0.0);
+  for (int b = 0; b < g.B; ++b) {
+    const double2 v = P1[((a * g.B + b) * nc + kc) * g.D + d];
+    const double2 p = cmul_conj(v, twiddle(g.twB, kbi - g.K, b, g.B));
+    acc.x += p.x;
+    acc.y += p.y;
+  }
+  P2[t] = acc;
+}
+
+// modes of the box: sum over a, then the removal filter -A_d/V on the shell
+// (0 elsewhere), doubled for kc > 0 (each stands for k and -k)
+__global__ void sep_modes(SepGrid g, const double2* __restrict__ P2, double2* __restrict__ Ch,
+                          double rx, double ry, double rz, int kmin, int kmax, double inv_v) {
+  const int nk = 2 * g.K + 1, nc = g.K + 1, na = 2 * g.KA + 1;
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long long)na * nk * nc * g.D) return;
+  const int d = (int)(t % g.D);
+  const int kc = (int)((t / g.D) % nc);
+  const int kbi = (int)((t / ((long long)g.D * nc)) % nk);
+  const int kai = (int)(t / ((long long)g.D * nc * nk));
+  const int ka = kai - g.KA, kb = kbi - g.K;
+  double2 acc = make_double2(0.0, 0.0);
+  for (int a = 0; a < g.A; ++a) {
+    const double2 v = P2[(((long long)a * nk + kbi) * nc + kc) * g.D + d];
+    const double2 p = cmul_conj(v, twiddle(g.twA, ka, a, g.A));
+    acc.x += p.x;
+    acc.y += p.y;
+  }
+  const long long k2 = (long long)ka * ka + (long long)kb * kb + (long long)kc * kc;
+  const bool s = k2 >= (long long)kmin * kmin && k2 <= (long long)kmax * kmax;
+  const double amp = d == 0 ? rx : (d == 1 ? ry : rz);
+  const double c = s ? -amp * inv_v * (kc > 0 ? 2.0 : 1.0) : 0.0;
+  Ch[t] = make_double2(c * acc.x, c * acc.y);
+}
+
+// R1[a][kb][kc][d] = sum_ka Ch[ka][kb][kc][d] e^{+2 pi i ka a / A}
+__global__ void sep_inverse_a(SepGrid g, const double2* __restrict__ Ch, double2* __restrict__ R1) {
+  const int nk = 2 * g.K + 1, nc = g.K + 1, na = 2 * g.KA + 1;
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long long)g.A * nk * nc * g.D) return;
+  const long long inner = t % ((long long)nk * nc * g.D);  // (kb, kc, d)
+  const int a = (int)(t / ((long long)nk * nc * g.D));
+  double2 acc = make_double2(0.0, 0.0);
+  for (int kai = 0; kai < na; ++kai) {
+    const double2 p = cmul(Ch[(long long)kai * nk * nc * g.D + inner], twiddle(g.twA, kai - g.KA, a, g.A));
+    acc.x += p.x;
+    acc.y += p.y;
+  }
+  R1[t] = acc;
+}
+
+// R2[a][b][kc][d] = sum_kb R1[a][kb][kc][d] e^{+2 pi i kb b / B}
+__global__ void sep_inverse_b(SepGrid g, const double2* __restrict__ R1, double2* __restrict__ R2) {
+  const int nk = 2 * g.K + 1, nc = g.K + 1;
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long long)g.A * g.B * nc * g.D) return;
+  const int d = (int)(t % g.D);
+  const int kc = (int)((t / g.D) % nc);
+  const long long ab = t / ((long long)g.D * nc);
+  const int b = (int)(ab % g.B);
+  const long long a = ab / g.B;
+  double2 acc = make_double2(0.0, 0.0);
+  for (int kbi = 0; kbi < nk; ++kbi) {
+    const double2 p = cmul(R1[((a * nk + kbi) * nc + kc) * g.D + d], twiddle(g.twB, kbi - g.K, b, g.B));
+    acc.x += p.x;
+    acc.y += p.y;
+  }
+  R2[t] = acc;
+}
+
+// field_d = injection_d + Re sum_kc R2[line][kc][d] e^{+2 pi i kc c / C}
+template <int K>
+__global__ void __launch_bounds__(256) sep_synthesis(SepGrid g, const double2* __restrict__ R2,
+                                                     const double* __restrict__ inj,
+                                                     double* __restrict__ field) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= g.V) return;
+  const long long line = i / g.C;
+  const int c = (int)(i - line * g.C);
+  double2 w[K + 1];
+#pragma unroll
+  for (int k = 0; k <= K; ++k) w[k] = twiddle(g.twC, k, c, g.C);
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    if (d >= g.D) break;
+    double f = inj ? inj[(long long)d * g.V + i] : 0.0;
+#pragma unroll
+    for (int k = 0; k <= K; ++k) {
+      const double2 z = __ldg(R2 + (line * (K + 1) + k) * g.D + d);
+      f += z.x * w[k].x - z.y * w[k].y;
+    }
+    field[(long long)d * g.V + i] = f;
+  }
+}
+
 struct SpectralForce {
   int force = 0;
   SpecGrid g{};
   long long V = 0;
   bool time_dependent = false;
+  bool sparse = false;                   // removal by the separable partial transforms
   cufftHandle fwd = 0, inv = 0;
   bool have_fwd = false, have_inv = false;
-  cufftDoubleComplex* spec = nullptr;    // [D][nspec] work spectrum
-  cufftDoubleComplex* inject = nullptr;  // [D][nspec] injection spectrum (Turbulent2D)
+  cufftDoubleComplex* spec = nullptr;    // [D][nspec] work spectrum (cuFFT removal)
+  cufftDoubleComplex* inject = nullptr;  // [D][nspec] injection spectrum (cuFFT removal)
+  double* inj_field = nullptr;           // [D][V] injection field (separable removal)
   double* mom = nullptr;                 // [D][V]
   double* field = nullptr;               // [D][V]
+  SepGrid sg{};
+  double2* tw = nullptr;                 // twiddle tables A | B | C
+  double2 *P1 = nullptr, *P2 = nullptr, *Ch = nullptr, *R1 = nullptr, *R2 = nullptr;
   double ramp[3] = {0, 0, 0};
   int rkmin = 0, rkmax = 0;
 };
@@ -135,10 +325,9 @@ void spectral_force_destroy(SpectralForce* sf) {
   if (!sf) return;
   if (sf->have_fwd) cufftDestroy(sf->fwd);
   if (sf->have_inv) cufftDestroy(sf->inv);
-  cudaFree(sf->spec);
-  cudaFree(sf->inject);
-  cudaFree(sf->mom);
-  cudaFree(sf->field);
+  void* ptrs[] = {sf->spec, sf->inject, sf->inj_field, sf->mom, sf->field, sf->tw,
+                  sf->P1, sf->P2, sf->Ch, sf->R1, sf->R2};
+  for (void* p : ptrs) cudaFree(p);
   delete sf;
 }
 
@@ -146,6 +335,45 @@ const double* spectral_force_field(const SpectralForce* sf) { return sf->field; 
 bool spectral_force_time_dependent(const SpectralForce* sf) { return sf->time_dependent; }
 
 static unsigned blocks_for(long long n) { return (unsigned)((n + 255) / 256); }
+
+// (cos, sin)(2 pi j / n) rounded from extended precision
+static void twiddle_table(std::vector<double2>& t, int n) {
+  const long double two_pi = 6.283185307179586476925286766559005768L;
+  for (int j = 0; j < n; ++j) {
+    const long double x = two_pi * (long double)j / (long double)n;
+    t.push_back(make_double2((double)std::cos(x), (double)std::sin(x)));
+  }
+}
+
+static int setup_sparse(SpectralForce* sf, char* err, size_t errlen) {
+  const SpecGrid& g = sf->g;
+  SepGrid& s = sf->sg;
+  s.D = g.D;
+  s.V = sf->V;
+  if (g.D == 2) { s.A = 1; s.B = g.lx; s.C = g.ly; } else { s.A = g.lx; s.B = g.ly; s.C = g.lz; }
+  s.K = sf->rkmax;
+  s.KA = g.D == 2 ? 0 : s.K;
+  std::vector<double2> t;
+  twiddle_table(t, s.A);
+  twiddle_table(t, s.B);
+  twiddle_table(t, s.C);
+  const long long nk = 2 * s.K + 1, nc = s.K + 1, na = 2 * s.KA + 1;
+  cudaError_t e;
+  if ((e = cudaMalloc(&sf->tw, sizeof(double2) * t.size())) != cudaSuccess ||
+      (e = cudaMalloc(&sf->P1, sizeof(double2) * s.A * s.B * nc * s.D)) != cudaSuccess ||
+      (e = cudaMalloc(&sf->R2, sizeof(double2) * s.A * s.B * nc * s.D)) != cudaSuccess ||
+      (e = cudaMalloc(&sf->P2, sizeof(double2) * s.A * nk * nc * s.D)) != cudaSuccess ||
+      (e = cudaMalloc(&sf->R1, sizeof(double2) * s.A * nk * nc * s.D)) != cudaSuccess ||
+      (e = cudaMalloc(&sf->Ch, sizeof(double2) * na * nk * nc * s.D)) != cudaSuccess)
+    return sf_fail(err, errlen, "device allocation failed", (int)e);
+  if ((e = cudaMemcpy(sf->tw, t.data(), sizeof(double2) * t.size(), cudaMemcpyHostToDevice)) !=
+      cudaSuccess)
+    return sf_fail(err, errlen, "twiddle upload failed", (int)e);
+  s.twA = sf->tw;
+  s.twB = sf->tw + s.A;
+  s.twC = sf->tw + s.A + s.B;
+  return 0;
+}
 
 int spectral_force_create(SpectralForce** out, int force, int D, int lx, int ly, int lz,
                           const double amp[3], int kmin, int kmax, const double ramp[3],
@@ -163,87 +391,123 @@ int spectral_force_create(SpectralForce** out, int force, int D, int lx, int ly,
   g.nspec = (long long)g.hx * g.hy * g.hz;
   sf->V = (long long)lx * ly * g.lz;
   sf->time_dependent = force != MLBM_FORCE_CONSTANT_SHELL;
+  sf->sparse = sf->time_dependent && rkmax <= kSparseMaxK;
   for (int d = 0; d < 3; ++d) sf->ramp[d] = ramp[d];
   sf->rkmin = rkmin;
   sf->rkmax = rkmax;
   const double scale = 1.0 / (double)sf->V;
+  const bool injection = force != MLBM_FORCE_ENERGY_REMOVAL;
+  auto bail = [&](const char* what, int code) {
+    spectral_force_destroy(sf);
+    return sf_fail(err, errlen, what, code);
+  };
 
+  cudaError_t e;
+  if ((e = cudaMalloc(&sf->field, sizeof(double) * sf->V * D)) != cudaSuccess)
+    return bail("device allocation failed", (int)e);
   int n[3] = {lx, ly, lz};
   cufftResult r;
-  if ((r = cufftPlanMany(&sf->inv, D, n, nullptr, 1, (int)g.nspec, nullptr, 1, (int)sf->V,
-                         CUFFT_Z2D, D)) != CUFFT_SUCCESS) {
-    spectral_force_destroy(sf);
-    return sf_fail(err, errlen, "cufftPlanMany Z2D failed", (int)r);
+  const bool need_inv = injection || !sf->sparse;
+  if (need_inv) {
+    if ((r = cufftPlanMany(&sf->inv, D, n, nullptr, 1, (int)g.nspec, nullptr, 1, (int)sf->V,
+                           CUFFT_Z2D, D)) != CUFFT_SUCCESS)
+      return bail("cufftPlanMany Z2D failed", (int)r);
+    sf->have_inv = true;
+    cufftSetStream(sf->inv, s);
+    if ((e = cudaMalloc(&sf->spec, sizeof(cufftDoubleComplex) * g.nspec * D)) != cudaSuccess)
+      return bail("device allocation failed", (int)e);
   }
-  sf->have_inv = true;
-  cufftSetStream(sf->inv, s);
-  cudaError_t e;
-  if ((e = cudaMalloc(&sf->spec, sizeof(cufftDoubleComplex) * g.nspec * D)) != cudaSuccess ||
-      (e = cudaMalloc(&sf->field, sizeof(double) * sf->V * D)) != cudaSuccess) {
-    spectral_force_destroy(sf);
-    return sf_fail(err, errlen, "device allocation failed", (int)e);
-  }
-  const bool injection = force != MLBM_FORCE_ENERGY_REMOVAL;
   if (injection) {
     shell_injection_kernel<<<blocks_for(g.nspec), 256, 0, s>>>(g, amp[0], amp[1], amp[2], kmin,
                                                                kmax, scale, sf->spec);
     count_launches(1);
   }
-  if (force == MLBM_FORCE_CONSTANT_SHELL) {
-    // time-independent: one backward transform, then only the field is kept
-    if ((r = cufftExecZ2D(sf->inv, sf->spec, sf->field)) != CUFFT_SUCCESS) {
-      spectral_force_destroy(sf);
-      return sf_fail(err, errlen, "cufftExecZ2D failed", (int)r);
+  if (force == MLBM_FORCE_CONSTANT_SHELL || (injection && sf->sparse)) {
+    // the injection field, transformed back once
+    double* dst = force == MLBM_FORCE_CONSTANT_SHELL ? sf->field : nullptr;
+    if (!dst) {
+      if ((e = cudaMalloc(&sf->inj_field, sizeof(double) * sf->V * D)) != cudaSuccess)
+        return bail("device allocation failed", (int)e);
+      dst = sf->inj_field;
     }
-    cudaStreamSynchronize(s);
+    if ((r = cufftExecZ2D(sf->inv, sf->spec, dst)) != CUFFT_SUCCESS)
+      return bail("cufftExecZ2D failed", (int)r);
+  }
+  if (sf->sparse) {
+    if (setup_sparse(sf, err, errlen)) {
+      spectral_force_destroy(sf);
+      return 1;
+    }
+  } else if (sf->time_dependent) {
+    if ((r = cufftPlanMany(&sf->fwd, D, n, nullptr, 1, (int)sf->V, nullptr, 1, (int)g.nspec,
+                           CUFFT_D2Z, D)) != CUFFT_SUCCESS)
+      return bail("cufftPlanMany D2Z failed", (int)r);
+    sf->have_fwd = true;
+    cufftSetStream(sf->fwd, s);
+    if ((e = cudaMalloc(&sf->mom, sizeof(double) * sf->V * D)) != cudaSuccess)
+      return bail("device allocation failed", (int)e);
+    if (injection) {
+      // the injection spectrum is kept: Z2D overwrites its input every step
+      if ((e = cudaMalloc(&sf->inject, sizeof(cufftDoubleComplex) * g.nspec * D)) != cudaSuccess)
+        return bail("device allocation failed", (int)e);
+      cudaMemcpyAsync(sf->inject, sf->spec, sizeof(cufftDoubleComplex) * g.nspec * D,
+                      cudaMemcpyDeviceToDevice, s);
+    }
+  }
+  if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return bail("spectral setup failed", (int)e);
+  if (sf->sparse || !sf->time_dependent) {
+    // the spectrum buffer and inverse plan served the injection only
     cudaFree(sf->spec);
     sf->spec = nullptr;
-    *out = sf;
-    return 0;
-  }
-  if ((r = cufftPlanMany(&sf->fwd, D, n, nullptr, 1, (int)sf->V, nullptr, 1, (int)g.nspec,
-                         CUFFT_D2Z, D)) != CUFFT_SUCCESS) {
-    spectral_force_destroy(sf);
-    return sf_fail(err, errlen, "cufftPlanMany D2Z failed", (int)r);
-  }
-  sf->have_fwd = true;
-  cufftSetStream(sf->fwd, s);
-  if ((e = cudaMalloc(&sf->mom, sizeof(double) * sf->V * D)) != cudaSuccess) {
-    spectral_force_destroy(sf);
-    return sf_fail(err, errlen, "device allocation failed", (int)e);
-  }
-  if (injection) {
-    // the injection spectrum is kept: Z2D overwrites its input every step
-    if ((e = cudaMalloc(&sf->inject, sizeof(cufftDoubleComplex) * g.nspec * D)) != cudaSuccess) {
-      spectral_force_destroy(sf);
-      return sf_fail(err, errlen, "device allocation failed", (int)e);
-    }
-    cudaMemcpyAsync(sf->inject, sf->spec, sizeof(cufftDoubleComplex) * g.nspec * D,
-                    cudaMemcpyDeviceToDevice, s);
-  }
-  if ((e = cudaStreamSynchronize(s)) != cudaSuccess) {
-    spectral_force_destroy(sf);
-    return sf_fail(err, errlen, "injection spectrum failed", (int)e);
+    if (sf->have_inv) cufftDestroy(sf->inv);
+    sf->have_inv = false;
   }
   *out = sf;
   return 0;
 }
 
+template <int K>
+static void launch_sparse(SpectralForce* sf, const double* rho, const double* u, cudaStream_t s) {
+  const SepGrid& g = sf->sg;
+  const long long lines = (long long)g.A * g.B;
+  sep_forward_c<K><<<(unsigned)((lines + 7) / 8), 256, 0, s>>>(g, rho, u, sf->P1);
+  const long long nk = 2 * g.K + 1, nc = g.K + 1, na = 2 * g.KA + 1;
+  sep_forward_b<<<blocks_for(g.A * nk * nc * g.D), 256, 0, s>>>(g, sf->P1, sf->P2);
+  sep_modes<<<blocks_for(na * nk * nc * g.D), 256, 0, s>>>(
+      g, sf->P2, sf->Ch, sf->ramp[0], sf->ramp[1], sf->ramp[2], sf->rkmin, sf->rkmax,
+      1.0 / (double)sf->V);
+  sep_inverse_a<<<blocks_for(g.A * nk * nc * g.D), 256, 0, s>>>(g, sf->Ch, sf->R1);
+  sep_inverse_b<<<blocks_for(lines * nc * g.D), 256, 0, s>>>(g, sf->R1, sf->R2);
+  sep_synthesis<K><<<blocks_for(g.V), 256, 0, s>>>(g, sf->R2, sf->inj_field, sf->field);
+  count_launches(6);
+}
+
 int spectral_force_update(SpectralForce* sf, const double* rho, const double* u, cudaStream_t s,
                           char* err, size_t errlen) {
   if (!sf->time_dependent) return 0;
-  const SpecGrid& g = sf->g;
-  momentum_kernel<<<blocks_for(sf->V), 256, 0, s>>>(rho, u, sf->mom, g.D, sf->V);
-  count_launches(1);
-  cufftResult r;
-  if ((r = cufftExecD2Z(sf->fwd, sf->mom, sf->spec)) != CUFFT_SUCCESS)
-    return sf_fail(err, errlen, "cufftExecD2Z failed", (int)r);
-  removal_filter_kernel<<<blocks_for(g.nspec), 256, 0, s>>>(
-      g, sf->spec, sf->inject, sf->ramp[0], sf->ramp[1], sf->ramp[2], sf->rkmin, sf->rkmax,
-      1.0 / (double)sf->V);
-  count_launches(1);
-  if ((r = cufftExecZ2D(sf->inv, sf->spec, sf->field)) != CUFFT_SUCCESS)
-    return sf_fail(err, errlen, "cufftExecZ2D failed", (int)r);
+  if (sf->sparse) {
+    switch (sf->sg.K) {
+      case 0: launch_sparse<0>(sf, rho, u, s); break;
+      case 1: launch_sparse<1>(sf, rho, u, s); break;
+      case 2: launch_sparse<2>(sf, rho, u, s); break;
+      case 3: launch_sparse<3>(sf, rho, u, s); break;
+      case 4: launch_sparse<4>(sf, rho, u, s); break;
+      default: launch_sparse<5>(sf, rho, u, s); break;
+    }
+  } else {
+    const SpecGrid& g = sf->g;
+    momentum_kernel<<<blocks_for(sf->V), 256, 0, s>>>(rho, u, sf->mom, g.D, sf->V);
+    count_launches(1);
+    cufftResult r;
+    if ((r = cufftExecD2Z(sf->fwd, sf->mom, sf->spec)) != CUFFT_SUCCESS)
+      return sf_fail(err, errlen, "cufftExecD2Z failed", (int)r);
+    removal_filter_kernel<<<blocks_for(g.nspec), 256, 0, s>>>(
+        g, sf->spec, sf->inject, sf->ramp[0], sf->ramp[1], sf->ramp[2], sf->rkmin, sf->rkmax,
+        1.0 / (double)sf->V);
+    count_launches(1);
+    if ((r = cufftExecZ2D(sf->inv, sf->spec, sf->field)) != CUFFT_SUCCESS)
+      return sf_fail(err, errlen, "cufftExecZ2D failed", (int)r);
+  }
   const cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return sf_fail(err, errlen, cudaGetErrorString(e), (int)e);
   return 0;
