@@ -74,6 +74,12 @@ WORKLOADS = {
                                     removalForceAmplitude=(1e-6, 1e-6, 1e-6), removalForcekMin=1,
                                     removalForcekMax=2, globalLength=(256, 256, 256),
                                     storage="f64", bytes_per_node=2 * 27 * 8 + 3 * 8),
+    "turbulent_d3q27_f32_256": dict(latticeT="D3Q27", collisionT="BGK", relaxationTime=0.55,
+                                    forcingSchemeT="ExactDifferenceMethod", forceT="Turbulent2D",
+                                    forceAmplitude=(1e-6, 1e-6, 1e-6), forcekMin=1, forcekMax=2,
+                                    removalForceAmplitude=(1e-6, 1e-6, 1e-6), removalForcekMin=1,
+                                    removalForcekMax=2, globalLength=(256, 256, 256),
+                                    storage="f32", bytes_per_node=2 * 27 * 4 + 3 * 4),
 }
 
 SPECTRAL_FORCES = ("ConstantShell", "EnergyRemoval", "Turbulent2D")

@@ -69,8 +69,9 @@ enum {
 };
 enum { MLBM_FORCING_NONE = 0, MLBM_FORCING_GUO = 1, MLBM_FORCING_SHAN_CHEN = 2,
        MLBM_FORCING_EXACT_DIFFERENCE = 3 };                         /* ForcingSchemeType */
-/* ForceType (Options.h:39-41). The spectral forces (Force.h:294-626) run with
- * FP64 storage; their shells use force_kmin/force_kmax and, for the removal
+/* ForceType (Options.h:39-41). The spectral forces (Force.h:294-626) are a
+ * per-node force field computed on the device (FP64; a float copy for FP32 /
+ * FP16 storage); their shells use force_kmin/force_kmax and, for the removal
  * part, removal_amplitude / removal_kmin / removal_kmax:
  *   CONSTANT_SHELL  time-independent solenoidal forcing on the shell
  *                   kmin <= |k| <= kmax (curl of a constant-amplitude spectrum)

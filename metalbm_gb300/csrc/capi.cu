@@ -377,8 +377,6 @@ extern "C" int mlbm_create(const mlbm_config* cfg, mlbm_handle** out) {
 
   const bool spectral = c.force >= MLBM_FORCE_CONSTANT_SHELL;
   if (spectral) {
-    if (c.storage != MLBM_STORAGE_F64)
-      return fail(nullptr, MLBM_ERR_INVALID, "the spectral forces run with FP64 storage");
     long long lmin = L[0];
     for (int d = 1; d < D; ++d) lmin = std::min(lmin, L[d]);
     const bool inj = c.force != MLBM_FORCE_ENERGY_REMOVAL, rem = c.force != MLBM_FORCE_CONSTANT_SHELL;
@@ -496,7 +494,8 @@ extern "C" int mlbm_create(const mlbm_config* cfg, mlbm_handle** out) {
     char msg[256] = {0};
     if (spectral_force_create(&h->spectral, c.force, D, (int)L[0], (int)L[1], (int)L[2],
                               c.force_amplitude, c.force_kmin, c.force_kmax, c.removal_amplitude,
-                              c.removal_kmin, c.removal_kmax, h->stream, msg, sizeof msg)) {
+                              c.removal_kmin, c.removal_kmax, c.storage != MLBM_STORAGE_F64,
+                              h->stream, msg, sizeof msg)) {
       h->error = std::string("spectral force: ") + msg;
       return bail(MLBM_ERR_CUDA);
     }
@@ -541,6 +540,7 @@ extern "C" int mlbm_create(const mlbm_config* cfg, mlbm_handle** out) {
   }
   p.force_type = spectral ? FORCE_FIELD : c.force;
   p.force_field = spectral ? spectral_force_field(h->spectral) : nullptr;
+  p.force_field_f = spectral ? spectral_force_field_f(h->spectral) : nullptr;
   p.kol_axis = c.kolmogorov_axis;
   p.kol_comp = c.kolmogorov_component;
   for (int d = 0; d < 3; ++d) p.amp[d] = d < D ? c.force_amplitude[d] : 0.0;

@@ -51,6 +51,7 @@ struct StepParams {
   double amp[3];
   const double* force_table[3];  // per-axis host-computed sin profiles (device)
   const double* force_field;     // [D][V] per-node force of FORCE_FIELD (device)
+  const float* force_field_f;    // its float copy (FP32/FP16 storage)
   // float copies for the low-precision kernels, which execute no FP64
   // instruction on their common path (a double->float conversion runs on
   // GB300's narrow FP64 pipe)

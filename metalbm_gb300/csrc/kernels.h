@@ -82,12 +82,15 @@ cudaError_t log_samples(int lattice, int storage, const void* prev, const StepPa
 // message to err.
 void count_launches(unsigned n);
 struct SpectralForce;
+// want_float: also keep a float copy of the field (FP32/FP16 storage).
 int spectral_force_create(SpectralForce** out, int force, int D, int lx, int ly, int lz,
                           const double amp[3], int kmin, int kmax, const double ramp[3],
-                          int rkmin, int rkmax, cudaStream_t s, char* err, size_t errlen);
+                          int rkmin, int rkmax, int want_float, cudaStream_t s, char* err,
+                          size_t errlen);
 int spectral_force_update(SpectralForce* sf, const double* rho, const double* u, cudaStream_t s,
                           char* err, size_t errlen);
 const double* spectral_force_field(const SpectralForce* sf);
+const float* spectral_force_field_f(const SpectralForce* sf);
 bool spectral_force_time_dependent(const SpectralForce* sf);
 void spectral_force_destroy(SpectralForce* sf);
 

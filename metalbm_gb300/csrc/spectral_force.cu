@@ -296,6 +296,14 @@ __global__ void __launch_bounds__(256) sep_synthesis(SepGrid g, const double2* _
   }
 }
 
+// float copy of the field for the FP32/FP16-storage kernels (integer-bit
+// rounding: conversion instructions run on the narrow FP64 path)
+__global__ void narrow_field_kernel(const double* __restrict__ in, float* __restrict__ out,
+                                    long long n) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = narrow_rn(in[i]);
+}
+
 struct SpectralForce {
   int force = 0;
   SpecGrid g{};
@@ -309,6 +317,7 @@ struct SpectralForce {
   double* inj_field = nullptr;           // [D][V] injection field (separable removal)
   double* mom = nullptr;                 // [D][V]
   double* field = nullptr;               // [D][V]
+  float* field_f = nullptr;              // [D][V] float copy, or null
   SepGrid sg{};
   double2* tw = nullptr;                 // twiddle tables A | B | C
   double2 *P1 = nullptr, *P2 = nullptr, *Ch = nullptr, *R1 = nullptr, *R2 = nullptr;
@@ -325,13 +334,14 @@ void spectral_force_destroy(SpectralForce* sf) {
   if (!sf) return;
   if (sf->have_fwd) cufftDestroy(sf->fwd);
   if (sf->have_inv) cufftDestroy(sf->inv);
-  void* ptrs[] = {sf->spec, sf->inject, sf->inj_field, sf->mom, sf->field, sf->tw,
+  void* ptrs[] = {sf->spec, sf->inject, sf->inj_field, sf->mom, sf->field, sf->field_f, sf->tw,
                   sf->P1, sf->P2, sf->Ch, sf->R1, sf->R2};
   for (void* p : ptrs) cudaFree(p);
   delete sf;
 }
 
 const double* spectral_force_field(const SpectralForce* sf) { return sf->field; }
+const float* spectral_force_field_f(const SpectralForce* sf) { return sf->field_f; }
 bool spectral_force_time_dependent(const SpectralForce* sf) { return sf->time_dependent; }
 
 static unsigned blocks_for(long long n) { return (unsigned)((n + 255) / 256); }
@@ -375,9 +385,17 @@ static int setup_sparse(SpectralForce* sf, char* err, size_t errlen) {
   return 0;
 }
 
+static void narrow_field(SpectralForce* sf, cudaStream_t s) {
+  if (!sf->field_f) return;
+  const long long n = sf->V * sf->g.D;
+  narrow_field_kernel<<<blocks_for(n), 256, 0, s>>>(sf->field, sf->field_f, n);
+  count_launches(1);
+}
+
 int spectral_force_create(SpectralForce** out, int force, int D, int lx, int ly, int lz,
                           const double amp[3], int kmin, int kmax, const double ramp[3],
-                          int rkmin, int rkmax, cudaStream_t s, char* err, size_t errlen) {
+                          int rkmin, int rkmax, int want_float, cudaStream_t s, char* err,
+                          size_t errlen) {
   *out = nullptr;
   SpectralForce* sf = new (std::nothrow) SpectralForce();
   if (!sf) return sf_fail(err, errlen, "host allocation failed", 0);
@@ -403,7 +421,8 @@ int spectral_force_create(SpectralForce** out, int force, int D, int lx, int ly,
   };
 
   cudaError_t e;
-  if ((e = cudaMalloc(&sf->field, sizeof(double) * sf->V * D)) != cudaSuccess)
+  if ((e = cudaMalloc(&sf->field, sizeof(double) * sf->V * D)) != cudaSuccess ||
+      (want_float && (e = cudaMalloc(&sf->field_f, sizeof(float) * sf->V * D)) != cudaSuccess))
     return bail("device allocation failed", (int)e);
   int n[3] = {lx, ly, lz};
   cufftResult r;
@@ -432,6 +451,7 @@ int spectral_force_create(SpectralForce** out, int force, int D, int lx, int ly,
     }
     if ((r = cufftExecZ2D(sf->inv, sf->spec, dst)) != CUFFT_SUCCESS)
       return bail("cufftExecZ2D failed", (int)r);
+    if (dst == sf->field) narrow_field(sf, s);
   }
   if (sf->sparse) {
     if (setup_sparse(sf, err, errlen)) {
@@ -508,6 +528,7 @@ int spectral_force_update(SpectralForce* sf, const double* rho, const double* u,
     if ((r = cufftExecZ2D(sf->inv, sf->spec, sf->field)) != CUFFT_SUCCESS)
       return sf_fail(err, errlen, "cufftExecZ2D failed", (int)r);
   }
+  narrow_field(sf, s);
   const cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return sf_fail(err, errlen, cudaGetErrorString(e), (int)e);
   return 0;

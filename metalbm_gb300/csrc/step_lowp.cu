@@ -314,6 +314,12 @@ __device__ __forceinline__ void node_force_float(const StepParams& p, uint32_t x
       F[2] = p.kol_comp == 2 ? v : 0.0f;
       break;
     }
+    case FORCE_FIELD: {  // Force<Generic>::setForce (Force.h:36-45), float copy
+      const uint32_t i = (x * p.ly + y) * p.lz + z;
+#pragma unroll
+      for (int d = 0; d < D; ++d) F[d] = __ldg(p.force_field_f + (long long)d * p.V + i);
+      break;
+    }
     default:
       break;
   }

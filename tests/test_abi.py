@@ -119,12 +119,12 @@ def test_new_lattices_run_with_fp64_storage_only(lib):
 
 
 def test_spectral_force_configurations_are_checked(lib):
-    """Spectral forces: FP64 storage only, shells 0 <= kmin <= kmax with
-    2 kmax below the shortest length; refused before any device work."""
+    """Spectral forces: shells 0 <= kmin <= kmax with 2 kmax below the
+    shortest length; refused before any device work."""
     from metalbm_gb300 import capi
     h = ct.c_void_p()
-    cases = [(dict(storage=capi.STORAGE_F32), b"FP64 storage"),
-             (dict(force_kmax=8), b"spectral shell"),
+    cases = [(dict(force_kmax=8), b"spectral shell"),
+             (dict(removal_kmax=8), b"spectral shell"),
              (dict(force_kmin=3, force_kmax=2), b"spectral shell")]
     for kw, msg in cases:
         c = capi.Config()

@@ -156,3 +156,31 @@ def test_time_dependent_spectral_force_matches_oracle(lattice, shape, force, rkm
     assert np.abs(fl["force"] - pf["force"]).max() <= 1e-12 * np.abs(pf["force"]).max()
     assert _rel(f, port.populations()) <= TOL_F
     assert np.abs(pf["force"]).max() > 0
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("storage,tol", [("f32", 2e-4), ("f16_shifted", 5e-3)])
+@pytest.mark.parametrize("lattice,collision,force", [("D3Q27", "BGK", "ConstantShell"),
+                                                     ("D3Q19", "BGK", "Turbulent2D"),
+                                                     ("D2Q9", "ELBM", "EnergyRemoval")])
+def test_spectral_force_low_precision_storage(storage, tol, lattice, collision, force):
+    """FP32 / FP16-shifted storage read a float copy of the force field; u
+    tracks the FP64-storage run within the storage tolerances of the other
+    forces (test_low_precision_storage_tracks_f64), and the stored force field
+    (FP64, from the stored fields) is the same to rounding."""
+    from metalbm_gb300 import Lattice, fields
+    D = 2 if lattice.startswith("D2") else 3
+    shape = (16, 12, 10) if D == 3 else (32, 24, 1)
+    rho, u = fields.perturbed_rest(shape, D, 0.02, seed=4, rho_amplitude=0.005)
+    out = {}
+    for st in ("f64", storage):
+        deck = _deck(lattice, force, shape, forceAmplitude=(1e-4, -5e-5, 2e-5), forcekMin=1,
+                     forcekMax=3, removalForceAmplitude=(0.05, 0.05, 0.05), storage=st,
+                     collisionT=collision, tau=0.6 if collision == "BGK" else 0.52)
+        with Lattice(deck) as lat:
+            lat.init_equilibrium(rho, u)
+            for _ in range(4):
+                lat.step(5, store=True)
+            out[st] = lat.fields()
+    assert _rel(out[storage]["u"], out["f64"]["u"]) <= tol
+    assert _rel(out[storage]["force"], out["f64"]["force"]) <= tol
