@@ -157,6 +157,13 @@ __global__ void __launch_bounds__(256) sep_forward_c(SepGrid g, const double* __
   for (int d = 0; d < 3; ++d)
 #pragma unroll
     for (int k = 0; k <= K; ++k) ar[d][k] = ai[d][k] = 0.0;
+  // running twiddle indices (k c) mod C, advanced by (32 k) mod C per stride
+  int idx[K + 1], step[K + 1];
+#pragma unroll
+  for (int k = 0; k <= K; ++k) {
+    idx[k] = (k * lane) % g.C;
+    step[k] = (32 * k) % g.C;
+  }
   for (int c = lane; c < g.C; c += 32) {
     const long long i = line * g.C + c;
     const double r = rho[i];
@@ -164,13 +171,20 @@ __global__ void __launch_bounds__(256) sep_forward_c(SepGrid g, const double* __
 #pragma unroll
     for (int d = 0; d < 3; ++d) m[d] = d < g.D ? r * u[(long long)d * g.V + i] : 0.0;
 #pragma unroll
-    for (int k = 0; k <= K; ++k) {
-      const double2 w = twiddle(g.twC, k, c, g.C);
+    for (int d = 0; d < 3; ++d) ar[d][0] += m[d];  // k = 0: twiddle 1
+#pragma unroll
+    for (int k = 1; k <= K; ++k) {
+      const double2 w = __ldg(g.twC + idx[k]);
 #pragma unroll
       for (int d = 0; d < 3; ++d) {
         ar[d][k] += m[d] * w.x;
         ai[d][k] -= m[d] * w.y;
       }
+    }
+#pragma unroll
+    for (int k = 1; k <= K; ++k) {
+      idx[k] += step[k];
+      if (idx[k] >= g.C) idx[k] -= g.C;
     }
   }
 #pragma unroll
@@ -201,11 +215,15 @@ __global__ void sep_forward_b(SepGrid g, const double2* __restrict__ P1, double2
   const int kbi = (int)((t / ((long long)g.D * nc)) % nk);
   const long long a = t / ((long long)g.D * nc * nk);
   double2 acc = make_double2(0.0, 0.0);
+  const int kbm = ((kbi - g.K) % g.B + g.B) % g.B;
+  int e = 0;  // (kb b) mod B
   for (int b = 0; b < g.B; ++b) {
     const double2 v = P1[((a * g.B + b) * nc + kc) * g.D + d];
-    const double2 p = cmul_conj(v, twiddle(g.twB, kbi - g.K, b, g.B));
+    const double2 p = cmul_conj(v, __ldg(g.twB + e));
     acc.x += p.x;
     acc.y += p.y;
+    e += kbm;
+    if (e >= g.B) e -= g.B;
   }
   P2[t] = acc;
 }
@@ -223,11 +241,15 @@ __global__ void sep_modes(SepGrid g, const double2* __restrict__ P2, double2* __
   const int kai = (int)(t / ((long long)g.D * nc * nk));
   const int ka = kai - g.KA, kb = kbi - g.K;
   double2 acc = make_double2(0.0, 0.0);
+  const int kam = (ka % g.A + g.A) % g.A;
+  int e = 0;  // (ka a) mod A
   for (int a = 0; a < g.A; ++a) {
     const double2 v = P2[(((long long)a * nk + kbi) * nc + kc) * g.D + d];
-    const double2 p = cmul_conj(v, twiddle(g.twA, ka, a, g.A));
+    const double2 p = cmul_conj(v, __ldg(g.twA + e));
     acc.x += p.x;
     acc.y += p.y;
+    e += kam;
+    if (e >= g.A) e -= g.A;
   }
   const long long k2 = (long long)ka * ka + (long long)kb * kb + (long long)kc * kc;
   const bool s = k2 >= (long long)kmin * kmin && k2 <= (long long)kmax * kmax;
@@ -281,14 +303,20 @@ __global__ void __launch_bounds__(256) sep_synthesis(SepGrid g, const double2* _
   const long long line = i / g.C;
   const int c = (int)(i - line * g.C);
   double2 w[K + 1];
+  int e = 0;  // (k c) mod C, by repeated addition of c < C
 #pragma unroll
-  for (int k = 0; k <= K; ++k) w[k] = twiddle(g.twC, k, c, g.C);
+  for (int k = 1; k <= K; ++k) {
+    e += c;
+    if (e >= g.C) e -= g.C;
+    w[k] = __ldg(g.twC + e);
+  }
 #pragma unroll
   for (int d = 0; d < 3; ++d) {
     if (d >= g.D) break;
     double f = inj ? inj[(long long)d * g.V + i] : 0.0;
+    f += __ldg(R2 + (line * (K + 1)) * g.D + d).x;  // k = 0: twiddle 1
 #pragma unroll
-    for (int k = 0; k <= K; ++k) {
+    for (int k = 1; k <= K; ++k) {
       const double2 z = __ldg(R2 + (line * (K + 1) + k) * g.D + d);
       f += z.x * w[k].x - z.y * w[k].y;
     }
