@@ -92,12 +92,19 @@ int scratch_for_current_device(Scratch** out) {
 
 }  // namespace
 
+// ((1 - 1/(2 tau)) w_q) inv_cs2 of the Guo source, from the lattice tables
+template <int LAT>
+static void guo_factors(StepParams& p, double tau) {
+  for (int q = 0; q < Lattice<LAT>::Q; ++q)
+    p.guo_k[q] = (1.0 - 1.0 / (2.0 * tau)) * Lattice<LAT>::w(q) * Lattice<LAT>::ics;
+}
+
 extern "C" int mlbm_step_f64_noalloc(const mlbm_config* cfg, const double* f_in, double* f_out,
                                      const double* force_profile, double* diag_out,
                                      unsigned int* error_word_out, void* stream) {
   if (!cfg) return noalloc_fail(MLBM_ERR_INVALID, "null configuration");
   const mlbm_config& c = *cfg;
-  if (c.lattice < MLBM_D2Q9 || c.lattice > MLBM_D3Q27)
+  if (c.lattice < MLBM_D2Q9 || c.lattice > MLBM_D3Q33)
     return noalloc_fail(MLBM_ERR_INVALID, "bad lattice %d", c.lattice);
   if (c.collision != MLBM_BGK)
     return noalloc_fail(MLBM_ERR_INVALID, "the allocation-free step is the BGK collision only");
@@ -107,8 +114,9 @@ extern "C" int mlbm_step_f64_noalloc(const mlbm_config* cfg, const double* f_in,
     return noalloc_fail(MLBM_ERR_INVALID, "bad forcing scheme or force");
   if (!(c.relaxation_time > 0.5) || !std::isfinite(c.relaxation_time))
     return noalloc_fail(MLBM_ERR_INVALID, "relaxation time must be > 0.5 (got %g)", c.relaxation_time);
-  const int D = c.lattice == MLBM_D2Q9 ? 2 : 3;
-  const int Q = c.lattice == MLBM_D2Q9 ? 9 : (c.lattice == MLBM_D3Q19 ? 19 : 27);
+  static const int kD[6] = {2, 3, 3, 3, 2, 3}, kQ[6] = {9, 19, 27, 15, 13, 33};
+  const int D = kD[c.lattice];
+  const int Q = kQ[c.lattice];
   const long long L[3] = {c.length[0], c.length[1], D == 2 ? 1 : c.length[2]};
   for (int d = 0; d < 3; ++d)
     if (L[d] < 1 || L[d] > 65536) return noalloc_fail(MLBM_ERR_INVALID, "bad length[%d] = %lld", d, L[d]);
@@ -142,19 +150,13 @@ extern "C" int mlbm_step_f64_noalloc(const mlbm_config* cfg, const double* f_in,
   p.beta = (double)1.0 / (2.0 * c.relaxation_time);  // Collision.h:122
   p.bgk_a = 1. - 2. * p.beta;
   p.bgk_b = 2. * p.beta;
-  for (int q = 0; q < Q; ++q) {
-    double w;
-    if (c.lattice == MLBM_D2Q9) {
-      w = q == 0 ? 4.0 / 9.0 : ((q == 2 || q == 5 || q == 7 || q == 8) ? 1.0 / 9.0 : 1.0 / 36.0);
-    } else if (c.lattice == MLBM_D3Q19) {
-      w = q == 0 ? 1.0 / 3.0
-                 : ((q == 1 || q == 6 || q == 11 || q == 12 || q == 15 || q == 16) ? 1.0 / 18.0 : 1.0 / 36.0);
-    } else {
-      w = q == 0 ? 8.0 / 27.0
-          : (q == 1 || q == 10 || q == 19 || q == 20 || q == 23 || q == 24) ? 2.0 / 27.0
-          : ((q >= 6 && q <= 9) || (q >= 15 && q <= 18)) ? 1.0 / 216.0 : 1.0 / 54.0;
-    }
-    p.guo_k[q] = (1.0 - 1.0 / (2.0 * c.relaxation_time)) * w * 3.0;  // ForcingScheme.h:115-116
+  switch (c.lattice) {  // ForcingScheme.h:115-116
+    case MLBM_D2Q9: guo_factors<LAT_D2Q9>(p, c.relaxation_time); break;
+    case MLBM_D3Q19: guo_factors<LAT_D3Q19>(p, c.relaxation_time); break;
+    case MLBM_D3Q27: guo_factors<LAT_D3Q27>(p, c.relaxation_time); break;
+    case MLBM_D3Q15: guo_factors<LAT_D3Q15>(p, c.relaxation_time); break;
+    case MLBM_D2Q13: guo_factors<LAT_D2Q13>(p, c.relaxation_time); break;
+    default: guo_factors<LAT_D3Q33>(p, c.relaxation_time); break;
   }
   p.force_type = c.force;
   p.kol_axis = c.kolmogorov_axis;

@@ -80,3 +80,36 @@ def test_no_alloc_step_rejects_lattices_beyond_its_scratch():
                                    None, None)
     assert rc == capi.ERR_INVALID
     assert b"allocation-free limit" in lib.mlbm_last_error(None)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("lattice,shape", [("D2Q13", (20, 16, 1)), ("D3Q33", (12, 10, 8)),
+                                           ("D3Q15", (12, 10, 8))])
+def test_no_alloc_step_on_the_other_lattices(lattice, shape):
+    """D2Q13 / D3Q33 (two-node reach) and D3Q15 with a constant Shan-Chen force:
+    the allocation-free step equals the handle step bit for bit."""
+    import torch
+    from metalbm_gb300 import InputDeck, Lattice, build, capi, fields
+    build.build()
+    lib = capi.load()
+    D = 2 if lattice.startswith("D2") else 3
+    V = int(np.prod(shape))
+    deck = InputDeck(latticeT=lattice, forcingSchemeT="ShanChen", forceT="Constant",
+                     relaxationTime=0.7, forceAmplitude=(2e-4, -1e-4, 1e-4), globalLength=shape)
+    rho, u = fields.perturbed_rest(shape, D, 0.02, seed=13, rho_amplitude=0.01)
+    with Lattice(deck) as lat:
+        lat.init_equilibrium(rho, u)
+        f0 = lat.populations()
+        lat.step(1)
+        ref = lat.populations()
+    Q = f0.shape[0]
+    d_in, d_out = _dev(f0, torch), torch.empty(Q * V, dtype=torch.float64, device="cuda")
+    d_diag = torch.zeros(5, dtype=torch.float64, device="cuda")
+    cfg = deck.to_c()
+    rc = lib.mlbm_step_f64_noalloc(ct.byref(cfg), ct.c_void_p(d_in.data_ptr()),
+                                   ct.c_void_p(d_out.data_ptr()), None,
+                                   ct.c_void_p(d_diag.data_ptr()), None,
+                                   ct.c_void_p(torch.cuda.current_stream().cuda_stream))
+    assert rc == capi.OK, lib.mlbm_last_error(None)
+    torch.cuda.synchronize()
+    assert np.array_equal(d_out.cpu().numpy().reshape(Q, V), ref)
