@@ -129,6 +129,7 @@ struct SepGrid {
   const double2* twA;  // (cos, sin)(2 pi j / n), j < n
   const double2* twB;
   const double2* twC;
+  const float2* twCf;  // float copy of twC (FP32/FP16-storage updates)
 };
 
 // e^{+2 pi i k j / n}
@@ -275,7 +276,8 @@ __global__ void sep_inverse_a(SepGrid g, const double2* __restrict__ Ch, double2
 }
 
 // R2[a][b][kc][d] = sum_kb R1[a][kb][kc][d] e^{+2 pi i kb b / B}
-__global__ void sep_inverse_b(SepGrid g, const double2* __restrict__ R1, double2* __restrict__ R2) {
+__global__ void sep_inverse_b(SepGrid g, const double2* __restrict__ R1, double2* __restrict__ R2,
+                              float2* __restrict__ R2f) {
   const int nk = 2 * g.K + 1, nc = g.K + 1;
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= (long long)g.A * g.B * nc * g.D) return;
@@ -290,7 +292,10 @@ __global__ void sep_inverse_b(SepGrid g, const double2* __restrict__ R1, double2
     acc.x += p.x;
     acc.y += p.y;
   }
-  R2[t] = acc;
+  if (R2f)
+    R2f[t] = make_float2(narrow_rn(acc.x), narrow_rn(acc.y));
+  else
+    R2[t] = acc;
 }
 
 // field_d = injection_d + Re sum_kc R2[line][kc][d] e^{+2 pi i kc c / C}
@@ -324,6 +329,104 @@ __global__ void __launch_bounds__(256) sep_synthesis(SepGrid g, const double2* _
   }
 }
 
+// FP32 variants of the two per-node stages, for FP32/FP16 storage: the
+// kernels read a float field, so the sums need FP32 accuracy only (about
+// 1e-6 relative on a force that is itself ~1e-8 of the populations), and FP32
+// runs at ~73x the FP64 rate. The FP64 field kept for stored fields is the
+// exact widening of the float one; the middle stages (a few thousand modes)
+// stay FP64.
+template <int K>
+__global__ void __launch_bounds__(256) sep_forward_c_f(SepGrid g, const double* __restrict__ rho,
+                                                       const double* __restrict__ u,
+                                                       double2* __restrict__ P1) {
+  const int lane = threadIdx.x & 31;
+  const long long line = (long long)blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5);
+  if (line >= (long long)g.A * g.B) return;  // uniform across the warp
+  float ar[3][K + 1], ai[3][K + 1];
+#pragma unroll
+  for (int d = 0; d < 3; ++d)
+#pragma unroll
+    for (int k = 0; k <= K; ++k) ar[d][k] = ai[d][k] = 0.0f;
+  int idx[K + 1], step[K + 1];
+#pragma unroll
+  for (int k = 0; k <= K; ++k) {
+    idx[k] = (k * lane) % g.C;
+    step[k] = (32 * k) % g.C;
+  }
+  for (int c = lane; c < g.C; c += 32) {
+    const long long i = line * g.C + c;
+    const float r = narrow_rn(rho[i]);
+    float m[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) m[d] = d < g.D ? r * narrow_rn(u[(long long)d * g.V + i]) : 0.0f;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) ar[d][0] += m[d];
+#pragma unroll
+    for (int k = 1; k <= K; ++k) {
+      const float2 w = __ldg(g.twCf + idx[k]);
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        ar[d][k] = fmaf(m[d], w.x, ar[d][k]);
+        ai[d][k] = fmaf(-m[d], w.y, ai[d][k]);
+      }
+    }
+#pragma unroll
+    for (int k = 1; k <= K; ++k) {
+      idx[k] += step[k];
+      if (idx[k] >= g.C) idx[k] -= g.C;
+    }
+  }
+#pragma unroll
+  for (int d = 0; d < 3; ++d)
+#pragma unroll
+    for (int k = 0; k <= K; ++k)
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        ar[d][k] += __shfl_down_sync(0xffffffffu, ar[d][k], o);
+        ai[d][k] += __shfl_down_sync(0xffffffffu, ai[d][k], o);
+      }
+  if (lane == 0) {
+#pragma unroll
+    for (int k = 0; k <= K; ++k)
+#pragma unroll
+      for (int d = 0; d < 3; ++d)
+        if (d < g.D)
+          P1[(line * (K + 1) + k) * g.D + d] = make_double2(widen_exact(ar[d][k]), widen_exact(ai[d][k]));
+  }
+}
+
+template <int K>
+__global__ void __launch_bounds__(256) sep_synthesis_f(SepGrid g, const float2* __restrict__ R2f,
+                                                       const float* __restrict__ inj,
+                                                       float* __restrict__ field_f,
+                                                       double* __restrict__ field) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= g.V) return;
+  const long long line = i / g.C;
+  const int c = (int)(i - line * g.C);
+  float2 w[K + 1];
+  int e = 0;
+#pragma unroll
+  for (int k = 1; k <= K; ++k) {
+    e += c;
+    if (e >= g.C) e -= g.C;
+    w[k] = __ldg(g.twCf + e);
+  }
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    if (d >= g.D) break;
+    float f = inj ? inj[(long long)d * g.V + i] : 0.0f;
+    f += __ldg(R2f + (line * (K + 1)) * g.D + d).x;
+#pragma unroll
+    for (int k = 1; k <= K; ++k) {
+      const float2 z = __ldg(R2f + (line * (K + 1) + k) * g.D + d);
+      f = fmaf(z.x, w[k].x, fmaf(-z.y, w[k].y, f));
+    }
+    field_f[(long long)d * g.V + i] = f;
+    field[(long long)d * g.V + i] = widen_exact(f);
+  }
+}
+
 // float copy of the field for the FP32/FP16-storage kernels (integer-bit
 // rounding: conversion instructions run on the narrow FP64 path)
 __global__ void narrow_field_kernel(const double* __restrict__ in, float* __restrict__ out,
@@ -343,6 +446,10 @@ struct SpectralForce {
   cufftDoubleComplex* spec = nullptr;    // [D][nspec] work spectrum (cuFFT removal)
   cufftDoubleComplex* inject = nullptr;  // [D][nspec] injection spectrum (cuFFT removal)
   double* inj_field = nullptr;           // [D][V] injection field (separable removal)
+  float* inj_field_f = nullptr;          // its float copy (FP32 updates)
+  bool single = false;                   // FP32 separable updates (FP32/FP16 storage)
+  float2* twf = nullptr;                 // float twiddle table of the C axis
+  float2* R2f = nullptr;
   double* mom = nullptr;                 // [D][V]
   double* field = nullptr;               // [D][V]
   float* field_f = nullptr;              // [D][V] float copy, or null
@@ -362,7 +469,8 @@ void spectral_force_destroy(SpectralForce* sf) {
   if (!sf) return;
   if (sf->have_fwd) cufftDestroy(sf->fwd);
   if (sf->have_inv) cufftDestroy(sf->inv);
-  void* ptrs[] = {sf->spec, sf->inject, sf->inj_field, sf->mom, sf->field, sf->field_f, sf->tw,
+  void* ptrs[] = {sf->spec, sf->inject, sf->inj_field, sf->inj_field_f, sf->twf, sf->R2f,
+                  sf->mom, sf->field, sf->field_f, sf->tw,
                   sf->P1, sf->P2, sf->Ch, sf->R1, sf->R2};
   for (void* p : ptrs) cudaFree(p);
   delete sf;
@@ -383,7 +491,7 @@ static void twiddle_table(std::vector<double2>& t, int n) {
   }
 }
 
-static int setup_sparse(SpectralForce* sf, char* err, size_t errlen) {
+static int setup_sparse(SpectralForce* sf, cudaStream_t st, char* err, size_t errlen) {
   const SpecGrid& g = sf->g;
   SepGrid& s = sf->sg;
   s.D = g.D;
@@ -410,6 +518,31 @@ static int setup_sparse(SpectralForce* sf, char* err, size_t errlen) {
   s.twA = sf->tw;
   s.twB = sf->tw + s.A;
   s.twC = sf->tw + s.A + s.B;
+  s.twCf = nullptr;
+  if (sf->single) {
+    std::vector<float2> tf;
+    for (int j = 0; j < s.C; ++j) {
+      const double2 v = t[s.A + s.B + j];
+      tf.push_back(make_float2((float)v.x, (float)v.y));
+    }
+    if ((e = cudaMalloc(&sf->twf, sizeof(float2) * s.C)) != cudaSuccess ||
+        (e = cudaMalloc(&sf->R2f, sizeof(float2) * s.A * s.B * nc * s.D)) != cudaSuccess)
+      return sf_fail(err, errlen, "device allocation failed", (int)e);
+    if ((e = cudaMemcpy(sf->twf, tf.data(), sizeof(float2) * s.C, cudaMemcpyHostToDevice)) !=
+        cudaSuccess)
+      return sf_fail(err, errlen, "twiddle upload failed", (int)e);
+    s.twCf = sf->twf;
+    if (sf->inj_field) {
+      const long long n = sf->V * s.D;
+      if ((e = cudaMalloc(&sf->inj_field_f, sizeof(float) * n)) != cudaSuccess)
+        return sf_fail(err, errlen, "device allocation failed", (int)e);
+      // on the handle's stream, after the transform that produced inj_field
+      narrow_field_kernel<<<blocks_for(n), 256, 0, st>>>(sf->inj_field, sf->inj_field_f, n);
+      count_launches(1);
+      if ((e = cudaStreamSynchronize(st)) != cudaSuccess)
+        return sf_fail(err, errlen, "injection narrowing failed", (int)e);
+    }
+  }
   return 0;
 }
 
@@ -438,6 +571,7 @@ int spectral_force_create(SpectralForce** out, int force, int D, int lx, int ly,
   sf->V = (long long)lx * ly * g.lz;
   sf->time_dependent = force != MLBM_FORCE_CONSTANT_SHELL;
   sf->sparse = sf->time_dependent && rkmax <= kSparseMaxK;
+  sf->single = sf->sparse && want_float;
   for (int d = 0; d < 3; ++d) sf->ramp[d] = ramp[d];
   sf->rkmin = rkmin;
   sf->rkmax = rkmax;
@@ -482,7 +616,7 @@ int spectral_force_create(SpectralForce** out, int force, int D, int lx, int ly,
     if (dst == sf->field) narrow_field(sf, s);
   }
   if (sf->sparse) {
-    if (setup_sparse(sf, err, errlen)) {
+    if (setup_sparse(sf, s, err, errlen)) {
       spectral_force_destroy(sf);
       return 1;
     }
@@ -518,15 +652,23 @@ template <int K>
 static void launch_sparse(SpectralForce* sf, const double* rho, const double* u, cudaStream_t s) {
   const SepGrid& g = sf->sg;
   const long long lines = (long long)g.A * g.B;
-  sep_forward_c<K><<<(unsigned)((lines + 7) / 8), 256, 0, s>>>(g, rho, u, sf->P1);
+  if (sf->single)
+    sep_forward_c_f<K><<<(unsigned)((lines + 7) / 8), 256, 0, s>>>(g, rho, u, sf->P1);
+  else
+    sep_forward_c<K><<<(unsigned)((lines + 7) / 8), 256, 0, s>>>(g, rho, u, sf->P1);
   const long long nk = 2 * g.K + 1, nc = g.K + 1, na = 2 * g.KA + 1;
   sep_forward_b<<<blocks_for(g.A * nk * nc * g.D), 256, 0, s>>>(g, sf->P1, sf->P2);
   sep_modes<<<blocks_for(na * nk * nc * g.D), 256, 0, s>>>(
       g, sf->P2, sf->Ch, sf->ramp[0], sf->ramp[1], sf->ramp[2], sf->rkmin, sf->rkmax,
       1.0 / (double)sf->V);
   sep_inverse_a<<<blocks_for(g.A * nk * nc * g.D), 256, 0, s>>>(g, sf->Ch, sf->R1);
-  sep_inverse_b<<<blocks_for(lines * nc * g.D), 256, 0, s>>>(g, sf->R1, sf->R2);
-  sep_synthesis<K><<<blocks_for(g.V), 256, 0, s>>>(g, sf->R2, sf->inj_field, sf->field);
+  sep_inverse_b<<<blocks_for(lines * nc * g.D), 256, 0, s>>>(g, sf->R1, sf->R2,
+                                                             sf->single ? sf->R2f : nullptr);
+  if (sf->single)
+    sep_synthesis_f<K><<<blocks_for(g.V), 256, 0, s>>>(g, sf->R2f, sf->inj_field_f, sf->field_f,
+                                                       sf->field);
+  else
+    sep_synthesis<K><<<blocks_for(g.V), 256, 0, s>>>(g, sf->R2, sf->inj_field, sf->field);
   count_launches(6);
 }
 
@@ -556,7 +698,7 @@ int spectral_force_update(SpectralForce* sf, const double* rho, const double* u,
     if ((r = cufftExecZ2D(sf->inv, sf->spec, sf->field)) != CUFFT_SUCCESS)
       return sf_fail(err, errlen, "cufftExecZ2D failed", (int)r);
   }
-  narrow_field(sf, s);
+  if (!sf->single) narrow_field(sf, s);  // the FP32 updates write the float field directly
   const cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return sf_fail(err, errlen, cudaGetErrorString(e), (int)e);
   return 0;
