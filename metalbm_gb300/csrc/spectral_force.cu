@@ -206,52 +206,63 @@ __global__ void __launch_bounds__(256) sep_forward_c(SepGrid g, const double* __
   }
 }
 
-// P2[a][kb][kc][d] = sum_b P1[a][b][kc][d] e^{-2 pi i kb b / B}
+// P2[a][kb][kc][d] = sum_b P1[a][b][kc][d] e^{-2 pi i kb b / B}; one warp per
+// output, the lanes splitting the sum (fixed reduction order)
+__device__ __forceinline__ double2 warp_sum2(double2 v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    v.x += __shfl_down_sync(0xffffffffu, v.x, o);
+    v.y += __shfl_down_sync(0xffffffffu, v.y, o);
+  }
+  return v;
+}
+
 __global__ void sep_forward_b(SepGrid g, const double2* __restrict__ P1, double2* __restrict__ P2) {
   const int nk = 2 * g.K + 1, nc = g.K + 1;
-  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= (long long)g.A * nk * nc * g.D) return;
+  const int lane = threadIdx.x & 31;
+  const long long t = (long long)blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5);
+  if (t >= (long long)g.A * nk * nc * g.D) return;  // uniform across the warp
   const int d = (int)(t % g.D);
   const int kc = (int)((t / g.D) % nc);
   const int kbi = (int)((t / ((long long)g.D * nc)) % nk);
   const long long a = t / ((long long)g.D * nc * nk);
-  double2 acc = make_double2(0.0, 0.0);
   const int kbm = ((kbi - g.K) % g.B + g.B) % g.B;
-  int e = 0;  // (kb b) mod B
-  for (int b = 0; b < g.B; ++b) {
+  double2 acc = make_double2(0.0, 0.0);
+  for (int b = lane; b < g.B; b += 32) {
     const double2 v = P1[((a * g.B + b) * nc + kc) * g.D + d];
+    const int e = (int)(((long long)kbm * b) % g.B);
     const double2 p = cmul_conj(v, __ldg(g.twB + e));
     acc.x += p.x;
     acc.y += p.y;
-    e += kbm;
-    if (e >= g.B) e -= g.B;
   }
-  P2[t] = acc;
+  acc = warp_sum2(acc);
+  if (lane == 0) P2[t] = acc;
 }
 
-// modes of the box: sum over a, then the removal filter -A_d/V on the shell
-// (0 elsewhere), doubled for kc > 0 (each stands for k and -k)
+// modes of the box: sum over a (one warp per mode), then the removal filter
+// -A_d/V on the shell (0 elsewhere), doubled for kc > 0 (each stands for k and -k)
 __global__ void sep_modes(SepGrid g, const double2* __restrict__ P2, double2* __restrict__ Ch,
                           double rx, double ry, double rz, int kmin, int kmax, double inv_v) {
   const int nk = 2 * g.K + 1, nc = g.K + 1, na = 2 * g.KA + 1;
-  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= (long long)na * nk * nc * g.D) return;
+  const int lane = threadIdx.x & 31;
+  const long long t = (long long)blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5);
+  if (t >= (long long)na * nk * nc * g.D) return;  // uniform across the warp
   const int d = (int)(t % g.D);
   const int kc = (int)((t / g.D) % nc);
   const int kbi = (int)((t / ((long long)g.D * nc)) % nk);
   const int kai = (int)(t / ((long long)g.D * nc * nk));
   const int ka = kai - g.KA, kb = kbi - g.K;
-  double2 acc = make_double2(0.0, 0.0);
   const int kam = (ka % g.A + g.A) % g.A;
-  int e = 0;  // (ka a) mod A
-  for (int a = 0; a < g.A; ++a) {
+  double2 acc = make_double2(0.0, 0.0);
+  for (int a = lane; a < g.A; a += 32) {
     const double2 v = P2[(((long long)a * nk + kbi) * nc + kc) * g.D + d];
+    const int e = (int)(((long long)kam * a) % g.A);
     const double2 p = cmul_conj(v, __ldg(g.twA + e));
     acc.x += p.x;
     acc.y += p.y;
-    e += kam;
-    if (e >= g.A) e -= g.A;
   }
+  acc = warp_sum2(acc);
+  if (lane != 0) return;
   const long long k2 = (long long)ka * ka + (long long)kb * kb + (long long)kc * kc;
   const bool s = k2 >= (long long)kmin * kmin && k2 <= (long long)kmax * kmax;
   const double amp = d == 0 ? rx : (d == 1 ? ry : rz);
@@ -657,8 +668,9 @@ static void launch_sparse(SpectralForce* sf, const double* rho, const double* u,
   else
     sep_forward_c<K><<<(unsigned)((lines + 7) / 8), 256, 0, s>>>(g, rho, u, sf->P1);
   const long long nk = 2 * g.K + 1, nc = g.K + 1, na = 2 * g.KA + 1;
-  sep_forward_b<<<blocks_for(g.A * nk * nc * g.D), 256, 0, s>>>(g, sf->P1, sf->P2);
-  sep_modes<<<blocks_for(na * nk * nc * g.D), 256, 0, s>>>(
+  // one warp per output: 8 outputs per 256-thread block
+  sep_forward_b<<<(unsigned)((g.A * nk * nc * g.D + 7) / 8), 256, 0, s>>>(g, sf->P1, sf->P2);
+  sep_modes<<<(unsigned)((na * nk * nc * g.D + 7) / 8), 256, 0, s>>>(
       g, sf->P2, sf->Ch, sf->ramp[0], sf->ramp[1], sf->ramp[2], sf->rkmin, sf->rkmax,
       1.0 / (double)sf->V);
   sep_inverse_a<<<blocks_for(g.A * nk * nc * g.D), 256, 0, s>>>(g, sf->Ch, sf->R1);
