@@ -41,8 +41,9 @@ enum {
 
 /* ---- template axes of the reference, as runtime enums -------------------
  * Names and order follow include/metaLBM/Options.h:12-43. */
-/* LatticeType (Options.h:12-13). D3Q15, D2Q13 and D3Q33 run with FP64
- * storage only; D2Q13 and D3Q33 reach two nodes (the reference's halo 2). */
+/* LatticeType (Options.h:12-13). D2Q13 and D3Q33 reach two nodes (the
+ * reference's halo 2) and run with FP64 storage only; D3Q15 also runs with
+ * FP32 / FP16-shifted storage. */
 enum {
   MLBM_D2Q9 = 0,
   MLBM_D3Q19 = 1,

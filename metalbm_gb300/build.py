@@ -40,7 +40,7 @@ def units() -> list[tuple[Path, list[str], str]]:
             out += [(src, extra + [f"-DMLBM_LAT={l}"], f"{src.stem}_L{l}") for l in range(6)]
         elif src.name == "step_lowp.cu":
             out += [(src, extra + [f"-DMLBM_LAT={l}", f"-DMLBM_ST={st}"], f"{src.stem}_L{l}_S{st}")
-                    for l in range(3) for st in (1, 2)]
+                    for l in range(4) for st in (1, 2)]  # D2Q9, D3Q19, D3Q27, D3Q15
         else:
             out.append((src, extra, src.stem))
     return out

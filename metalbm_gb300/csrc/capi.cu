@@ -349,9 +349,10 @@ extern "C" int mlbm_create(const mlbm_config* cfg, mlbm_handle** out) {
   if (c.force < 0 || c.force > MLBM_FORCE_TURBULENT_2D)
     return fail(nullptr, MLBM_ERR_INVALID, "bad force %d", c.force);
   if (c.storage < 0 || c.storage > 2) return fail(nullptr, MLBM_ERR_INVALID, "bad storage %d", c.storage);
-  if (c.storage != MLBM_STORAGE_F64 && c.lattice > MLBM_D3Q27)
+  if (c.storage != MLBM_STORAGE_F64 && (c.lattice == MLBM_D2Q13 || c.lattice == MLBM_D3Q33))
     return fail(nullptr, MLBM_ERR_INVALID,
-                "FP32 / FP16 storage supports D2Q9, D3Q19 and D3Q27; lattice %d runs with FP64 storage",
+                "FP32 / FP16 storage supports D2Q9, D3Q19, D3Q27 and D3Q15; lattice %d runs with "
+                "FP64 storage",
                 c.lattice);
   if (!(c.relaxation_time > 0.5) || !std::isfinite(c.relaxation_time))
     return fail(nullptr, MLBM_ERR_INVALID, "relaxation time must be > 0.5 (got %g)", c.relaxation_time);

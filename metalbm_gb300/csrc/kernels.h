@@ -124,7 +124,18 @@ cudaError_t log_samples_lowp_L1_S2(const void* prev, const StepParams& p, const 
 cudaError_t step_f64_L2(int collision, int forcing, const double* prev, double* next, const StepParams& p, cudaStream_t s);
 cudaError_t init_f64_L2(const double* rho, const double* u, double* f, long long V, cudaStream_t s);
 cudaError_t log_samples_f64_L2(const double* prev, const StepParams& p, const long long* nodes, long long n, double* features, double* alpha, int* solved, cudaStream_t s);
-// D3Q15, D2Q13, D3Q33 (FP64 storage only)
+// D3Q15 with FP32 / FP16-shifted storage
+cudaError_t step_lowp_L3_S1(int collision, int fs, const void* prev, void* next, const StepParams& p, cudaStream_t s);
+cudaError_t init_lowp_L3_S1(const double* rho, const double* u, void* f, long long V, cudaStream_t s);
+cudaError_t lowp_to_f64_L3_S1(const void* f, int q, double* out, long long V, cudaStream_t s);
+cudaError_t f64_to_lowp_L3_S1(const double* in, int q, void* f, long long V, cudaStream_t s);
+cudaError_t log_samples_lowp_L3_S1(const void* prev, const StepParams& p, const long long* nodes, long long n, double* features, double* alpha, int* solved, cudaStream_t s);
+cudaError_t step_lowp_L3_S2(int collision, int fs, const void* prev, void* next, const StepParams& p, cudaStream_t s);
+cudaError_t init_lowp_L3_S2(const double* rho, const double* u, void* f, long long V, cudaStream_t s);
+cudaError_t lowp_to_f64_L3_S2(const void* f, int q, double* out, long long V, cudaStream_t s);
+cudaError_t f64_to_lowp_L3_S2(const double* in, int q, void* f, long long V, cudaStream_t s);
+cudaError_t log_samples_lowp_L3_S2(const void* prev, const StepParams& p, const long long* nodes, long long n, double* features, double* alpha, int* solved, cudaStream_t s);
+// D3Q15, D2Q13, D3Q33 with FP64 storage
 cudaError_t step_f64_L3(int collision, int forcing, const double* prev, double* next, const StepParams& p, cudaStream_t s);
 cudaError_t init_f64_L3(const double* rho, const double* u, double* f, long long V, cudaStream_t s);
 cudaError_t log_samples_f64_L3(const double* prev, const StepParams& p, const long long* nodes, long long n, double* features, double* alpha, int* solved, cudaStream_t s);

@@ -74,9 +74,13 @@ cudaError_t finalize_diag(const double* partials, int nblocks, double* out, cuda
     case 3: return F##_L3 ARGS; case 4: return F##_L4 ARGS; case 5: return F##_L5 ARGS; \
   } \
   return cudaErrorInvalidValue;
+// the FP32 / FP16 units exist for D2Q9, D3Q19, D3Q27 and D3Q15 (0..3)
+#define MLBM_BY_LAT4(L, C0, C1, C2, C3) \
+  switch (L) { case 0: return C0; case 1: return C1; case 2: return C2; case 3: return C3; } \
+  return cudaErrorInvalidValue;
 #define MLBM_BY_LAT_ST(L, S, F, ARGS) \
-  if (S == 1) { MLBM_BY_LAT(L, F##_L0_S1 ARGS, F##_L1_S1 ARGS, F##_L2_S1 ARGS) } \
-  if (S == 2) { MLBM_BY_LAT(L, F##_L0_S2 ARGS, F##_L1_S2 ARGS, F##_L2_S2 ARGS) } \
+  if (S == 1) { MLBM_BY_LAT4(L, F##_L0_S1 ARGS, F##_L1_S1 ARGS, F##_L2_S1 ARGS, F##_L3_S1 ARGS) } \
+  if (S == 2) { MLBM_BY_LAT4(L, F##_L0_S2 ARGS, F##_L1_S2 ARGS, F##_L2_S2 ARGS, F##_L3_S2 ARGS) } \
   return cudaErrorInvalidValue;
 
 cudaError_t entropy_test(int lattice, const float* f, const double* fneq, long long nodes,

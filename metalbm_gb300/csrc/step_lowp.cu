@@ -1325,10 +1325,12 @@ static cudaError_t launch_lowp(int collision, const void* prev, void* next, cons
   return cudaGetLastError();
 }
 
-// This file is compiled once per (lattice, storage) pair (MLBM_LAT = 0..2,
-// MLBM_ST = 1 F32 or 2 F16-shifted); misc.cu dispatches.
+// This file is compiled once per (lattice, storage) pair (MLBM_LAT = 0..3:
+// D2Q9, D3Q19, D3Q27, D3Q15 -- the lattices of reach 1 with inv_cs2 = 3 and a
+// conserving equilibrium, which this file's pair algebra and series form
+// assume; MLBM_ST = 1 F32 or 2 F16-shifted); misc.cu dispatches.
 #if !defined(MLBM_LAT) || !defined(MLBM_ST)
-#error "compile step_lowp.cu with -DMLBM_LAT=<0|1|2> -DMLBM_ST=<1|2>"
+#error "compile step_lowp.cu with -DMLBM_LAT=<0..3> -DMLBM_ST=<1|2>"
 #endif
 #define MLBM_CAT2(a, b, c, d) a##b##c##d
 #define MLBM_CAT(a, b, c, d) MLBM_CAT2(a, b, c, d)

@@ -98,11 +98,11 @@ def test_collision_enum_matches_header_and_deck(lib):
     assert b"collision" in lib.mlbm_last_error(None)
 
 
-def test_new_lattices_run_with_fp64_storage_only(lib):
-    """D3Q15, D2Q13 and D3Q33 are FP64-storage lattices: FP32 / FP16 storage
-    is refused before any device work, with the reason."""
+def test_two_node_lattices_run_with_fp64_storage_only(lib):
+    """D2Q13 and D3Q33 (reach two nodes) are FP64-storage lattices: FP32 /
+    FP16 storage is refused before any device work, with the reason."""
     from metalbm_gb300 import capi
-    for lattice in (capi.D3Q15, capi.D2Q13, capi.D3Q33):
+    for lattice in (capi.D2Q13, capi.D3Q33):
         for storage in (capi.STORAGE_F32, capi.STORAGE_F16_SHIFTED):
             c = capi.Config()
             lib.mlbm_config_init(ct.byref(c))

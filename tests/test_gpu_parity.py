@@ -203,7 +203,7 @@ def test_diagnostics_match_fields():
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("storage,tol", [("f32", 2e-4), ("f16_shifted", 5e-3)])
-@pytest.mark.parametrize("lattice", ["D2Q9", "D3Q19", "D3Q27"])
+@pytest.mark.parametrize("lattice", ["D2Q9", "D3Q19", "D3Q27", "D3Q15"])
 @pytest.mark.parametrize("forcing,force", [("Guo", "Kolmogorov"), ("ExactDifferenceMethod", "Sinusoidal"),
                                            ("ShanChen", "Constant"), ("None", "None")])
 def test_low_precision_storage_tracks_f64(storage, tol, lattice, forcing, force):
@@ -230,14 +230,15 @@ def test_low_precision_storage_tracks_f64(storage, tol, lattice, forcing, force)
 
 
 @pytest.mark.gpu
-def test_mixed_entropic_tracks_f64():
+@pytest.mark.parametrize("lattice", ["D3Q27", "D3Q15"])
+def test_mixed_entropic_tracks_f64(lattice):
     """FP32-storage entropic step (FP64 alpha solve) against the FP64 one."""
     from metalbm_gb300 import InputDeck, Lattice, fields
     shape = (16, 12, 10)
     rho, u = fields.taylor_green(shape, u0=0.05)
     out = {}
     for st in ("f64", "f32"):
-        with Lattice(InputDeck(latticeT="D3Q27", collisionT="ELBM", relaxationTime=0.50025,
+        with Lattice(InputDeck(latticeT=lattice, collisionT="ELBM", relaxationTime=0.50025,
                                globalLength=shape, storage=st, alphaSolver="residual",
                                newtonTolerance=1e-12, deviationThreshold=0.0)) as lat:
             lat.init_equilibrium(rho, u)
