@@ -271,10 +271,9 @@ class PortRun:
             if w["forceT"] == "ConstantShell":
                 F = sf.constant_shell_field(self.shape, D, w["forceAmplitude"], w["forcekMin"],
                                             w["forcekMax"])
-            elif w["forceT"] == "EnergyRemoval":
-                F = sf.energy_removal_field(self.rho, self.u, self.shape, D,
-                                            w["removalForceAmplitude"], w["removalForcekMin"],
-                                            w["removalForcekMax"])
+            elif w["forceT"] == "EnergyRemoval":  # the force parameters (Algorithm.h:90-91)
+                F = sf.energy_removal_field(self.rho, self.u, self.shape, D, w["forceAmplitude"],
+                                            w["forcekMin"], w["forcekMax"])
             else:
                 F = sf.turbulent_field(self.rho, self.u, self.shape, D, w["forceAmplitude"],
                                        w["forcekMin"], w["forcekMax"],

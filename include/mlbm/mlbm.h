@@ -72,12 +72,15 @@ enum { MLBM_FORCING_NONE = 0, MLBM_FORCING_GUO = 1, MLBM_FORCING_SHAN_CHEN = 2,
        MLBM_FORCING_EXACT_DIFFERENCE = 3 };                         /* ForcingSchemeType */
 /* ForceType (Options.h:39-41). The spectral forces (Force.h:294-626) are a
  * per-node force field computed on the device (FP64; a float copy for FP32 /
- * FP16 storage); their shells use force_kmin/force_kmax and, for the removal
- * part, removal_amplitude / removal_kmin / removal_kmax:
- *   CONSTANT_SHELL  time-independent solenoidal forcing on the shell
- *                   kmin <= |k| <= kmax (curl of a constant-amplitude spectrum)
- *   ENERGY_REMOVAL  F = -A P_shell(rho u) from the last stored fields, every step
- *   TURBULENT_2D    CONSTANT_SHELL + ENERGY_REMOVAL (any dimension) */
+ * FP16 storage). Every force takes force_amplitude and the shell
+ * force_kmin <= |k| <= force_kmax (Algorithm.h:90-91); removal_amplitude /
+ * removal_kmin / removal_kmax are the removal part of TURBULENT_2D only
+ * (Force.h:585-587):
+ *   CONSTANT_SHELL  time-independent solenoidal forcing on the shell (curl of
+ *                   a constant-amplitude spectrum)
+ *   ENERGY_REMOVAL  F = -A P_shell(rho u) from the last stored fields
+ *   TURBULENT_2D    CONSTANT_SHELL(force_*) + ENERGY_REMOVAL(removal_*), any
+ *                   dimension */
 enum {
   MLBM_FORCE_NONE = 0,
   MLBM_FORCE_CONSTANT = 1,

@@ -380,8 +380,10 @@ extern "C" int mlbm_create(const mlbm_config* cfg, mlbm_handle** out) {
   if (spectral) {
     long long lmin = L[0];
     for (int d = 1; d < D; ++d) lmin = std::min(lmin, L[d]);
-    const bool inj = c.force != MLBM_FORCE_ENERGY_REMOVAL, rem = c.force != MLBM_FORCE_CONSTANT_SHELL;
-    if ((inj && (c.force_kmin < 0 || c.force_kmax < c.force_kmin || 2LL * c.force_kmax >= lmin)) ||
+    // every force takes forceAmplitude / forcekMin / forcekMax (Algorithm.h:90-91);
+    // the removal* parameters are the removal part of Turbulent2D (Force.h:585-587)
+    const bool rem = c.force == MLBM_FORCE_TURBULENT_2D;
+    if ((c.force_kmin < 0 || c.force_kmax < c.force_kmin || 2LL * c.force_kmax >= lmin) ||
         (rem && (c.removal_kmin < 0 || c.removal_kmax < c.removal_kmin ||
                  2LL * c.removal_kmax >= lmin)))
       return fail(nullptr, MLBM_ERR_INVALID,
@@ -493,10 +495,15 @@ extern "C" int mlbm_create(const mlbm_config* cfg, mlbm_handle** out) {
   // Spectral forces: the force field on the device (spectral_force.cu).
   if (spectral) {
     char msg[256] = {0};
+    // EnergyRemoval alone removes with the force amplitude and shell; in
+    // Turbulent2D the force parameters inject and the removal ones remove
+    const bool alone = c.force == MLBM_FORCE_ENERGY_REMOVAL;
     if (spectral_force_create(&h->spectral, c.force, D, (int)L[0], (int)L[1], (int)L[2],
-                              c.force_amplitude, c.force_kmin, c.force_kmax, c.removal_amplitude,
-                              c.removal_kmin, c.removal_kmax, c.storage != MLBM_STORAGE_F64,
-                              h->stream, msg, sizeof msg)) {
+                              c.force_amplitude, c.force_kmin, c.force_kmax,
+                              alone ? c.force_amplitude : c.removal_amplitude,
+                              alone ? c.force_kmin : c.removal_kmin,
+                              alone ? c.force_kmax : c.removal_kmax,
+                              c.storage != MLBM_STORAGE_F64, h->stream, msg, sizeof msg)) {
       h->error = std::string("spectral force: ") + msg;
       return bail(MLBM_ERR_CUDA);
     }

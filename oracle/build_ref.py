@@ -33,11 +33,17 @@ class RefCase:
     lattice: str          # D2Q9 | D3Q19 | D3Q27 | D3Q15 | D2Q13 | D3Q33
     collision: str        # BGK | ELBM | ForcedBNR_ELBM | Approached_ELBM | ... (CollisionType)
     forcing: str          # None | Guo | ShanChen | ExactDifferenceMethod
-    force: str            # None | Constant | Sinusoidal | Kolmogorov
+    force: str            # None | Constant | Sinusoidal | Kolmogorov | ConstantShell | ...
     tau: float
     amp: tuple[float, float, float]
     wavelength: tuple[float, float, float]
     size: tuple[int, int, int]
+    # spectral-force shells: forcekMin/Max, removalForceAmplitude, removalForcekMin/Max
+    kmin: int = 1
+    kmax: int = 2
+    ramp: tuple[float, float, float] = (0.0, 0.0, 0.0)
+    rkmin: int = 1
+    rkmax: int = 2
 
 
 # Small cases for golden vectors (non-square, non-power-of-two grids to catch
@@ -116,6 +122,19 @@ CASES: dict[str, RefCase] = {
                                            (2e-4, 1e-4, -1e-4), (1.0, 1.0, 1.0), (8, 10, 9)),
     "d3q33_elbm_none_none": RefCase("D3Q33", "ELBM", "None", "None", 0.500250125062531,
                                     (0.0, 0.0, 0.0), (1.0, 1.0, 1.0), (12, 10, 8)),
+    # 2-D spectral forces (Force.h:294-626), with the DFT stand-in of
+    # oracle/ref_stub/fftw3-mpi.h; well defined in 2-D (the 3-D partner writes
+    # are out of range)
+    "d2q9_bgk_guo_constantshell": RefCase("D2Q9", "BGK", "Guo", "ConstantShell", 0.6,
+                                          (1e-3, -2e-3, 0.0), (1.0, 1.0, 1.0), (24, 16, 1),
+                                          kmin=1, kmax=3),
+    "d2q9_bgk_guo_energyremoval": RefCase("D2Q9", "BGK", "Guo", "EnergyRemoval", 0.6,
+                                          (0.05, 0.08, 0.0), (1.0, 1.0, 1.0), (24, 16, 1),
+                                          kmin=1, kmax=3),
+    "d2q9_bgk_edm_turbulent2d": RefCase("D2Q9", "BGK", "ExactDifferenceMethod", "Turbulent2D",
+                                        0.7, (2e-3, 1e-3, 0.0), (1.0, 1.0, 1.0), (20, 24, 1),
+                                        kmin=2, kmax=4, ramp=(0.04, 0.03, 0.0), rkmin=1,
+                                        rkmax=2),
     # CPU-baseline timing cases (sizes of the benchmark workloads, run for a
     # bounded number of steps).
     "time_d3q19_bgk_guo_kolmogorov_128": RefCase("D3Q19", "BGK", "Guo", "Kolmogorov", 0.55,
@@ -136,9 +155,8 @@ def compile_case(name: str, case: RefCase) -> Path:
     out_dir = OUT / name
     out_dir.mkdir(parents=True, exist_ok=True)
     exe = out_dir / "run"
+    stamp = out_dir / "cmd"  # the compile command of `exe`: a changed case rebuilds
     sources = [HERE / "ref_harness.cpp", HERE / "ref_deck.in"] + sorted(HERE.glob("ref_stub/*.h"))
-    if exe.exists() and all(exe.stat().st_mtime > s.stat().st_mtime for s in sources):
-        return exe
     defs = {
         "NPROCS": "1", "NTHREADS": "1", "USE_FFTW": "1",
         "GLOBAL_LENGTH_X": str(case.size[0]), "GLOBAL_LENGTH_Y": str(case.size[1]),
@@ -150,6 +168,10 @@ def compile_case(name: str, case: RefCase) -> Path:
         "MLBM_AMP_Z": _lit(case.amp[2]),
         "MLBM_WL_X": _lit(case.wavelength[0]), "MLBM_WL_Y": _lit(case.wavelength[1]),
         "MLBM_WL_Z": _lit(case.wavelength[2]),
+        "MLBM_KMIN": str(case.kmin), "MLBM_KMAX": str(case.kmax),
+        "MLBM_RAMP_X": _lit(case.ramp[0]), "MLBM_RAMP_Y": _lit(case.ramp[1]),
+        "MLBM_RAMP_Z": _lit(case.ramp[2]),
+        "MLBM_RKMIN": str(case.rkmin), "MLBM_RKMAX": str(case.rkmax),
     }
     cmd = ["g++", "-std=c++14", "-O2", "-ffp-contract=off", "-fpermissive", "-w",
            f"-I{HERE / 'ref_stub'}", f"-I{HERE}", f"-I{REF_INCLUDE / 'metaLBM'}",
@@ -158,9 +180,13 @@ def compile_case(name: str, case: RefCase) -> Path:
         defs[f"MLBM_FORCE_IS_{case.force.upper()}"] = "1"
     cmd += [f"-D{k}={v}" for k, v in defs.items()]
     cmd += [str(HERE / "ref_harness.cpp"), "-o", str(exe)]
+    if (exe.exists() and stamp.exists() and stamp.read_text() == " ".join(cmd)
+            and all(exe.stat().st_mtime > src.stat().st_mtime for src in sources)):
+        return exe
     res = subprocess.run(cmd, capture_output=True, text=True)
     if res.returncode != 0:
         raise RuntimeError(f"building {name} failed:\n{res.stderr[-4000:]}")
+    stamp.write_text(" ".join(cmd))
     return exe
 
 

@@ -16,7 +16,8 @@ What is restated (reference file:line), per the code's evident intent:
   (i k_y psi, -i k_x psi) in 2-D; then the backward transform divided by the
   node count (Transformer.h:98-108);
 * EnergyRemoval (Force.h:434-572): F_d = -A_d P_shell(rho u_d), the momentum
-  of the stored fields filtered to the shell;
+  of the stored fields filtered to the shell; alone it takes forceAmplitude
+  and forcekMin / forcekMax like every force (Algorithm.h:90-91);
 * Turbulent2D (Force.h:575-622): ConstantShell(forceAmplitude, forcekMin,
   forcekMax) + EnergyRemoval(removalForceAmplitude, removalForcekMin,
   removalForcekMax).

@@ -25,11 +25,17 @@ def load(case):
 
 def deck_for(meta, **kw):
     from metalbm_gb300 import InputDeck
+    spectral = {"forcekMin": meta.get("kmin", 1), "forcekMax": meta.get("kmax", 2),
+                "removalForceAmplitude": tuple(meta.get("ramp", (0.0, 0.0, 0.0))),
+                "removalForcekMin": meta.get("rkmin", 1), "removalForcekMax": meta.get("rkmax", 2)}
     return InputDeck(latticeT=meta["lattice"], collisionT=meta["collision"],
                      forcingSchemeT=meta["forcing"], forceT=meta["force"],
                      relaxationTime=meta["tau"], forceAmplitude=tuple(meta["amp"]),
                      forceWaveLength=tuple(meta["wavelength"]), globalLength=tuple(meta["size"]),
-                     **kw)
+                     **spectral, **kw)
+
+
+SPECTRAL_FORCES = ("ConstantShell", "EnergyRemoval", "Turbulent2D")
 
 
 def rel(a, b):
@@ -53,7 +59,13 @@ def test_f64_matches_reference(case):
         lat.sync(60000)
         f = lat.populations()
         fl = lat.fields()
-    if meta["collision"] == "BGK":
+    if meta["force"] in SPECTRAL_FORCES:
+        # the force field comes from cuFFT / the separable transforms, the
+        # reference's from the DFT stand-in: equal to rounding
+        assert rel(fl["force"], g["force"]) <= 1e-13
+        assert rel(f, g["f"]) <= 1e-13 and rel(fl["u"], g["u"]) <= 1e-12
+        assert rel(fl["rho"], g["rho"]) <= 1e-13
+    elif meta["collision"] == "BGK":
         assert np.array_equal(f, g["f"]), rel(f, g["f"])
         assert np.array_equal(fl["rho"], g["rho"])
         assert np.array_equal(fl["u"], g["u"])

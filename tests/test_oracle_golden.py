@@ -29,7 +29,11 @@ def port_for(meta, **kw):
         size=tuple(meta["size"]), alpha_mode=ALPHA_REFERENCE, **kw))
 
 
-CASES = sorted(p.stem for p in GOLDEN.glob("*.npz"))
+CASES_ALL = sorted(p.stem for p in GOLDEN.glob("*.npz"))
+# the spectral-force goldens: FFT-based forces, compared within tolerance
+SPECTRAL_CASES = [c for c in CASES_ALL
+                  if any(k in c for k in ("constantshell", "energyremoval", "turbulent2d"))]
+CASES = [c for c in CASES_ALL if c not in SPECTRAL_CASES]
 
 
 @pytest.mark.parametrize("case", CASES)
@@ -150,3 +154,39 @@ def test_residual_mode_logarithm_accuracy():
     assert (np.abs(got - ref) <= bound).all()
     away = np.abs(ref) >= 0.5
     assert (np.abs(got - ref)[away] <= 2 * np.spacing(np.abs(ref[away]))).all()
+
+
+def spectral_field(meta, rho0, u0):
+    """The restated force field of a spectral golden (oracle/spectral_force.py);
+    the reference stores its fields only on the last step, so EnergyRemoval
+    reads the initial ones throughout."""
+    from oracle import spectral_force as sf
+    D = 2 if meta["lattice"].startswith("D2") else 3
+    shape = tuple(meta["size"])
+    if meta["force"] == "ConstantShell":
+        return sf.constant_shell_field(shape, D, meta["amp"], meta["kmin"], meta["kmax"])
+    if meta["force"] == "EnergyRemoval":
+        return sf.energy_removal_field(rho0, u0, shape, D, meta["amp"], meta["kmin"], meta["kmax"])
+    return sf.turbulent_field(rho0, u0, shape, D, meta["amp"], meta["kmin"], meta["kmax"],
+                              meta["ramp"], meta["rkmin"], meta["rkmax"])
+
+
+@pytest.mark.parametrize("case", SPECTRAL_CASES)
+def test_spectral_force_restatement_matches_reference(case):
+    """2-D ConstantShell / EnergyRemoval / Turbulent2D: the reference, built
+    with the DFT stand-in for FFTW (oracle/ref_stub/fftw3-mpi.h), against the
+    numpy restatement driving the oracle's force-field mode. FFT and DFT round
+    differently: force within 1e-14 max|F|, f within 1e-13, u within 1e-12."""
+    g, meta = load(case)
+    F = spectral_field(meta, g["rho0"], g["u0"])
+    assert np.abs(F - g["force"]).max() <= 1e-14 * np.abs(g["force"]).max()
+    port = OraclePort(OracleConfig(lattice=meta["lattice"], collision=meta["collision"],
+                                   forcing=meta["forcing"], force="Field", tau=meta["tau"],
+                                   size=tuple(meta["size"])))
+    port.init_equilibrium(g["rho0"], g["u0"])
+    port.set_force_field(F)
+    port.step(meta["steps"])
+    fl = port.fields()
+    assert np.abs(port.populations() - g["f"]).max() <= 1e-13 * np.abs(g["f"]).max()
+    assert np.abs(fl["u"] - g["u"]).max() <= 1e-12 * np.abs(g["u"]).max()
+    assert np.abs(fl["rho"] - g["rho"]).max() <= 1e-13

@@ -132,8 +132,11 @@ def test_time_dependent_spectral_force_matches_oracle(lattice, shape, force, rkm
     D = 2 if lattice.startswith("D2") else 3
     A, RA = (2e-4, -1e-4, 3e-4), (0.05, 0.08, 0.03)
     rho, u = fields.perturbed_rest(shape, D, 0.03, seed=7, rho_amplitude=0.01)
-    deck = _deck(lattice, force, shape, forceAmplitude=A, forcekMin=2, forcekMax=4,
-                 removalForceAmplitude=RA, removalForcekMin=1, removalForcekMax=rkmax)
+    if force == "EnergyRemoval":  # alone it takes the force parameters (Algorithm.h:90-91)
+        deck = _deck(lattice, force, shape, forceAmplitude=RA, forcekMin=1, forcekMax=rkmax)
+    else:
+        deck = _deck(lattice, force, shape, forceAmplitude=A, forcekMin=2, forcekMax=4,
+                     removalForceAmplitude=RA, removalForcekMin=1, removalForcekMax=rkmax)
     steps = 6
     with Lattice(deck) as lat:
         lat.init_equilibrium(rho, u)
