@@ -2,8 +2,8 @@
 
 `pinned_array(shape)` maps anonymous memory, asks for transparent huge pages
 (madvise MADV_HUGEPAGE) and registers the range with CUDA
-(cudaHostRegister). Measured on the GB300 machines this build runs on (a VM
-with 64 KiB base pages): copies of the 4.3 GB field arrays of a 512^3
+(cudaHostRegister). Measured on a GB300 virtual machine with 64 KiB base
+pages: copies of the 4.3 GB field arrays of a 512^3
 lattice take 22 ms in both directions every time from such a buffer, while
 buffers from the CUDA host allocator alternate between 22 ms and 80 ms (and
 the upload between 60 ms and 230 ms), the cost of translating many small

@@ -10,8 +10,8 @@ mlbm_get_fields (dense node order, [D][V]):
   (Transformer.h:146-151, AnalysisList.h:140-148); no 2 pi / L factor.
 * Curl (Transformer.h:118-187 in 2D, 189-295 in 3D): omega_hat = i k x u_hat,
   brought back with the normalised backward transform, then divided by V once
-  more by Curl::normalize (Transformer.h:181-187, 285-294), which the driver
-  calls after every evaluation (Routine.h:102-104, 128-131). In 2D the
+  more by Curl::normalize (Transformer.h:181-187, 285-294), which the reference's
+  Routine calls after every evaluation (Routine.h:102-104, 128-131). In 2D the
   reference keeps only the real part of omega_hat (its imaginary part is
   multiplied by 0, Transformer.h:160-164). `reference=True` reproduces all of
   this; `reference=False` gives the textbook vorticity of a field sampled on

@@ -6,7 +6,7 @@ import pytest
 
 @pytest.mark.gpu
 def test_d2q9_kolmogorov_1000_steps_matches_oracle_with_diagnostics():
-    """BASELINE configuration [0]: D2Q9 BGK FP64, 256^2, tau 0.6, Guo,
+    """The D2Q9 Kolmogorov configuration: D2Q9 BGK FP64, 256^2, tau 0.6, Guo,
     Kolmogorov F_x(y) = 1e-5 sin(2 pi 4 y / 256), rho0 = 1, u ~ U[-1e-4, 1e-4]
     (seed 0), f at equilibrium, 1000 steps; energy, enstrophy and max Mach
     every 100 steps. The GPU state equals the oracle bit for bit at every
