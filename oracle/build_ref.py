@@ -135,6 +135,10 @@ CASES: dict[str, RefCase] = {
                                         0.7, (2e-3, 1e-3, 0.0), (1.0, 1.0, 1.0), (20, 24, 1),
                                         kmin=2, kmax=4, ramp=(0.04, 0.03, 0.0), rkmin=1,
                                         rkmax=2),
+    "d2q9_elbm_guo_turbulent2d": RefCase("D2Q9", "ELBM", "Guo", "Turbulent2D", 0.52,
+                                         (1e-3, 0.0, 0.0), (1.0, 1.0, 1.0), (24, 20, 1),
+                                         kmin=3, kmax=5, ramp=(0.05, 0.05, 0.0), rkmin=1,
+                                         rkmax=2),
     # CPU-baseline timing cases (sizes of the benchmark workloads, run for a
     # bounded number of steps).
     "time_d3q19_bgk_guo_kolmogorov_128": RefCase("D3Q19", "BGK", "Guo", "Kolmogorov", 0.55,

@@ -61,10 +61,13 @@ def test_f64_matches_reference(case):
         fl = lat.fields()
     if meta["force"] in SPECTRAL_FORCES:
         # the force field comes from cuFFT / the separable transforms, the
-        # reference's from the DFT stand-in: equal to rounding
+        # reference's from the DFT stand-in: equal to rounding (entropic runs
+        # add the CUDA-log difference of TOL_F64)
+        tol = 1e-13 if meta["collision"] == "BGK" else TOL_F64
         assert rel(fl["force"], g["force"]) <= 1e-13
-        assert rel(f, g["f"]) <= 1e-13 and rel(fl["u"], g["u"]) <= 1e-12
-        assert rel(fl["rho"], g["rho"]) <= 1e-13
+        assert rel(f, g["f"]) <= tol and rel(fl["u"], g["u"]) <= 1e-12
+        assert rel(fl["rho"], g["rho"]) <= tol
+        assert np.abs(fl["alpha"] - g["alpha"]).max() <= 1e-7
     elif meta["collision"] == "BGK":
         assert np.array_equal(f, g["f"]), rel(f, g["f"])
         assert np.array_equal(fl["rho"], g["rho"])
