@@ -69,9 +69,10 @@ def _rfftn(a, xp, shape):
 
 
 def _irfftn(a, xp, shape):
+    axes = tuple(range(len(shape)))
     if xp is np:
-        return np.fft.irfftn(a, s=shape)
-    return xp.fft.irfftn(a, s=shape)
+        return np.fft.irfftn(a, s=shape, axes=axes)
+    return xp.fft.irfftn(a, s=shape, dim=axes)
 
 
 def active_shape(shape):
@@ -114,13 +115,24 @@ def energy(rho, u) -> float:
     return float((0.5 * rho * (u * u).sum(0)).sum() / rho.shape[0])
 
 
-def energy_spectrum(u, shape):
-    """Shell-averaged energy spectrum E(k), k = 0 .. max(L)/2 - 1."""
+def reference_shell_count(shape) -> int:
+    """The reference's number of spectrum shells, gFD::maxWaveNumber()
+    (FourierDomain.h:77-79): arrayMax(globalLength) / 2, whose recursion
+    takes the minimum of the remaining lengths (Helpers.h:37-39), so
+    max(L_x, min(L_y, L_z)) / 2 with L_z = 1 on 2-D lattices."""
+    lx, ly, lz = (tuple(shape) + (1, 1))[:3]
+    return max(lx, min(ly, lz)) // 2
+
+
+def energy_spectrum(u, shape, reference: bool = True):
+    """Shell-averaged energy spectrum E(k) (PowerSpectra, Analysis.h:122-177;
+    AnalysisList.h:135-171, 194): k = 0 .. K - 1 with K the reference's shell
+    count (`reference=True`, see reference_shell_count) or max(L) / 2."""
     xp = _xp(u)
     sh = active_shape(shape)
     D = len(sh)
     V = int(np.prod(sh))
-    kmax = max(sh) // 2
+    kmax = reference_shell_count(shape) if reference else max(sh) // 2
     k = _wavenumbers(sh, xp, u)
     kk = sum(c * c for c in k)
     knorm = xp.floor(xp.sqrt(kk)) if xp is not np else np.floor(np.sqrt(kk))

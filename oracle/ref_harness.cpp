@@ -31,6 +31,7 @@
 #include <chrono>
 #include <cstdio>
 #include <cstdlib>
+#include <string>
 #include <vector>
 
 // The reference's Force<Constant>::setForceArray and
@@ -153,5 +154,79 @@ int main(int argc, char** argv) {
     return 4;
   }
   std::fclose(fout);
+
+  // Spectral analyses of the stored fields, after the dump (the curl and the
+  // spectra transform the velocity in place and back): the Routine's curl
+  // (Routine.h:69-72, 128-131), the scalar list's loop (AnalysisList.h:55-66,
+  // 86-89) and the spectral list's loop (AnalysisList.h:135-171, 194), on the
+  // reference's own Curl, TotalEnergy, TotalEnstrophy and PowerSpectra.
+  // Written to <output>.analysis: vorticity [2D-3][V], energy, enstrophy,
+  // the number of shells, the energy spectrum.
+  {
+    const Position offset = gFD::offset(MPIInit::rank);  // Curl<3> keeps a reference to it
+    const auto gl = Cast<unsigned int, ptrdiff_t, 3>::Do(gSD::sLength());
+    Curl<double, Architecture::CPU, PartitionningType::OneD, L::dimD, L::dimD> curl(
+        fieldList.velocity.getData(n), fieldList.vorticity.getData(n), gl.data(), offset);
+    curl.executeSpace();
+    curl.normalize();
+
+    TotalEnergy<T> energy(fieldList.density.getData(n), fieldList.velocity.getData(n));
+    TotalEnstrophy<T> enstrophy(fieldList.vorticity.getData(n));
+    energy.reset();
+    enstrophy.reset();
+    for (unsigned x = 0; x < lx; ++x)
+      for (unsigned y = 0; y < ly; ++y)
+        for (unsigned z = 0; z < lz; ++z) {
+          const Position iP{{x, y, z}};
+          energy(iP);
+          enstrophy(iP);
+        }
+    energy.normalize();
+    enstrophy.normalize();
+
+    constexpr unsigned K = gFD::maxWaveNumber();
+    PowerSpectra<T, K> spectra(fieldList.velocity.getData(n), gl.data(), "energy_spectra");
+    spectra.reset();
+    spectra.executeForward();
+    const Position fl = lFD::length();
+    for (unsigned x = 0; x < fl[d::X]; ++x)
+      for (unsigned y = 0; y < fl[d::Y]; ++y)
+        for (unsigned z = 0; z < fl[d::Z]; ++z) {
+          const Position iFP{{x, y, z}};
+          WaveNumber iK{{0}};
+          iK[d::X] = iFP[d::X] + offset[d::X] <= gSD::sLength()[d::X] / 2
+                         ? iFP[d::X] + offset[d::X]
+                         : iFP[d::X] + offset[d::X] - gSD::sLength()[d::X];
+          iK[d::Y] = iFP[d::Y] <= gSD::sLength()[d::Y] / 2 ? iFP[d::Y]
+                                                            : iFP[d::Y] - gSD::sLength()[d::Y];
+          iK[d::Z] = iFP[d::Z] <= gSD::sLength()[d::Z] / 2 ? iFP[d::Z]
+                                                            : iFP[d::Z] - gSD::sLength()[d::Z];
+          const unsigned kNorm = iK.norm();
+          spectra(iFP, lFD::getIndex(iFP), iK, kNorm);
+        }
+    spectra.executeBackward();
+    spectra.normalize();
+
+    const int DV = 2 * L::dimD - 3;
+    std::vector<double> an((size_t)DV * V + 3 + K, 0.0);
+    for (unsigned x = 0; x < lx; ++x)
+      for (unsigned y = 0; y < ly; ++y)
+        for (unsigned z = 0; z < lz; ++z) {
+          const Position iP{{x, y, z}};
+          for (int c = 0; c < DV; ++c)
+            an[(size_t)c * V + dense(x, y, z)] = fieldList.vorticity.getValue(iP, n, c);
+        }
+    an[(size_t)DV * V] = energy.scalar;
+    an[(size_t)DV * V + 1] = enstrophy.scalar;
+    an[(size_t)DV * V + 2] = (double)K;
+    for (unsigned k = 0; k < K; ++k) an[(size_t)DV * V + 3 + k] = spectra.spectra[k];
+    const std::string path = std::string(argv[2]) + ".analysis";
+    FILE* fa = std::fopen(path.c_str(), "wb");
+    if (!fa || std::fwrite(an.data(), sizeof(double), an.size(), fa) != an.size()) {
+      std::fprintf(stderr, "cannot write %s\n", path.c_str());
+      return 5;
+    }
+    std::fclose(fa);
+  }
   return 0;
 }

@@ -22,7 +22,9 @@ def run_reference(case: str, rho: np.ndarray, u: np.ndarray, steps: int) -> dict
     """Run reference case ``case`` from f = f_eq(rho, u) for ``steps`` steps.
 
     rho: [V]; u: [D, V] in dense reference node order. Returns f [Q, V], rho,
-    u (hydrodynamic), alpha, force, and the loop's wall seconds.
+    u (hydrodynamic), alpha, force, the loop's wall seconds, and the
+    reference's spectral analyses of the stored fields (vorticity, energy,
+    enstrophy, spectrum).
     """
     c = CASES[case]
     exe = compile_case(case, c)
@@ -39,6 +41,8 @@ def run_reference(case: str, rho: np.ndarray, u: np.ndarray, steps: int) -> dict
         subprocess.run([str(exe), str(fi), str(fo), str(int(steps))], check=True,
                        cwd=str(OUT / case), capture_output=True)
         out = np.fromfile(fo, dtype=np.float64)
+        fa = Path(str(fo) + ".analysis")
+        an = np.fromfile(fa, dtype=np.float64) if fa.exists() else None
     o = 0
 
     def take(n):
@@ -53,5 +57,14 @@ def run_reference(case: str, rho: np.ndarray, u: np.ndarray, steps: int) -> dict
     alpha = take(V)
     force = take(D * V).reshape(D, V)
     seconds = float(take(1)[0])
-    return {"f": f, "rho": rho_o, "u": u_o, "alpha": alpha, "force": force,
-            "seconds": seconds}
+    res = {"f": f, "rho": rho_o, "u": u_o, "alpha": alpha, "force": force,
+           "seconds": seconds}
+    if an is not None:
+        # the reference's spectral analyses of the stored fields (harness):
+        # vorticity [2D-3, V], energy, enstrophy, energy spectrum [maxWaveNumber]
+        nv = (2 * D - 3) * V
+        res["vorticity"] = an[:nv].reshape(2 * D - 3, V)
+        res["energy"], res["enstrophy"] = float(an[nv]), float(an[nv + 1])
+        K = int(an[nv + 2])
+        res["spectrum"] = an[nv + 3:nv + 3 + K]
+    return res

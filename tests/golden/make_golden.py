@@ -6,6 +6,8 @@ they exist) on small seeded inputs and stores inputs and outputs per case:
 
     <case>.npz : rho0 [V], u0 [D,V]          inputs (f starts at f_eq(rho0,u0))
                  f [Q,V], rho, u, alpha, force   reference state after `steps`
+                 vorticity [2D-3,V], energy, enstrophy, spectrum
+                                                 its spectral analyses of those fields
                  meta (json: the case parameters, steps, seeds)
 
 All arrays are float64 in dense reference node order (index (x*Ly+y)*Lz+z).
@@ -53,8 +55,12 @@ def main(only=None) -> None:
         rho, u, gen = case_inputs(name)
         ref = run_reference(name, rho, u, STEPS)
         meta = {"case": name, "steps": STEPS, "generator": gen, **asdict(CASES[name])}
+        # with the reference's spectral analyses of the stored fields: vorticity,
+        # total energy and enstrophy, shell energy spectrum (Analysis.h:33-177)
         np.savez_compressed(OUT / f"{name}.npz", rho0=rho, u0=u, f=ref["f"], rho=ref["rho"],
                             u=ref["u"], alpha=ref["alpha"], force=ref["force"],
+                            vorticity=ref["vorticity"], energy=ref["energy"],
+                            enstrophy=ref["enstrophy"], spectrum=ref["spectrum"],
                             meta=np.array(json.dumps(meta)))
         print(name, "alpha range", ref["alpha"].min(), ref["alpha"].max())
 

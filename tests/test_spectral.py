@@ -1,8 +1,77 @@
-"""Host spectral diagnostics (restatement of the reference's FFTW analyses)."""
+"""Host spectral diagnostics (restatement of the reference's FFTW analyses).
+
+Pinned against the reference itself: every golden vector carries the
+reference's vorticity, total energy, total enstrophy and shell energy
+spectrum of its stored fields (its Curl / TotalEnergy / TotalEnstrophy /
+PowerSpectra run by the oracle harness with the DFT stand-in for FFTW).
+"""
+import json
+
 import numpy as np
+import pytest
 
 from metalbm_gb300 import spectral
 from metalbm_gb300.fields import taylor_green
+
+from conftest import GOLDEN
+
+GOLDEN_CASES = sorted(p.stem for p in GOLDEN.glob("*.npz"))
+
+
+def _golden(case):
+    z = np.load(GOLDEN / f"{case}.npz")
+    meta = json.loads(str(z["meta"]))
+    D = 2 if meta["lattice"].startswith("D2") else 3
+    lx, ly, lz = meta["size"]
+    return z, (lx, ly, 1 if D == 2 else lz), D
+
+
+@pytest.mark.parametrize("case", GOLDEN_CASES)
+def test_analyses_match_reference(case):
+    """Reference-mode vorticity (with its 2-D real-part-only curl and extra
+    1/V), enstrophy, energy and shell spectrum of the reference's stored
+    fields equal the reference's own analyses to rounding (FFT against the
+    oracle's DFT): 1e-13 relative."""
+    z, shape, D = _golden(case)
+    w = spectral.vorticity(z["u"], shape, reference=True)
+    assert np.abs(w - z["vorticity"]).max() <= 1e-13 * np.abs(z["vorticity"]).max()
+    assert abs(spectral.enstrophy(z["u"], shape, reference=True) - float(z["enstrophy"])) <= \
+        1e-13 * float(z["enstrophy"])
+    assert abs(spectral.energy(z["rho"], z["u"]) - float(z["energy"])) <= 1e-13 * float(z["energy"])
+    sp = np.asarray(spectral.energy_spectrum(z["u"], shape, reference=True))
+    ref = z["spectrum"]
+    assert sp.shape == ref.shape
+    assert np.abs(sp - ref).max() <= 1e-13 * np.abs(ref).max()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", ["d2q9_bgk_guo_kolmogorov", "d3q19_bgk_guo_kolmogorov",
+                                  "d3q27_elbm_none_none"])
+def test_analyses_on_the_gpu_match_reference(case):
+    """The same analyses on the device (cuFFT through torch) from the GPU
+    step's stored fields, and the step's fused energy reduction, against the
+    reference's analyses of its own run."""
+    import torch
+    from metalbm_gb300 import InputDeck, Lattice
+    z, shape, D = _golden(case)
+    meta = json.loads(str(z["meta"]))
+    deck = InputDeck(latticeT=meta["lattice"], collisionT=meta["collision"],
+                     forcingSchemeT=meta["forcing"], forceT=meta["force"],
+                     relaxationTime=meta["tau"], forceAmplitude=tuple(meta["amp"]),
+                     forceWaveLength=tuple(meta["wavelength"]), globalLength=tuple(meta["size"]))
+    with Lattice(deck) as lat:
+        lat.init_equilibrium(z["rho0"], z["u0"])
+        lat.step(meta["steps"], store=True, diagnostics=True)
+        fl, d = lat.fields(), lat.diagnostics()
+    u = torch.from_numpy(fl["u"]).cuda()
+    w = spectral.vorticity(u, shape, reference=True)
+    w = w.cpu().numpy() if hasattr(w, "cpu") else np.asarray(w)
+    tol = 1e-13 if meta["collision"] == "BGK" else 1e-11
+    assert np.abs(w - z["vorticity"]).max() <= tol * np.abs(z["vorticity"]).max()
+    sp = spectral.energy_spectrum(u, shape, reference=True)
+    sp = sp.cpu().numpy() if hasattr(sp, "cpu") else np.asarray(sp)
+    assert np.abs(sp - z["spectrum"]).max() <= tol * np.abs(z["spectrum"]).max()
+    assert abs(d["energy"] - float(z["energy"])) <= tol * float(z["energy"])
 
 
 def test_vorticity_of_taylor_green():
@@ -48,6 +117,14 @@ def test_reference_2d_curl_keeps_real_part_only():
     re = (1j * (kx * uh[1] - ky * uh[0])).real
     expect = np.fft.irfftn(re + 0j, s=(16, 12)).ravel() / (16 * 12)
     assert np.abs(w[0] - expect).max() < 1e-14
+
+
+def test_reference_shell_count_takes_the_min_of_the_rest():
+    """The reference's maxWaveNumber: max(L_x, min(L_y, L_z)) / 2."""
+    assert spectral.reference_shell_count((8, 10, 9)) == 4
+    assert spectral.reference_shell_count((12, 10, 8)) == 6
+    assert spectral.reference_shell_count((16, 20, 1)) == 8
+    assert spectral.reference_shell_count((32, 32, 32)) == 16
 
 
 def test_energy_spectrum_single_shell_and_parseval():
