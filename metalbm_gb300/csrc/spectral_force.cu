@@ -605,7 +605,7 @@ int spectral_force_create(SpectralForce** out, int force, int D, int lx, int ly,
                            CUFFT_Z2D, D)) != CUFFT_SUCCESS)
       return bail("cufftPlanMany Z2D failed", (int)r);
     sf->have_inv = true;
-    cufftSetStream(sf->inv, s);
+    if ((r = cufftSetStream(sf->inv, s)) != CUFFT_SUCCESS) return bail("cufftSetStream failed", (int)r);
     if ((e = cudaMalloc(&sf->spec, sizeof(cufftDoubleComplex) * g.nspec * D)) != cudaSuccess)
       return bail("device allocation failed", (int)e);
   }
@@ -636,15 +636,16 @@ int spectral_force_create(SpectralForce** out, int force, int D, int lx, int ly,
                            CUFFT_D2Z, D)) != CUFFT_SUCCESS)
       return bail("cufftPlanMany D2Z failed", (int)r);
     sf->have_fwd = true;
-    cufftSetStream(sf->fwd, s);
+    if ((r = cufftSetStream(sf->fwd, s)) != CUFFT_SUCCESS) return bail("cufftSetStream failed", (int)r);
     if ((e = cudaMalloc(&sf->mom, sizeof(double) * sf->V * D)) != cudaSuccess)
       return bail("device allocation failed", (int)e);
     if (injection) {
       // the injection spectrum is kept: Z2D overwrites its input every step
       if ((e = cudaMalloc(&sf->inject, sizeof(cufftDoubleComplex) * g.nspec * D)) != cudaSuccess)
         return bail("device allocation failed", (int)e);
-      cudaMemcpyAsync(sf->inject, sf->spec, sizeof(cufftDoubleComplex) * g.nspec * D,
-                      cudaMemcpyDeviceToDevice, s);
+      if ((e = cudaMemcpyAsync(sf->inject, sf->spec, sizeof(cufftDoubleComplex) * g.nspec * D,
+                             cudaMemcpyDeviceToDevice, s)) != cudaSuccess)
+      return bail("injection copy failed", (int)e);
     }
   }
   if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return bail("spectral setup failed", (int)e);
