@@ -114,3 +114,30 @@ def solenoidal_shell(shape, kmin: float, kmax: float, amplitude: float, seed: in
     if peak > 0:
         u *= amplitude / peak
     return u.reshape(3, -1)
+
+
+def reference_initial_fields(shape, dims: int, density_type: str = "Homogeneous",
+                             density_value: float = 1.0, velocity_type: str = "Homogeneous",
+                             velocity_vector=(0.0, 0.0, 0.0)):
+    """The reference's initial fields (initDensity / initVelocity,
+    Initialize.h:19-68): density `density_value` everywhere, or for "Peak"
+    three times that value at the single node
+    ((Lx - 1) 0.4, (Ly - 1) 0.3, (Lz - 1) 0.2) (each truncated to an
+    integer); velocity `velocity_vector` (its first `dims` components)
+    everywhere. The reference's other velocity types (Perturbated, Wave,
+    Decay) have no implementation there: it prints an error and keeps the
+    homogeneous field, and so does this function."""
+    lx, ly, lz = shape
+    V = lx * ly * lz
+    rho = np.full(V, float(density_value))
+    if density_type == "Peak":
+        cx, cy, cz = int((lx - 1) * 0.4), int((ly - 1) * 0.3), int((lz - 1) * 0.2)
+        rho[(cx * ly + cy) * lz + cz] = 3.0 * float(density_value)
+    elif density_type != "Homogeneous":
+        raise ValueError(f"unknown initDensityT {density_type!r}")
+    if velocity_type not in ("Homogeneous", "Perturbated", "Wave", "Decay"):
+        raise ValueError(f"unknown initVelocityT {velocity_type!r}")
+    u = np.empty((dims, V))
+    for d in range(dims):
+        u[d] = float(velocity_vector[d])
+    return rho, u

@@ -54,6 +54,11 @@ class InputDeck:
     # reference is axis = 1 (y), component = 0 (x), Force.h:262-267.
     kolmogorovAxis: int = 1
     kolmogorovComponent: int = 0
+    # initial fields (src/Input_prod.in:43-46, Initialize.h:19-68)
+    initDensityT: str = "Homogeneous"
+    initDensityValue: float = 1.0
+    initVelocityT: str = "Homogeneous"
+    initVelocityVector: tuple = (0.0, 0.0, 0.0)
     # spectral forces (src/Input_prod_3d.in:50-58): integer wavenumber shells
     forcekMin: int = 1
     forcekMax: int = 2
@@ -74,6 +79,7 @@ class InputDeck:
         self.forceWaveLength = tuple(self.forceWaveLength)
         self.globalLength = tuple(self.globalLength)
         self.removalForceAmplitude = tuple(self.removalForceAmplitude)
+        self.initVelocityVector = tuple(self.initVelocityVector)
 
     @property
     def Q(self) -> int:
@@ -224,6 +230,15 @@ class Lattice:
         self._check(self._lib.mlbm_set_stream(self._h, ct.c_void_p(stream_ptr or 0)))
 
     # --- state
+    def initialize(self):
+        """f = f_eq of the deck's initial fields (initDensity / initVelocity,
+        then initDistribution, Initialize.h:19-116)."""
+        from .fields import reference_initial_fields
+        d = self.deck
+        rho, u = reference_initial_fields(self.shape, self.D, d.initDensityT, d.initDensityValue,
+                                          d.initVelocityT, d.initVelocityVector)
+        self.init_equilibrium(rho, u)
+
     def init_equilibrium(self, rho: np.ndarray, u: np.ndarray, layout: int = capi.LAYOUT_DENSE):
         rho = np.ascontiguousarray(rho, np.float64)
         u = np.ascontiguousarray(u, np.float64)

@@ -123,3 +123,28 @@ def test_registered_host_buffers_round_trip():
                                         o_u.ctypes.data_as(dp), None, None, 0) == 0
         ref = lat.fields()
     assert np.array_equal(o_rho, ref["rho"]) and np.array_equal(o_u, ref["u"])
+
+
+@pytest.mark.gpu
+def test_deck_initial_fields_step_like_the_oracle():
+    """Lattice.initialize() from the deck's initDensityT = Peak and a
+    homogeneous initVelocityVector (Initialize.h:19-116), then BGK steps with
+    Guo / Kolmogorov: bit-identical to the oracle from the same fields."""
+    from metalbm_gb300 import InputDeck, Lattice
+    from metalbm_gb300.fields import reference_initial_fields
+    from oracle import OracleConfig, OraclePort
+    shape = (16, 12, 10)
+    deck = InputDeck(latticeT="D3Q19", forcingSchemeT="Guo", forceT="Kolmogorov",
+                     relaxationTime=0.6, forceAmplitude=(1e-4, 0, 0), forceWaveLength=(6.0, 1, 1),
+                     globalLength=shape, initDensityT="Peak", initDensityValue=1.0,
+                     initVelocityVector=(0.01, -0.005, 0.002))
+    with Lattice(deck) as lat:
+        lat.initialize()
+        lat.step(5)
+        f = lat.populations()
+    rho, u = reference_initial_fields(shape, 3, "Peak", 1.0, "Homogeneous", (0.01, -0.005, 0.002))
+    port = OraclePort(OracleConfig(lattice="D3Q19", forcing="Guo", force="Kolmogorov", tau=0.6,
+                                   amplitude=(1e-4, 0, 0), wavelength=(6.0, 1, 1), size=shape))
+    port.init_equilibrium(rho, u)
+    port.step(5)
+    assert np.array_equal(f, port.populations())

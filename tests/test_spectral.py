@@ -140,3 +140,17 @@ def test_energy_spectrum_single_shell_and_parseval():
     E = spectral.energy_spectrum(tg, shape)
     assert abs(E.sum() - 0.5 * (tg ** 2).sum()) < 1e-12 * V
     assert np.argmax(E) == 1  # |k| = sqrt(2) -> shell 1
+
+
+def test_reference_initial_fields_known_answers():
+    """initDensity / initVelocity (Initialize.h:19-68): the Peak node and the
+    homogeneous velocity."""
+    from metalbm_gb300.fields import reference_initial_fields
+    rho, u = reference_initial_fields((20, 12, 1), 2, "Peak", 1.5, "Homogeneous", (0.01, -0.02, 0.0))
+    peak = (int(19 * 0.4) * 12 + int(11 * 0.3)) * 1 + 0
+    assert rho[peak] == 4.5 and np.count_nonzero(rho != 1.5) == 1
+    assert (u[0] == 0.01).all() and (u[1] == -0.02).all() and u.shape == (2, 240)
+    rho, u = reference_initial_fields((8, 6, 5), 3, "Peak")
+    assert rho[(int(7 * 0.4) * 6 + int(5 * 0.3)) * 5 + int(4 * 0.2)] == 3.0
+    with pytest.raises(ValueError):
+        reference_initial_fields((4, 4, 4), 3, "Gaussian")
