@@ -1,22 +1,21 @@
 // Spectral forces (Force.h:294-626): ConstantShell, EnergyRemoval and
-// Turbulent2D as a per-node force field [D][V] that the FP64 step kernels
-// read (FORCE_FIELD in node_force).
+// Turbulent2D as a per-node force field [D][V] that the step kernels read
+// (FORCE_FIELD in node_force / node_force_float).
 //
 // The reference computes them with FFTW r2c/c2r transforms on the host
-// (Transformer.h:19-110). Here the transforms are cuFFT D2Z/Z2D plans batched
-// over the D components, and everything between them is one kernel pass over
-// the half spectrum:
-//   * ConstantShell: the spectrum A on the shell kmin^2 <= |k|^2 <= kmax^2
-//     (integer wavenumbers, Force.h:339-347, 386), made solenoidal by the curl
-//     i k x T (3-D, Transformer.h:207-272) or (i k_y psi, -i k_x psi) (2-D,
-//     Transformer.h:298-387), divided by the node count (the backward
-//     transform's normalisation, Transformer.h:98-108) and transformed back
-//     once, at creation;
-//   * EnergyRemoval: every step, the momentum rho u of the last stored fields
-//     (Force.h:442-463), forward transform, -A_d on the shell and 0 elsewhere
-//     (Force.h:496-532), divided by the node count, backward transform;
-//   * Turbulent2D: the two added (Force.h:596-612), in the spectrum, so one
-//     backward transform serves both.
+// (Transformer.h:19-110). Here:
+//   * ConstantShell (and Turbulent2D's injection part): the spectrum A on the
+//     shell kmin^2 <= |k|^2 <= kmax^2 (integer wavenumbers, Force.h:339-347,
+//     386), made solenoidal by the curl i k x T (3-D, Transformer.h:207-272)
+//     or (i k_y psi, -i k_x psi) (2-D, Transformer.h:298-387), divided by the
+//     node count (the backward transform's normalisation,
+//     Transformer.h:98-108): one batched cuFFT Z2D at creation.
+//   * EnergyRemoval (and Turbulent2D's removal part): -A_d times the momentum
+//     rho u of the last stored fields filtered to the shell (Force.h:442-532).
+//     Shells up to k = 5 use the separable partial transforms below (sums
+//     along the contiguous axis, then the two others, the filter, and back;
+//     FP32 per-node stages for FP32/FP16 storage); larger shells use batched
+//     cuFFT D2Z, one filter pass and Z2D.
 // Every spectrum stays Hermitian: the reference's partner writes on the
 // k_y = k_z = 0 row of 3-D lattices, which index y = L_y and land one row off
 // (or past the array), are not reproduced. Shells stay below the Nyquist
