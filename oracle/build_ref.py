@@ -122,6 +122,12 @@ CASES: dict[str, RefCase] = {
                                            (2e-4, 1e-4, -1e-4), (1.0, 1.0, 1.0), (8, 10, 9)),
     "d3q33_elbm_none_none": RefCase("D3Q33", "ELBM", "None", "None", 0.500250125062531,
                                     (0.0, 0.0, 0.0), (1.0, 1.0, 1.0), (12, 10, 8)),
+    "d3q33_elbm_edm_constant": RefCase("D3Q33", "ELBM", "ExactDifferenceMethod", "Constant", 0.51,
+                                       (1e-4, -2e-4, 1e-4), (1.0, 1.0, 1.0), (10, 9, 8)),
+    "d3q15_bgk_edm_kolmogorov": RefCase("D3Q15", "BGK", "ExactDifferenceMethod", "Kolmogorov",
+                                        0.62, (1e-3, 0.0, 0.0), (7.0, 1.0, 1.0), (9, 14, 8)),
+    "d2q13_bgk_shanchen_constant": RefCase("D2Q13", "BGK", "ShanChen", "Constant", 0.68,
+                                           (2e-4, -1e-4, 0.0), (1.0, 1.0, 1.0), (18, 14, 1)),
     # 2-D spectral forces (Force.h:294-626), with the DFT stand-in of
     # oracle/ref_stub/fftw3-mpi.h; well defined in 2-D (the 3-D partner writes
     # are out of range)
