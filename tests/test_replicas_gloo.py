@@ -33,3 +33,26 @@ def test_max_over_ranks_and_job_value_two_ranks():
         p.join(timeout=60)
     assert [o[1] for o in out] == [150.0, 150.0]
     assert out[0][2] == pytest.approx(2 * 1000 * 10 / 0.150 / 1e6)
+
+
+@pytest.mark.parametrize("workload", ["bgk_d3q19_f64_256", "turbulent_d3q27_f32_256"])
+def test_reference_arm_prints_the_contract_line(workload):
+    """`bench.py --impl reference` (the reference's CPU algorithm, the C
+    restatement, on the host cores): one JSON line with the arm's metric,
+    unit, cpu_baseline and a zero-copy e2e, on CPU."""
+    import json
+    import subprocess
+    import sys
+    from conftest import ROOT
+    r = subprocess.run([sys.executable, str(ROOT / "bench.py"), "--impl", "reference",
+                        "--workload", workload, "--steps", "1", "--warmup", "3"],
+                       capture_output=True, text=True, timeout=600, cwd=str(ROOT))
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [l for l in r.stdout.splitlines() if l.startswith("{")]
+    assert len(lines) == 1
+    d = json.loads(lines[0])
+    assert d["impl"] == "reference" and d["unit"] == "MLUPS" and d["value"] > 0
+    assert d["cpu_baseline"]["value"] == d["value"] and d["cpu_baseline"]["kind"] == "port"
+    assert d["e2e"] == {"value": d["value"], "unit": "MLUPS", "h2d_bytes_per_step": 0,
+                        "d2h_bytes_per_step": 0}
+    assert d["config"]["workload"] == workload
