@@ -81,6 +81,69 @@ class InputDeck:
         self.removalForceAmplitude = tuple(self.removalForceAmplitude)
         self.initVelocityVector = tuple(self.initVelocityVector)
 
+    @classmethod
+    def from_reference_deck(cls, source, lengths=None, **overrides) -> "InputDeck":
+        """An InputDeck from a reference deck (`src/Input_*.in`: a C++ header
+        of `constexpr <type> <name> = <value>;` definitions), as text or a
+        path. The hot path's parameters are taken over (lattice, collision,
+        forcing, force and their amplitudes / wavelengths / shells, relaxation
+        time, initial fields, lengths); lengths given as compile-time macros
+        (GLOBAL_LENGTH_X ...) come from `lengths`. Choices this library does
+        not implement raise ValueError: a non-Pull algorithm and an
+        equilibrium other than TruncationMa3 (`Incompressible`, named by
+        several shipped decks, is not an EquilibriumType of Options.h:31, so
+        those decks do not compile in the reference either)."""
+        import re
+        from pathlib import Path
+        text = str(source)
+        if "constexpr" not in text and Path(text).exists():
+            text = Path(text).read_text()
+        defs = {}
+        for line in text.splitlines():
+            line = line.split("//")[0]
+            m = re.match(r"\s*constexpr\s+[\w:<>]+(?:\s+int)?\s+(\w+)\s*=\s*(.+?);", line)
+            if m:
+                defs[m.group(1)] = m.group(2).strip()
+
+        def enum(name):
+            return defs[name].split("::")[-1]
+
+        def vec(name):
+            return tuple(float(v) for v in re.findall(r"[-+0-9.eE]+", defs[name]))
+
+        if "algorithmT" in defs and enum("algorithmT") != "Pull":
+            raise ValueError(f"algorithmT {enum('algorithmT')}: only the pull algorithm is built")
+        if "equilibriumT" in defs and enum("equilibriumT") != "TruncationMa3":
+            raise ValueError(f"equilibriumT {enum('equilibriumT')}: only TruncationMa3 is built "
+                             "(Options.h:31 has no Incompressible)")
+        kw = {}
+        for key in ("latticeT", "collisionT", "forcingSchemeT", "forceT", "initDensityT",
+                    "initVelocityT"):
+            if key in defs:
+                kw[key] = enum(key)
+        for key in ("relaxationTime", "initDensityValue"):
+            if key in defs:
+                kw[key] = float(defs[key])
+        for key in ("forcekMin", "forcekMax", "removalForcekMin", "removalForcekMax"):
+            if key in defs:
+                kw[key] = int(defs[key])
+        for key in ("forceAmplitude", "forceWaveLength", "removalForceAmplitude",
+                    "initVelocityVector"):
+            if key in defs:
+                kw[key] = vec(key)
+        length = []
+        for d, key in enumerate(("globalLengthX", "globalLengthY", "globalLengthZ")):
+            v = defs.get(key, "1")
+            if re.fullmatch(r"\d+", v):
+                length.append(int(v))
+            elif lengths is not None:
+                length.append(int(lengths[d]))
+            else:
+                raise ValueError(f"{key} = {v}: give the lengths (lengths=(Lx, Ly, Lz))")
+        kw["globalLength"] = tuple(length)
+        kw.update(overrides)
+        return cls(**kw)
+
     @property
     def Q(self) -> int:
         return Q_OF[self.latticeT]

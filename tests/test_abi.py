@@ -140,3 +140,46 @@ def test_spectral_force_configurations_are_checked(lib):
     c.force = 7
     assert lib.mlbm_create(ct.byref(c), ct.byref(h)) == capi.ERR_INVALID
     assert c.removal_kmin == 1 and c.removal_kmax == 2 and c.removal_amplitude[0] == 1e-6
+
+
+def test_input_deck_from_a_reference_deck():
+    """The reference's deck syntax (constexpr definitions, src/Input_prod.in:9-79)
+    read into an InputDeck; macro lengths from the caller; unsupported choices
+    refused with the reason."""
+    from metalbm_gb300.lattice import InputDeck
+    deck_text = """
+    namespace lbm {
+      constexpr LatticeType latticeT = LatticeType::D3Q27;
+      constexpr int globalLengthX = GLOBAL_LENGTH_X;  // set by CMake
+      constexpr int globalLengthY = GLOBAL_LENGTH_Y;
+      constexpr int globalLengthZ = GLOBAL_LENGTH_Z;
+      constexpr AlgorithmType algorithmT = AlgorithmType::Pull;
+      constexpr dataT relaxationTime = 0.55;
+      constexpr CollisionType collisionT = CollisionType::BGK;
+      constexpr EquilibriumType equilibriumT = EquilibriumType::TruncationMa3;
+      constexpr InitDensityType initDensityT = InitDensityType::Peak;
+      constexpr dataT initDensityValue = 1.0;
+      constexpr Vector initVelocityVector = { {0.0, 1e-3, 0.0} };
+      constexpr ForcingSchemeType forcingSchemeT = ForcingSchemeType::ExactDifferenceMethod;
+      constexpr ForceType forceT = ForceType::ConstantShell;
+      constexpr Vector forceAmplitude = { {1e1, 1e1, 1e1} };
+      constexpr Vector forceWaveLength = { {32.0, 32.0, 32.0} };
+      constexpr int forcekMin = 1;
+      constexpr int forcekMax = 2;
+      constexpr Vector removalForceAmplitude = { {1.e-6, 1.e-6, 1.e-6} };
+      constexpr unsigned int writeStep = 2000;
+    }
+    """
+    d = InputDeck.from_reference_deck(deck_text, lengths=(64, 48, 32), storage="f32")
+    assert (d.latticeT, d.collisionT, d.forcingSchemeT, d.forceT) == (
+        "D3Q27", "BGK", "ExactDifferenceMethod", "ConstantShell")
+    assert d.relaxationTime == 0.55 and d.globalLength == (64, 48, 32) and d.storage == "f32"
+    assert d.forceAmplitude == (10.0, 10.0, 10.0) and (d.forcekMin, d.forcekMax) == (1, 2)
+    assert d.removalForceAmplitude == (1e-6, 1e-6, 1e-6) and d.initDensityT == "Peak"
+    assert d.initVelocityVector == (0.0, 1e-3, 0.0)
+    d.to_c()  # a valid configuration
+    with pytest.raises(ValueError, match="lengths"):
+        InputDeck.from_reference_deck(deck_text)
+    with pytest.raises(ValueError, match="TruncationMa3"):
+        InputDeck.from_reference_deck(deck_text.replace("TruncationMa3", "Incompressible"),
+                                      lengths=(8, 8, 8))
