@@ -432,8 +432,8 @@ def run_ours(args):
                 "traffic_source": prof.get("source")}
     if "fp64_inst_per_node" in prof:
         # the kernel's binding roof: GB300's FP64 pipe (no FP64 figure in
-        # MEASURED_PEAKS.json; the peak is the DFMA rate measured by
-        # metalbm_gb300/cpp/fp64_throughput.cu on this pool)
+        # MEASURED_PEAKS.json; the peak is the DFMA rate of a throughput
+        # probe on a GB300, profiles/fp64_throughput_gb300.md)
         gops = prof["fp64_inst_per_node"] * V / (avg_launch_ms * 1e-3) / 1e9
         roofline["fp64_pipe"] = {"achieved": gops, "peak": prof["fp64_peak_gops"],
                                  "unit": "G FP64 instr/s", "frac": gops / prof["fp64_peak_gops"],

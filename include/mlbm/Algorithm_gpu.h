@@ -65,12 +65,28 @@ class AlgorithmGPU {
   }
 
   // Algorithm::iterate: one fused pull step; when isStored, the step stores
-  // rho, the hydrodynamic velocity, alpha and F (Algorithm.h:150-194).
+  // rho, the hydrodynamic velocity, alpha and F (Algorithm.h:150-194). The
+  // wait for the device is bounded by syncTimeoutMs: past it, mlbm::Error with
+  // code MLBM_ERR_TIMEOUT (the handle stays usable; the step still completes).
   void iterate(unsigned int /*iteration*/) {
     const auto t0 = std::chrono::steady_clock::now();
     check(mlbm_step(h_, 1, isStored ? MLBM_STEP_STORE_FIELDS : 0u), h_);
-    check(mlbm_sync(h_, -1), h_);
+    check(mlbm_sync(h_, syncTimeoutMs), h_);
     dtComputation_ = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  }
+
+  // The reference's signature, so that Routine::compute's call site
+  // (Routine.h:126) compiles unchanged: iterate(iteration, defaultStream,
+  // bulkStream, leftStream, rightStream, leftEvent, rightEvent)
+  // (Algorithm.h:326-358). The streams and events order the reference's
+  // halo exchange against its bulk sweep; the periodic wrap is inside the
+  // kernel here, so they are not used and the step runs on the handle's
+  // stream.
+  template <class StreamT, class EventT>
+  void iterate(unsigned int iteration, StreamT& /*defaultStream*/, StreamT& /*bulkStream*/,
+               StreamT& /*leftStream*/, StreamT& /*rightStream*/, EventT& /*leftEvent*/,
+               EventT& /*rightEvent*/) {
+    iterate(iteration);
   }
 
   // The stored fields of the last isStored step into FieldList arrays
@@ -95,6 +111,8 @@ class AlgorithmGPU {
 
  public:
   bool isStored;
+  // Limit of each wait for the device in iterate, milliseconds (< 0: none).
+  int syncTimeoutMs = 600000;
 
  private:
   double dtComputation_;

@@ -156,7 +156,12 @@ typedef struct {
   int removal_kmin;           /* removalForcekMin, reference 1 */
   int removal_kmax;           /* removalForcekMax, reference 2 */
   double removal_amplitude[3]; /* removalForceAmplitude, reference 1e-6 */
-  int reserved[4];
+  /* RESIDUAL alpha solver: iteration cap of the safeguarded bisection-Newton
+   * (0: newton_max_iterations, as the reference passes one iterationMax to
+   * both solvers, Collision.h:336-341, 892-897). With newton_max_iterations = 0
+   * every node whose guess fails goes straight to the bracketed solver. */
+  int bisection_max_iterations;
+  int reserved[3];
 } mlbm_config;
 
 typedef struct {
@@ -310,10 +315,11 @@ unsigned long long mlbm_kernel_launch_count(void);
  * sum 1/2 rho |u|^2 (divide by V for mlbm_diag.energy), max Mach, 2, 2} and,
  * if non-NULL, the device error word to *error_word_out. Enqueued on
  * `stream` (a cudaStream_t; NULL = legacy default stream) on the current
- * device; returns before the work completes. The first call on a device looks
- * up the scratch's device address (cudaGetSymbolAddress), so make it before
- * any stream capture. Every call shares the scratch: calls that overlap on
- * the GPU race. Errors: mlbm_last_error(NULL). */
+ * device; returns before the work completes. Every call looks up the
+ * scratch's device address (cudaGetSymbolAddress, no allocation); the first
+ * call on a device also loads the library's device code there, so make that
+ * first call before any stream capture. Every call shares the scratch: calls
+ * that overlap on the GPU race. Errors: mlbm_last_error(NULL). */
 int mlbm_step_f64_noalloc(const mlbm_config* cfg, const double* f_in, double* f_out,
                           const double* force_profile, double* diag_out,
                           unsigned int* error_word_out, void* stream);

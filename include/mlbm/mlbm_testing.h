@@ -30,6 +30,17 @@ int mlbm_testing_entropy(int lattice, const float* f, const double* fneq, long l
  * in double-float arithmetic (dfloat = 1) or FP64 (dfloat = 0). Host arrays. */
 int mlbm_testing_neq(int lattice, const float* f, long long nodes, int dfloat, double* fneq);
 
+/* The FP64 entropic step's alpha for n single nodes given as pulled
+ * populations f[n][Q] and non-equilibrium parts fneq[n][Q] (FP64): alpha_max
+ * and the 0.95 alpha_max limiter (Collision.h:305-326, 362-367), then the
+ * RESIDUAL solve from guess[n] (|F| <= tol; Newton capped at newton_maxit,
+ * the bisection-Newton of EntropicStep.h:142-220 at bisect_maxit), with the
+ * deviation shortcut off. flags[n]: 1 limited, 2 the bracketed solver ran,
+ * 4 alpha = 2 fallback. Host arrays; allocates temporary device buffers. */
+int mlbm_testing_alpha_solve(int lattice, double tol, int newton_maxit, int bisect_maxit,
+                             long long n, const double* f, const double* fneq,
+                             const double* guess, double* alpha, int* flags);
+
 #ifdef __cplusplus
 }
 #endif

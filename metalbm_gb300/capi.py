@@ -36,7 +36,8 @@ EXPORTS = [
     "mlbm_last_error", "mlbm_kernel_launch_count", "mlbm_step_f64_noalloc",
     "mlbm_get_alpha", "mlbm_set_alpha",
 ]
-TESTING_EXPORTS = ["mlbm_testing_fast_log", "mlbm_testing_entropy", "mlbm_testing_neq"]
+TESTING_EXPORTS = ["mlbm_testing_fast_log", "mlbm_testing_entropy", "mlbm_testing_neq",
+                   "mlbm_testing_alpha_solve"]
 
 
 class Config(ct.Structure):
@@ -49,7 +50,8 @@ class Config(ct.Structure):
                 ("newton_max_iterations", ct.c_int), ("deviation_threshold", ct.c_double),
                 ("device", ct.c_int), ("force_kmin", ct.c_int), ("force_kmax", ct.c_int),
                 ("removal_kmin", ct.c_int), ("removal_kmax", ct.c_int),
-                ("removal_amplitude", ct.c_double * 3), ("reserved", ct.c_int * 4)]
+                ("removal_amplitude", ct.c_double * 3), ("bisection_max_iterations", ct.c_int),
+                ("reserved", ct.c_int * 3)]
 
 
 class Diag(ct.Structure):
@@ -124,6 +126,8 @@ def load(path: Path | str | None = None):
         "mlbm_testing_entropy": ([ct.c_int, fp, dp, ct.c_longlong, dp, ct.c_int, ct.c_int, dp,
                                   dp, ct.POINTER(ct.c_int)], ct.c_int),
         "mlbm_testing_neq": ([ct.c_int, fp, ct.c_longlong, ct.c_int, dp], ct.c_int),
+        "mlbm_testing_alpha_solve": ([ct.c_int, ct.c_double, ct.c_int, ct.c_int, ct.c_longlong,
+                                      dp, dp, dp, dp, ct.POINTER(ct.c_int)], ct.c_int),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)

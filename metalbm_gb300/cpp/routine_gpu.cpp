@@ -7,9 +7,10 @@
 //
 // Usage: routine_gpu <in.bin> <out.bin> <steps> <lattice 0..5> <collision 0..7>
 //                    <forcing 0..3> <force 0..3> <tau> <ax> <ay> <az> <lx> <ly> <lz>
-//                    <Lx> <Ly> <Lz>
+//                    <Lx> <Ly> <Lz> [<sync timeout ms> [<alpha solver 0..1>]]
 //   in.bin : float64 rho[V], u[D][V] dense (index (x*Ly+y)*Lz+z)
 //   out.bin: float64 f[Q][V], rho[V], u[D][V], alpha[V], force[D][V], seconds
+// Exit status: 0 done, 5 an mlbm error, 6 a wait for the device timed out.
 #include <cstdio>
 #include <cstdlib>
 #include <vector>
@@ -17,7 +18,7 @@
 #include "mlbm/Algorithm_gpu.h"
 
 int main(int argc, char** argv) {
-  if (argc != 18) {
+  if (argc < 18 || argc > 20) {
     std::fprintf(stderr, "usage: see the header of routine_gpu.cpp\n");
     return 2;
   }
@@ -33,6 +34,14 @@ int main(int argc, char** argv) {
     cfg.force_amplitude[d] = std::atof(argv[9 + d]);
     cfg.force_wavelength[d] = std::atof(argv[12 + d]);
     cfg.length[d] = std::atoi(argv[15 + d]);
+  }
+  const int timeout_ms = argc > 18 ? std::atoi(argv[18]) : 600000;
+  if (argc > 19) {  // the bracketed residual solver at 1e-12 instead of the reference's
+    cfg.alpha_mode = std::atoi(argv[19]);
+    if (cfg.alpha_mode == MLBM_ALPHA_RESIDUAL) {
+      cfg.newton_tolerance = 1e-12;
+      cfg.deviation_threshold = 0.0;
+    }
   }
   if (cfg.lattice < MLBM_D2Q9 || cfg.lattice > MLBM_D3Q33) {
     std::fprintf(stderr, "bad lattice %d\n", cfg.lattice);
@@ -61,13 +70,19 @@ int main(int argc, char** argv) {
         for (int c = 0; c < D; ++c) velocity[c * n + ref(x, y, z)] = in[(1 + c) * V + dense(x, y, z)];
       }
 
+  // Stand-ins for the reference's Stream<arch> / Event<arch> (Routine.h:35-42):
+  // the drop-in's iterate takes them and does not use them.
+  struct Stream {} defaultStream, bulkStream, leftStream, rightStream;
+  struct Event {} leftEvent, rightEvent;
   try {
     mlbm::AlgorithmGPU algorithm(cfg);
+    algorithm.syncTimeoutMs = timeout_ms;
     algorithm.initialize(density.data(), velocity.data());
     double seconds = 0.0;
     for (int it = 1; it <= steps; ++it) {
       algorithm.isStored = (it == steps);
-      algorithm.iterate(it);
+      algorithm.iterate(it, defaultStream, bulkStream, leftStream, rightStream, leftEvent,
+                        rightEvent);
       seconds += algorithm.getComputationTime();
     }
     std::vector<double> distribution((size_t)Q * n, 0.0), alpha(n), force((size_t)D * n);
@@ -95,7 +110,7 @@ int main(int argc, char** argv) {
     std::fclose(fo);
   } catch (const mlbm::Error& e) {
     std::fprintf(stderr, "mlbm error %d: %s\n", e.code, e.what());
-    return 5;
+    return e.code == MLBM_ERR_TIMEOUT ? 6 : 5;
   }
   return 0;
 }

@@ -360,7 +360,7 @@ extern "C" int mlbm_create(const mlbm_config* cfg, mlbm_handle** out) {
   if (c.alpha_guess < 0 || c.alpha_guess > 2) return fail(nullptr, MLBM_ERR_INVALID, "bad alpha guess");
   if (c.alpha_guess == MLBM_GUESS_LEARNED && c.storage == MLBM_STORAGE_F64)
     return fail(nullptr, MLBM_ERR_INVALID, "the learned alpha guess runs with FP32/FP16 storage");
-  if (c.newton_max_iterations < 0 || !(c.newton_tolerance >= 0))
+  if (c.newton_max_iterations < 0 || c.bisection_max_iterations < 0 || !(c.newton_tolerance >= 0))
     return fail(nullptr, MLBM_ERR_INVALID, "bad Newton parameters");
   const int D = kD[c.lattice];
   long long L[3] = {c.length[0], c.length[1], D == 2 ? 1 : c.length[2]};
@@ -563,6 +563,8 @@ extern "C" int mlbm_create(const mlbm_config* cfg, mlbm_handle** out) {
   p.guess_mode = c.alpha_guess;
   p.newton_tol = c.newton_tolerance;
   p.newton_maxit = c.newton_max_iterations;
+  p.bisect_maxit = c.bisection_max_iterations > 0 ? c.bisection_max_iterations
+                                                  : c.newton_max_iterations;
   p.deviation_threshold = c.deviation_threshold;
   p.deviation_threshold_f = (float)c.deviation_threshold;
   p.rho_out = h->rho;
@@ -1058,6 +1060,52 @@ extern "C" int mlbm_testing_entropy(int lattice, const float* f, const double* f
   if (e == cudaSuccess) e = cudaMemcpy(series, dS, ns, cudaMemcpyDeviceToHost);
   release();
   if (e != cudaSuccess) return fail(nullptr, MLBM_ERR_CUDA, "entropy test: %s", cudaGetErrorString(e));
+  return MLBM_OK;
+}
+
+extern "C" int mlbm_testing_alpha_solve(int lattice, double tol, int newton_maxit,
+                                        int bisect_maxit, long long n, const double* f,
+                                        const double* fneq, const double* guess, double* alpha,
+                                        int* flags) {
+  if (lattice < 0 || lattice > MLBM_D3Q33 || !f || !fneq || !guess || !alpha || !flags ||
+      n <= 0 || newton_maxit < 0 || bisect_maxit < 0 || !(tol >= 0))
+    return MLBM_ERR_INVALID;
+  const int Q = kQ[lattice];
+  LogEntry tab[LOG_TABLE];
+  make_log_table(tab);
+  const size_t nq = sizeof(double) * Q * n, n8 = sizeof(double) * n, n4 = sizeof(int) * n;
+  void *df = nullptr, *dn = nullptr, *dg = nullptr, *da = nullptr, *dfl = nullptr, *dt = nullptr;
+  auto release = [&]() {
+    cudaFree(df); cudaFree(dn); cudaFree(dg); cudaFree(da); cudaFree(dfl); cudaFree(dt);
+  };
+  if (cudaMalloc(&df, nq) != cudaSuccess || cudaMalloc(&dn, nq) != cudaSuccess ||
+      cudaMalloc(&dg, n8) != cudaSuccess || cudaMalloc(&da, n8) != cudaSuccess ||
+      cudaMalloc(&dfl, n4) != cudaSuccess || cudaMalloc(&dt, sizeof tab) != cudaSuccess) {
+    release();
+    cudaGetLastError();
+    return fail(nullptr, MLBM_ERR_ALLOC, "testing buffers");
+  }
+  StepParams p{};
+  p.alpha_mode = ALPHA_RESIDUAL;
+  p.guess_mode = GUESS_PREVIOUS;
+  p.newton_tol = tol;
+  p.newton_maxit = newton_maxit;
+  p.bisect_maxit = bisect_maxit;
+  p.deviation_threshold = 0.0;
+  p.log_table = dt;
+  cudaError_t e = cudaMemcpy(df, f, nq, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(dn, fneq, nq, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(dg, guess, n8, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(dt, tab, sizeof tab, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess)
+    e = alpha_solve_test(lattice, (const double*)df, (const double*)dn, (const double*)dg, n, p,
+                         (double*)da, (int*)dfl, 0);
+  count_launches(1);
+  if (e == cudaSuccess) e = cudaDeviceSynchronize();
+  if (e == cudaSuccess) e = cudaMemcpy(alpha, da, n8, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(flags, dfl, n4, cudaMemcpyDeviceToHost);
+  release();
+  if (e != cudaSuccess) return fail(nullptr, MLBM_ERR_CUDA, "alpha solve test: %s", cudaGetErrorString(e));
   return MLBM_OK;
 }
 

@@ -63,6 +63,7 @@ struct StepParams {
   int alpha_mode, guess_mode;
   double newton_tol;
   int newton_maxit;
+  int bisect_maxit;          // cap of the bracketed solver (RESIDUAL mode)
   double deviation_threshold;
   float deviation_threshold_f;
   // optional outputs on this step

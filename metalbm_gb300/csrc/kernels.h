@@ -54,6 +54,19 @@ cudaError_t entropy_test_L2(const float* f, const double* fneq, long long nodes,
                             int nx, int mode, const void* table, const void* table_fine, double* F, double* D,
                             int* series, cudaStream_t s);
 
+// The FP64 kernel's entropic alpha (shortcut, limiter, solve) on single nodes
+// [n][Q] (tests); p supplies the solver mode, tolerance, caps and log table.
+cudaError_t alpha_solve_test(int lattice, const double* f, const double* fneq,
+                             const double* guess, long long n, const StepParams& p, double* alpha,
+                             int* flags, cudaStream_t s);
+#define MLBM_DECL_ALPHA_TEST(N)                                                              \
+  cudaError_t alpha_solve_test_L##N(const double* f, const double* fneq, const double* guess, \
+                                    long long n, const StepParams& p, double* alpha,          \
+                                    int* flags, cudaStream_t s);
+MLBM_DECL_ALPHA_TEST(0) MLBM_DECL_ALPHA_TEST(1) MLBM_DECL_ALPHA_TEST(2)
+MLBM_DECL_ALPHA_TEST(3) MLBM_DECL_ALPHA_TEST(4) MLBM_DECL_ALPHA_TEST(5)
+#undef MLBM_DECL_ALPHA_TEST
+
 // f_neq as the FP32-storage entropic main pass forms it (tests).
 cudaError_t neq_test(int lattice, const float* f, long long nodes, int dfloat, double* out,
                      cudaStream_t s);

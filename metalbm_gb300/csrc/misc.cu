@@ -98,6 +98,12 @@ cudaError_t neq_test(int lattice, const float* f, long long nodes, int dfloat, d
               neq_test_L2(f, nodes, dfloat, out, s))
 }
 
+cudaError_t alpha_solve_test(int lattice, const double* f, const double* fneq,
+                             const double* guess, long long n, const StepParams& p, double* alpha,
+                             int* flags, cudaStream_t s) {
+  MLBM_BY_LAT6(lattice, alpha_solve_test, (f, fneq, guess, n, p, alpha, flags, s))
+}
+
 cudaError_t step_f64(int lattice, int collision, int forcing, const double* prev, double* next,
                      const StepParams& p, cudaStream_t s) {
   MLBM_BY_LAT6(lattice, step_f64, (collision, forcing, prev, next, p, s))

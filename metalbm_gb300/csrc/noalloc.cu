@@ -21,7 +21,6 @@
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
-#include <mutex>
 
 #include "../../include/mlbm/mlbm.h"
 #include "kernels.h"
@@ -38,7 +37,6 @@ namespace {
 constexpr int kBlock = 256;              // nodes per block of the BGK kernel
 constexpr int kMaxBlocks = 65536;        // partial slots in the scratch array
 constexpr long long kMaxNodes = (long long)kMaxBlocks * kBlock;  // 16,777,216 = 256^3
-constexpr int kMaxDevices = 64;
 
 // Scratch of the fused diagnostics: one slot of DIAG_FIELDS doubles per block
 // (2.5 MiB), plus the device error word. Shared by every call on a device.
@@ -48,10 +46,7 @@ static __device__ __align__(256) unsigned int g_noalloc_error_word;
 struct Scratch {
   double* partials = nullptr;
   unsigned int* error_word = nullptr;
-  bool ready = false;
 };
-std::mutex g_setup_mutex;
-Scratch g_scratch[kMaxDevices];
 
 int noalloc_fail(int code, const char* fmt, ...) __attribute__((format(printf, 2, 3)));
 int noalloc_fail(int code, const char* fmt, ...) {
@@ -64,29 +59,28 @@ int noalloc_fail(int code, const char* fmt, ...) {
   return code;
 }
 
-// Once per device, with that device current: the device addresses of the
-// scratch symbols. In host code the symbols' names are host-side stand-ins,
-// not device addresses, so the kernel gets these pointers instead.
-int scratch_for_current_device(Scratch** out) {
+// With the calling thread's current device current: the device addresses of
+// the scratch symbols. In host code the symbols' names are host-side
+// stand-ins, not device addresses, so the kernels get these pointers instead.
+// The first call on a device loads this library's device code there (the
+// set-up); later lookups read a table on the host and allocate nothing. The
+// address is looked up on every call rather than cached, because a device
+// reset or a new primary context reloads the module, possibly elsewhere.
+int scratch_for_current_device(Scratch* out) {
   int dev = -1;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return noalloc_fail(MLBM_ERR_NO_DEVICE, "no current CUDA device: %s", cudaGetErrorString(e));
-  if (dev < 0 || dev >= kMaxDevices) return noalloc_fail(MLBM_ERR_INVALID, "device ordinal %d out of range", dev);
-  std::lock_guard<std::mutex> lock(g_setup_mutex);
-  Scratch& s = g_scratch[dev];
-  if (!s.ready) {
-    void* p = nullptr;
-    e = cudaGetSymbolAddress(&p, g_noalloc_partials);
-    if (e != cudaSuccess)
-      return noalloc_fail(MLBM_ERR_CUDA, "cudaGetSymbolAddress(partials) failed: %s", cudaGetErrorString(e));
-    s.partials = static_cast<double*>(p);
-    e = cudaGetSymbolAddress(&p, g_noalloc_error_word);
-    if (e != cudaSuccess)
-      return noalloc_fail(MLBM_ERR_CUDA, "cudaGetSymbolAddress(error word) failed: %s", cudaGetErrorString(e));
-    s.error_word = static_cast<unsigned int*>(p);
-    s.ready = true;
-  }
-  *out = &s;
+  void* p = nullptr;
+  e = cudaGetSymbolAddress(&p, g_noalloc_partials);
+  if (e != cudaSuccess)
+    return noalloc_fail(MLBM_ERR_CUDA, "cudaGetSymbolAddress(partials) on device %d failed: %s", dev,
+                        cudaGetErrorString(e));
+  out->partials = static_cast<double*>(p);
+  e = cudaGetSymbolAddress(&p, g_noalloc_error_word);
+  if (e != cudaSuccess)
+    return noalloc_fail(MLBM_ERR_CUDA, "cudaGetSymbolAddress(error word) on device %d failed: %s", dev,
+                        cudaGetErrorString(e));
+  out->error_word = static_cast<unsigned int*>(p);
   return MLBM_OK;
 }
 
@@ -136,9 +130,10 @@ extern "C" int mlbm_step_f64_noalloc(const mlbm_config* cfg, const double* f_in,
        c.kolmogorov_component >= D))
     return noalloc_fail(MLBM_ERR_INVALID, "bad Kolmogorov axis/component");
 
-  Scratch* s = nullptr;
-  int rc = scratch_for_current_device(&s);
+  Scratch scratch;
+  int rc = scratch_for_current_device(&scratch);
   if (rc != MLBM_OK) return rc;
+  const Scratch* s = &scratch;
 
   // Step parameters, formed as mlbm_create forms them.
   StepParams p{};

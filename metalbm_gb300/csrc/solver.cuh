@@ -6,7 +6,9 @@
 // first leaves its bracket), Newton from there (the update of
 // EntropicStep.h:111-140), and when Newton leaves (1, alpha_max) or runs out
 // of iterations, the safeguarded bisection-Newton of EntropicStep.h:142-220 on
-// [1, alpha_max]; alpha = 2 when that fails too.
+// [1, alpha_max]; alpha = 2 when that fails too. Newton takes at most maxit
+// steps and the bracketed solver bmaxit (maxit = 0 sends every node whose
+// guess fails straight to the bracketed solver).
 //
 // The whole solve is one loop with a single evaluation site: F and F' cost Q
 // FP64 logarithms, and one inlined copy of them keeps the kernel's code (its
@@ -29,7 +31,7 @@ __device__ __forceinline__ double newton_step(double fe, double de) {
 template <class Eval, bool kFloatStep = false>
 __device__ __forceinline__ double residual_alpha_solve(const Eval& eval, double guess,
                                                        double alt, double alphaMax, double tol,
-                                                       int maxit, unsigned c[]) {
+                                                       int maxit, int bmaxit, unsigned c[]) {
   enum { P_GUESS, P_NEWTON, P_LOW, P_HIGH, P_BISECT, P_DONE };
   int phase;
   double x;
@@ -37,14 +39,14 @@ __device__ __forceinline__ double residual_alpha_solve(const Eval& eval, double 
   else if (alt > 1.0 && alt < alphaMax) { x = alt; phase = P_NEWTON; }
   else { x = 1.0; phase = P_LOW; ++c[CNT_BISECT]; }
   unsigned iters = 0;
-  int newton_left = maxit, bisect_left = maxit;
+  int newton_left = maxit, bisect_left = bmaxit;
   bool first_bisect = true;
   double fLow = 0.0, xLow = 1.0, xHigh = alphaMax, dx = 0.0, dxOld = 0.0;
   double result = 2.0;
   bool ok = false;
   // one evaluation per pass: guess + maxit Newton + 2 bracket ends +
-  // midpoint + maxit bisection steps at most
-  for (int pass = 0; pass < 2 * maxit + 4 && phase != P_DONE; ++pass) {
+  // midpoint + bmaxit bisection steps at most
+  for (int pass = 0; pass < maxit + bmaxit + 4 && phase != P_DONE; ++pass) {
     double fe, de;
     eval(x, fe, de);
     if (phase == P_GUESS || phase == P_NEWTON) {

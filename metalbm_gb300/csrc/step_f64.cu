@@ -310,7 +310,8 @@ __device__ __forceinline__ double entropic_alpha(const StepParams& p, const doub
   }
   double r[L::Q];
   const HLog1p<LAT> ev = make_hlog1p<LAT>(f, fneq, r, tab);
-  return residual_alpha_solve(ev, guess, guess, alphaMax, p.newton_tol, p.newton_maxit, c);
+  return residual_alpha_solve(ev, guess, guess, alphaMax, p.newton_tol, p.newton_maxit,
+                              p.bisect_maxit, c);
 }
 
 template <int LAT, int FS>
@@ -411,6 +412,32 @@ __global__ void samples_f64_kernel(const double* __restrict__ prev, StepParams p
   solved[s] = (!small && alphaMax >= 2.0) ? 1 : 0;
 }
 
+// Residual-mode alpha solve of single nodes given as FP64 pulled populations
+// and non-equilibrium parts [n][Q] (tests): entropic_alpha of the FP64 kernel
+// with the caller's guess. flags: 1 alpha_max < 2 (0.95 alpha_max), 2 the
+// bracketed solver ran, 4 alpha = 2 fallback.
+template <int LAT>
+__global__ void __launch_bounds__(128) alpha_solve_test_kernel(
+    const double* __restrict__ f, const double* __restrict__ fneq,
+    const double* __restrict__ guess, long long n, StepParams p, double* __restrict__ alpha,
+    int* __restrict__ flags) {
+  using L = Lattice<LAT>;
+  __shared__ LogEntry s_log[LOG_TABLE];
+  stage_log_table(s_log, reinterpret_cast<const LogEntry*>(p.log_table));
+  __syncthreads();
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double fi[L::Q], ni[L::Q];
+#pragma unroll
+  for (int q = 0; q < L::Q; ++q) {
+    fi[q] = f[i * L::Q + q];
+    ni[q] = fneq[i * L::Q + q];
+  }
+  unsigned c[CNT_COUNT] = {0, 0, 0, 0, 0, 0, 0, 0};
+  alpha[i] = entropic_alpha<LAT>(p, fi, ni, guess[i], c, s_log);
+  flags[i] = (c[CNT_LIMITED] ? 1 : 0) | (c[CNT_BISECT] ? 2 : 0) | (c[CNT_FALLBACK] ? 4 : 0);
+}
+
 // ---- host-side launchers --------------------------------------------------
 template <int LAT, int FS>
 static cudaError_t launch_bgk(const double* prev, double* next, const StepParams& p,
@@ -468,6 +495,15 @@ cudaError_t MLBM_CAT(init_f64_L, MLBM_LAT)(const double* rho, const double* u, d
                                              long long V, cudaStream_t s) {
   const unsigned grid = (unsigned)((V + 255) / 256);
   init_f64_kernel<MLBM_LAT><<<grid, 256, 0, s>>>(rho, u, f, V);
+  return cudaGetLastError();
+}
+
+cudaError_t MLBM_CAT(alpha_solve_test_L, MLBM_LAT)(const double* f, const double* fneq,
+                                                    const double* guess, long long n,
+                                                    const StepParams& p, double* alpha,
+                                                    int* flags, cudaStream_t s) {
+  const unsigned grid = (unsigned)((n + 127) / 128);
+  alpha_solve_test_kernel<MLBM_LAT><<<grid, 128, 0, s>>>(f, fneq, guess, n, p, alpha, flags);
   return cudaGetLastError();
 }
 

@@ -992,11 +992,12 @@ __device__ __forceinline__ void elbm_node(const typename Storage<ST>::T* __restr
         const auto ev = make_entropy_eval<LAT, ST, true>(P, n, nf, rabs, s_log, s_fine, s_lnw);
         const double tol = p.newton_tol - series_error_bound<LAT, ST>(rabs, rho);
         alpha = residual_alpha_solve<decltype(ev), true>(ev, guess, plain, alphaMax, tol,
-                                                         p.newton_maxit, cnt);
+                                                         p.newton_maxit, p.bisect_maxit, cnt);
       } else {
         const auto ev = make_entropy_eval<LAT, ST, false>(P, n, nf, rabs, s_log, s_fine, s_lnw);
         alpha = residual_alpha_solve<decltype(ev), true>(ev, guess, plain, alphaMax,
-                                                         p.newton_tol - 4e-15, p.newton_maxit, cnt);
+                                                         p.newton_tol - 4e-15, p.newton_maxit,
+                                                         p.bisect_maxit, cnt);
       }
     }
   }

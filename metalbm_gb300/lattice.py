@@ -34,6 +34,8 @@ _STORAGES = {"f64": capi.STORAGE_F64, "f32": capi.STORAGE_F32,
              "f16_shifted": capi.STORAGE_F16_SHIFTED}
 _ALPHA = {"reference": capi.ALPHA_REFERENCE, "residual": capi.ALPHA_RESIDUAL}
 _GUESS = {"previous": capi.GUESS_PREVIOUS, "two": capi.GUESS_TWO, "learned": capi.GUESS_LEARNED}
+# default limit of Lattice.sync (a bounded poll; -1 waits without limit)
+SYNC_TIMEOUT_MS = 600_000
 Q_OF = {"D2Q9": 9, "D3Q19": 19, "D3Q27": 27, "D3Q15": 15, "D2Q13": 13, "D3Q33": 33}
 D_OF = {"D2Q9": 2, "D3Q19": 3, "D3Q27": 3, "D3Q15": 3, "D2Q13": 2, "D3Q33": 3}
 
@@ -71,6 +73,8 @@ class InputDeck:
     alphaGuess: str = "previous"
     newtonTolerance: float = 1e-8
     newtonMaxIterations: int = 50
+    # cap of the residual solver's bisection-Newton (0: newtonMaxIterations)
+    bisectionMaxIterations: int = 0
     deviationThreshold: float = 1e-3
     device: int = 0
 
@@ -95,9 +99,14 @@ class InputDeck:
         those decks do not compile in the reference either)."""
         import re
         from pathlib import Path
-        text = str(source)
-        if "constexpr" not in text and Path(text).exists():
-            text = Path(text).read_text()
+        if isinstance(source, Path):
+            text = source.read_text()
+        else:
+            text = str(source)
+            # a short single-line string without definitions names a file
+            if ("constexpr" not in text and "\n" not in text and len(text) < 4096
+                    and Path(text).is_file()):
+                text = Path(text).read_text()
         defs = {}
         for line in text.splitlines():
             line = line.split("//")[0]
@@ -105,11 +114,20 @@ class InputDeck:
             if m:
                 defs[m.group(1)] = m.group(2).strip()
 
+        if not defs:
+            raise ValueError("no `constexpr <type> <name> = <value>;` definitions in the deck")
+
         def enum(name):
             return defs[name].split("::")[-1]
 
         def vec(name):
-            return tuple(float(v) for v in re.findall(r"[-+0-9.eE]+", defs[name]))
+            # MathVector<...>{{a, b, c}}: the numbers between the innermost braces
+            inner = re.findall(r"\{([^{}]*)\}", defs[name])
+            body = inner[-1] if inner else defs[name]
+            try:
+                return tuple(float(v) for v in body.split(",") if v.strip())
+            except ValueError:
+                raise ValueError(f"{name} = {defs[name]}: not a vector of numbers") from None
 
         if "algorithmT" in defs and enum("algorithmT") != "Pull":
             raise ValueError(f"algorithmT {enum('algorithmT')}: only the pull algorithm is built")
@@ -183,6 +201,7 @@ class InputDeck:
         c.alpha_guess = _GUESS[self.alphaGuess]
         c.newton_tolerance = float(self.newtonTolerance)
         c.newton_max_iterations = int(self.newtonMaxIterations)
+        c.bisection_max_iterations = int(self.bisectionMaxIterations)
         c.deviation_threshold = float(self.deviationThreshold)
         c.device = int(self.device)
         return c
@@ -323,7 +342,10 @@ class Lattice:
                 (capi.STEP_LOG_SAMPLES if samples else 0)
         self._check(self._lib.mlbm_step(self._h, int(n), flags))
 
-    def sync(self, timeout_ms: int = -1):
+    def sync(self, timeout_ms: int = SYNC_TIMEOUT_MS):
+        """Wait for the handle's stream (a bounded poll; MlbmError with
+        ERR_TIMEOUT past `timeout_ms`, < 0 waits without limit), then check
+        the device error word."""
         self._check(self._lib.mlbm_sync(self._h, int(timeout_ms)))
 
     def fields(self) -> dict[str, np.ndarray]:

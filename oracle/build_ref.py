@@ -1,7 +1,8 @@
 """Build recipe for the reference metaLBM CPU path used as a test oracle.
 
 Test infrastructure only. Each case is compiled from the reference headers
-where they lie under /root/reference/include/metaLBM (never copied), with our
+where they lie (<reference root>/include/metaLBM, never copied; the root is
+the environment variable MLBM_REFERENCE_ROOT), with our
 own MPI/HDF5/FFTW stand-ins from oracle/ref_stub, the deck oracle/ref_deck.in
 and the harness oracle/ref_harness.cpp. Outputs go to oracle/_ref/<case>/run
 (git-ignored). The reference is a header-only template library whose every
@@ -24,7 +25,7 @@ from dataclasses import dataclass
 from pathlib import Path
 
 HERE = Path(__file__).resolve().parent
-REF_INCLUDE = Path("/root/reference/include")
+REF_INCLUDE = Path(os.environ.get("MLBM_REFERENCE_ROOT", "/root/reference")) / "include"
 OUT = HERE / "_ref"
 
 
@@ -159,14 +160,15 @@ def _lit(v: float) -> str:
     return repr(float(v))
 
 
-def compile_case(name: str, case: RefCase) -> Path:
+def compile_case(name: str, case: RefCase, harness: Path | None = None) -> Path:
     if not REF_INCLUDE.is_dir():
         raise FileNotFoundError(f"reference headers not found at {REF_INCLUDE}")
     out_dir = OUT / name
     out_dir.mkdir(parents=True, exist_ok=True)
     exe = out_dir / "run"
     stamp = out_dir / "cmd"  # the compile command of `exe`: a changed case rebuilds
-    sources = [HERE / "ref_harness.cpp", HERE / "ref_deck.in"] + sorted(HERE.glob("ref_stub/*.h"))
+    harness = harness or HERE / "ref_harness.cpp"
+    sources = [harness, HERE / "ref_deck.in"] + sorted(HERE.glob("ref_stub/*.h"))
     defs = {
         "NPROCS": "1", "NTHREADS": "1", "USE_FFTW": "1",
         "GLOBAL_LENGTH_X": str(case.size[0]), "GLOBAL_LENGTH_Y": str(case.size[1]),
@@ -189,7 +191,7 @@ def compile_case(name: str, case: RefCase) -> Path:
     if case.force in ("Constant", "Sinusoidal"):
         defs[f"MLBM_FORCE_IS_{case.force.upper()}"] = "1"
     cmd += [f"-D{k}={v}" for k, v in defs.items()]
-    cmd += [str(HERE / "ref_harness.cpp"), "-o", str(exe)]
+    cmd += [str(harness), "-o", str(exe)]
     if (exe.exists() and stamp.exists() and stamp.read_text() == " ".join(cmd)
             and all(exe.stat().st_mtime > src.stat().st_mtime for src in sources)):
         return exe
@@ -198,6 +200,16 @@ def compile_case(name: str, case: RefCase) -> Path:
         raise RuntimeError(f"building {name} failed:\n{res.stderr[-4000:]}")
     stamp.write_text(" ".join(cmd))
     return exe
+
+
+def build_bisection(lattice: str = "D3Q27") -> Path:
+    """oracle/_ref/bisection_<lattice>/run: the reference's
+    Bisection_NewtonRaphsonSolver with its EntropicStepFunctor on given node
+    data (oracle/ref_bisection.cpp), for the golden vectors of
+    tests/golden/bisection/."""
+    case = RefCase(lattice, "ELBM", "None", "None", 0.500250125062531, (0.0, 0.0, 0.0),
+                   (1.0, 1.0, 1.0), (4, 4, 4) if lattice[1] == "3" else (4, 4, 1))
+    return compile_case(f"bisection_{lattice.lower()}", case, HERE / "ref_bisection.cpp")
 
 
 def build(names: list[str] | None = None, jobs: int | None = None) -> dict[str, Path]:

@@ -167,6 +167,41 @@ double oracle_equilibrium(int lattice, double rho, const double* u, int q) {
   return equilibrium(&L, rho, u, dotD(u, u, L.D), q);
 }
 
+/* Residual-mode alpha solve of single nodes (tests): alpha_max (capped at
+ * 2.5, Collision.h:305-326), then the solve from guess[i] with Newton capped
+ * at newton_maxit and the bisection-Newton at bisect_maxit. flags[i]: bit 0
+ * alpha_max < 2 (alpha = 0.95 alpha_max), bit 1 the bracketed solver ran,
+ * bit 2 alpha = 2 fallback. */
+static double solve_residual(const double* f, const double* fneq, const double* w, int Q,
+                             double tol, int maxit, int bisect_maxit, double guess, double xMax,
+                             long long* iters, long long* fallbacks, long long* bisections);
+void oracle_solve_alpha_nodes(int lattice, double tol, int newton_maxit, int bisect_maxit, long n,
+                              const double* f, const double* fneq, const double* guess,
+                              double* alpha, int* flags) {
+  lattice_t L;
+  lattice_init(&L, lattice);
+  for (long i = 0; i < n; ++i) {
+    const double* fi = f + i * L.Q;
+    const double* ni = fneq + i * L.Q;
+    double alphaMax = 2.5;
+    for (int q = 0; q < L.Q; ++q)
+      if (ni[q] > 0) {
+        const double t = fabs(fi[q]) / ni[q];
+        if (t < alphaMax) alphaMax = t;
+      }
+    flags[i] = 0;
+    if (alphaMax < 2.) {
+      alpha[i] = 0.95 * alphaMax;
+      flags[i] = 1;
+      continue;
+    }
+    long long it = 0, fb = 0, bi = 0;
+    alpha[i] = solve_residual(fi, ni, L.w, L.Q, tol, newton_maxit, bisect_maxit, guess[i],
+                              alphaMax, &it, &fb, &bi);
+    flags[i] = (bi ? 2 : 0) | (fb ? 4 : 0);
+  }
+}
+
 struct oracle_state {
   oracle_config cfg;
   lattice_t L;
@@ -453,8 +488,8 @@ static int bisection_newton_residual(const hlog1p_t* h, double tol, int maxit, d
 
 /* Residual-mode solve from a guess (see mlbm_oracle.h). */
 static double solve_residual(const double* f, const double* fneq, const double* w, int Q,
-                             double tol, int maxit, double guess, double xMax, long long* iters,
-                             long long* fallbacks, long long* bisections) {
+                             double tol, int maxit, int bisect_maxit, double guess, double xMax,
+                             long long* iters, long long* fallbacks, long long* bisections) {
   pthread_once(&g_log_once, build_log_table);
   double r[QMAX], B1 = 0.0, sfn = 0.0, rmax = 0.0;
   for (int q = 0; q < Q; ++q) {
@@ -478,7 +513,7 @@ static double solve_residual(const double* f, const double* fneq, const double* 
     }
   }
   ++*bisections;
-  if (bisection_newton_residual(&h, tol, maxit, &x, 1.0, xMax, iters)) return x;
+  if (bisection_newton_residual(&h, tol, bisect_maxit, &x, 1.0, xMax, iters)) return x;
   ++*fallbacks;
   return 2.0;
 }
@@ -506,6 +541,8 @@ static double entropic_alpha(const oracle_state* s, const double* f, const doubl
   if (c->guess_mode == ORACLE_GUESS_TWO) guess = 2.0;
   if (c->alpha_mode == ORACLE_ALPHA_RESIDUAL)
     return solve_residual(f, fneq, s->L.w, Q, c->newton_tolerance, c->newton_max_iterations,
+                          c->bisection_max_iterations > 0 ? c->bisection_max_iterations
+                                                          : c->newton_max_iterations,
                           guess, alphaMax, iters, fallbacks, bisections);
   double alpha = guess;
   if (newton(&h, c->newton_tolerance, c->newton_max_iterations, &alpha, 1., alphaMax, iters))

@@ -62,6 +62,7 @@ typedef struct {
   int newton_max_iterations;  /* reference: 50 (Collision.h:337) */
   double deviation_threshold; /* reference: 1e-3 (Collision.h:357) */
   int threads;                /* host threads sharing the sweep (>=1) */
+  int bisection_max_iterations; /* RESIDUAL: cap of the bracketed solver (0: the Newton cap) */
 } oracle_config;
 
 typedef struct oracle_state oracle_state;
@@ -85,6 +86,12 @@ void oracle_get_counters(const oracle_state* s, long long* newton_iterations,
 
 /* The residual mode's FP64 logarithm (Tang's table-driven method). */
 double oracle_fast_log(double x);
+
+/* Residual-mode alpha solve of n single nodes (f, f_neq: [n][Q]); see
+ * mlbm_oracle.c. */
+void oracle_solve_alpha_nodes(int lattice, double tol, int newton_maxit, int bisect_maxit, long n,
+                              const double* f, const double* fneq, const double* guess,
+                              double* alpha, int* flags);
 
 /* Single-node entry points for unit tests: equilibrium population q. */
 double oracle_equilibrium(int lattice, double rho, const double* u, int q);

@@ -38,7 +38,8 @@ class _Cfg(ct.Structure):
                 ("kolmogorov_component", ct.c_int), ("lx", ct.c_int), ("ly", ct.c_int),
                 ("lz", ct.c_int), ("alpha_mode", ct.c_int), ("guess_mode", ct.c_int),
                 ("newton_tolerance", ct.c_double), ("newton_max_iterations", ct.c_int),
-                ("deviation_threshold", ct.c_double), ("threads", ct.c_int)]
+                ("deviation_threshold", ct.c_double), ("threads", ct.c_int),
+                ("bisection_max_iterations", ct.c_int)]
 
 
 def build_port(force: bool = False) -> Path:
@@ -78,6 +79,9 @@ def _load():
         lib.oracle_equilibrium.restype = ct.c_double
         lib.oracle_equilibrium.argtypes = [ct.c_int, ct.c_double, dp, ct.c_int]
         lib.oracle_lattice_tables.argtypes = [ct.c_int, dp, dp]
+        lib.oracle_solve_alpha_nodes.argtypes = [ct.c_int, ct.c_double, ct.c_int, ct.c_int,
+                                                 ct.c_long, dp, dp, dp, dp,
+                                                 ct.POINTER(ct.c_int)]
         lib.oracle_fast_log.restype = ct.c_double
         lib.oracle_fast_log.argtypes = [ct.c_double]
         _lib = lib
@@ -116,6 +120,7 @@ class OracleConfig:
     newton_max_iterations: int = 50
     deviation_threshold: float = 1e-3
     threads: int = 1
+    bisection_max_iterations: int = 0  # 0: the Newton cap
 
 
 class OraclePort:
@@ -134,7 +139,7 @@ class OraclePort:
                  (ct.c_double * 3)(*cfg.wavelength), cfg.kolmogorov_axis,
                  cfg.kolmogorov_component, lx, ly, lz, cfg.alpha_mode, cfg.guess_mode,
                  cfg.newton_tolerance, cfg.newton_max_iterations, cfg.deviation_threshold,
-                 max(1, cfg.threads))
+                 max(1, cfg.threads), int(cfg.bisection_max_iterations))
         self._lib = _load()
         self._h = self._lib.oracle_create(ct.byref(c))
         if not self._h:
@@ -193,3 +198,19 @@ def equilibrium(lattice: str, rho: float, u, q: int) -> float:
 def fast_log(x: float) -> float:
     """The residual mode's FP64 logarithm (Tang's table-driven method)."""
     return _load().oracle_fast_log(float(x))
+
+
+def solve_alpha_nodes(lattice: str, f: np.ndarray, fneq: np.ndarray, guess: np.ndarray,
+                      tol: float = 1e-12, newton_maxit: int = 50, bisect_maxit: int = 50):
+    """The residual-mode alpha solve on single nodes (f, f_neq: [n, Q]):
+    (alpha [n], flags [n]: 1 limited, 2 bracketed solver ran, 4 alpha = 2)."""
+    f = np.ascontiguousarray(f, np.float64)
+    fneq = np.ascontiguousarray(fneq, np.float64)
+    guess = np.ascontiguousarray(guess, np.float64)
+    n = f.shape[0]
+    alpha = np.empty(n)
+    flags = np.empty(n, np.int32)
+    _load().oracle_solve_alpha_nodes(LATTICES[lattice], float(tol), int(newton_maxit),
+                                     int(bisect_maxit), n, _ptr(f), _ptr(fneq), _ptr(guess),
+                                     _ptr(alpha), flags.ctypes.data_as(ct.POINTER(ct.c_int)))
+    return alpha, flags

@@ -183,3 +183,10 @@ def test_input_deck_from_a_reference_deck():
     with pytest.raises(ValueError, match="TruncationMa3"):
         InputDeck.from_reference_deck(deck_text.replace("TruncationMa3", "Incompressible"),
                                       lengths=(8, 8, 8))
+    # vectors written with an explicit type name, and a long single-line string
+    # that is neither a deck nor a file name: a ValueError, not an OSError
+    typed = deck_text.replace("= { {1e1, 1e1, 1e1} }", "= MathVector<dataT, 3>{{1e1, 2e1, -3e1}}")
+    d = InputDeck.from_reference_deck(typed, lengths=(8, 8, 8))
+    assert d.forceAmplitude == (10.0, 20.0, -30.0)
+    with pytest.raises(ValueError):
+        InputDeck.from_reference_deck("x" * 5000)

@@ -1,0 +1,219 @@
+"""The benchmark configurations at their stated sizes, on the GPU, against the
+oracle (the C restatement, pinned bit for bit to the reference's CPU build),
+and the bracketed alpha solver against the reference's own function.
+
+* D3Q19 BGK FP64, tau 0.55, Guo, Kolmogorov F_x(z) = 1e-6 sin(2 pi 2 z / L)
+  (two periods along the contiguous axis), rho0 = 1, u ~ U[-1e-4, 1e-4]
+  (seed 1): 500 steps at 64^3 and 5 steps at 256^3, bit-identical.
+* D3Q27 entropic FP64, beta = 0.9995, Taylor-Green U0 = 0.05, the reference
+  alpha solver (Newton to |step| <= 1e-8, alpha = 2 fallback): 2000 steps at
+  64^3 and 3 steps at 256^3, within 1e-12 (max |a - b| / max |b|) in f, rho
+  and u.
+* D3Q27 entropic, FP32 storage, learned alpha guess, residual solver at
+  1e-12, Taylor-Green + solenoidal perturbation (1e-3 on 8 <= |k| <= 10,
+  seed 2) at 256^3: u within 1e-6 of the FP64 step after 200 steps.
+* The bracketed solver (bisection-Newton, EntropicStep.h:142-220) forced on
+  every node: against the reference's Bisection_NewtonRaphsonSolver on node
+  data (tests/golden/bisection), and in full steps against the oracle.
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+
+TAU_ENTROPIC = 1.0 / (2.0 * 0.9995)
+
+
+def rel(a, b):
+    return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300))
+
+
+def threads():
+    return os.cpu_count() or 1
+
+
+def d3q19_kolmogorov(L):
+    from metalbm_gb300 import InputDeck, fields
+    from oracle import OracleConfig
+    shape = (L, L, L)
+    rho, u = fields.perturbed_rest(shape, 3, 1e-4, seed=1)
+    kw = dict(forceAmplitude=(1e-6, 0.0, 0.0), forceWaveLength=(L / 2.0, 1.0, 1.0))
+    deck = InputDeck(latticeT="D3Q19", forcingSchemeT="Guo", forceT="Kolmogorov",
+                     relaxationTime=0.55, kolmogorovAxis=2, globalLength=shape, **kw)
+    port = OracleConfig(lattice="D3Q19", forcing="Guo", force="Kolmogorov", tau=0.55,
+                        amplitude=kw["forceAmplitude"], wavelength=kw["forceWaveLength"],
+                        kolmogorov_axis=2, size=shape, threads=threads())
+    return deck, port, rho, u
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("L,steps", [(64, 500), (256, 5)])
+def test_d3q19_bgk_f64_kolmogorov_matches_oracle(L, steps):
+    from metalbm_gb300 import Lattice
+    from oracle import OraclePort
+    deck, pcfg, rho, u = d3q19_kolmogorov(L)
+    with Lattice(deck) as lat:
+        lat.init_equilibrium(rho, u)
+        lat.step(steps, store=True, diagnostics=True)
+        f = lat.populations()
+        fl = lat.fields()
+    port = OraclePort(pcfg)
+    port.init_equilibrium(rho, u)
+    port.step(steps)
+    assert np.array_equal(f, port.populations())
+    pf = port.fields()
+    assert np.array_equal(fl["rho"], pf["rho"]) and np.array_equal(fl["u"], pf["u"])
+
+
+def taylor_green_entropic(L, **deck_kw):
+    from metalbm_gb300 import InputDeck, fields
+    shape = (L, L, L)
+    rho, u = fields.taylor_green(shape, u0=0.05)
+    deck = InputDeck(latticeT="D3Q27", collisionT="ELBM", relaxationTime=TAU_ENTROPIC,
+                     globalLength=shape, **deck_kw)
+    return deck, rho, u
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("L,steps,chunk", [(64, 2000, 250), (256, 3, 3)])
+def test_d3q27_entropic_reference_mode_matches_oracle(L, steps, chunk):
+    """Reference alpha solver (tolerance 1e-8, 50 iterations, alpha = 2
+    fallback, deviation shortcut 1e-3): CUDA's FP64 log against the host
+    libm's is the only difference. Compared every `chunk` steps."""
+    from metalbm_gb300 import Lattice
+    from oracle import OracleConfig, OraclePort
+    deck, rho, u = taylor_green_entropic(L)
+    port = OraclePort(OracleConfig(lattice="D3Q27", collision="ELBM", tau=TAU_ENTROPIC,
+                                   size=(L, L, L), threads=threads()))
+    port.init_equilibrium(rho, u)
+    errs = []
+    with Lattice(deck) as lat:
+        lat.init_equilibrium(rho, u)
+        done = 0
+        while done < steps:
+            n = min(chunk, steps - done)
+            lat.step(n, store=True)
+            port.step(n)
+            done += n
+            fl, pf = lat.fields(), port.fields()
+            e = {"step": done, "f": rel(lat.populations(), port.populations()),
+                 "rho": rel(fl["rho"], pf["rho"]), "u": rel(fl["u"], pf["u"]),
+                 "alpha": float(np.abs(fl["alpha"] - pf["alpha"]).max())}
+            errs.append(e)
+        d = lat.diagnostics()
+    assert d["fallback_nodes"] >= 0
+    worst = max(max(e["f"], e["rho"], e["u"]) for e in errs)
+    assert worst <= 1e-12, json.dumps(errs)
+
+
+@pytest.mark.gpu
+def test_d3q27_f32_learned_tracks_f64_at_256():
+    """The learned-guess FP32-storage step against the FP64 step (residual
+    solver, the same tolerance) from the same Taylor-Green + perturbation
+    field: max |u_f32 - u_f64| <= 1e-6 after 200 steps, no alpha = 2
+    fallback."""
+    from metalbm_gb300 import Lattice, alpha_model, fields
+    L, steps = 256, 200
+    deck_kw = dict(alphaSolver="residual", newtonTolerance=1e-12, deviationThreshold=0.0)
+    deck, rho, u = taylor_green_entropic(L, **deck_kw)
+    u = u + fields.solenoidal_shell((L, L, L), 8.0, 10.0, 1e-3, seed=2)
+    out = {}
+    for storage, guess in (("f64", "previous"), ("f32", "learned")):
+        d = deck.__class__(**{**deck.__dict__, "storage": storage, "alphaGuess": guess})
+        with Lattice(d) as lat:
+            if guess == "learned":
+                lat.set_alpha_model(alpha_model.load_model(
+                    alpha_model.default_model_path("D3Q27")))
+            lat.init_equilibrium(rho, u)
+            lat.step(steps, store=True, diagnostics=True)
+            out[storage] = lat.fields()["u"]
+            out[storage + "_d"] = lat.diagnostics()
+    assert out["f32_d"]["fallback_nodes"] == 0 and out["f64_d"]["fallback_nodes"] == 0
+    assert np.abs(out["f32"] - out["f64"]).max() <= 1e-6
+
+
+def _bisection_golden():
+    z = np.load(GOLDEN / "bisection" / "d3q27_nodes.npz")
+    return {k: z[k] for k in z.files if k != "meta"}, json.loads(str(z["meta"]))
+
+
+def _gpu_alpha_solve(g, tol, newton_maxit, bisect_maxit):
+    import ctypes as ct
+    from metalbm_gb300 import capi
+    lib = capi.load()
+    n = len(g["f"])
+    f = np.ascontiguousarray(g["f"])
+    fn = np.ascontiguousarray(g["fneq"])
+    guess = np.full(n, 2.0)
+    alpha = np.empty(n)
+    flags = np.empty(n, np.int32)
+    dp = ct.POINTER(ct.c_double)
+    rc = lib.mlbm_testing_alpha_solve(2, tol, newton_maxit, bisect_maxit, n, f.ctypes.data_as(dp),
+                                      fn.ctypes.data_as(dp), guess.ctypes.data_as(dp),
+                                      alpha.ctypes.data_as(dp),
+                                      flags.ctypes.data_as(ct.POINTER(ct.c_int)))
+    assert rc == 0, lib.mlbm_last_error(None)
+    return alpha, flags
+
+
+@pytest.mark.gpu
+def test_gpu_bisection_matches_reference_solver():
+    """The FP64 kernel's bracketed solver, forced on every node (Newton cap 0),
+    against the reference's Bisection_NewtonRaphsonSolver on the golden node
+    data: same roots within the two stopping rules (|F| <= tol here, |step| <=
+    tol there), and bit-identical to the oracle's restatement."""
+    from metalbm_gb300 import build
+    from oracle.port import solve_alpha_nodes
+    from test_oracle_golden import residual_bound
+    build.build()
+    g, meta = _bisection_golden()
+    tol, maxit = meta["tolerance"], meta["iteration_max"]
+    a, flags = _gpu_alpha_solve(g, tol, 0, maxit)
+    assert (flags == 2).all()
+    assert (np.abs(a - g["alpha"]) <= residual_bound(g, tol)).all()
+    ao, _ = solve_alpha_nodes("D3Q27", g["f"], g["fneq"], np.full(len(a), 2.0), tol, 0, maxit)
+    assert np.array_equal(a, ao)
+    # Newton first (default caps): no node needs the bracket on these nodes
+    a2, flags2 = _gpu_alpha_solve(g, tol, maxit, maxit)
+    assert not (flags2 & 4).any()
+    assert (np.abs(a2 - g["alpha"]) <= residual_bound(g, tol)).all()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("storage", ["f64", "f32"])
+def test_forced_bisection_steps(storage):
+    """Full entropic steps with Newton capped at 0: every solved node whose
+    guess fails goes through the bracketed solver (bisection_nodes > 0), none
+    falls back to alpha = 2; FP64 storage equals the oracle bit for bit with
+    the same caps, FP32 storage follows the FP64 step."""
+    from metalbm_gb300 import InputDeck, Lattice, fields
+    from oracle import ALPHA_RESIDUAL, OracleConfig, OraclePort
+    shape = (20, 16, 12)
+    rho, u = fields.taylor_green(shape, u0=0.08)
+    kw = dict(latticeT="D3Q27", collisionT="ELBM", relaxationTime=0.50025, globalLength=shape,
+              alphaSolver="residual", newtonTolerance=1e-12, deviationThreshold=0.0,
+              newtonMaxIterations=0, bisectionMaxIterations=50)
+    with Lattice(InputDeck(storage=storage, **kw)) as lat:
+        lat.init_equilibrium(rho, u)
+        lat.step(4, store=True, diagnostics=True)
+        f = lat.populations()
+        fl = lat.fields()
+        d = lat.diagnostics()
+    assert d["bisection_nodes"] > 0 and d["fallback_nodes"] == 0
+    if storage == "f64":  # every solved node either passes its guess or brackets
+        assert d["bisection_nodes"] == d["solved_nodes"] - d["guess_hits"]
+    port = OraclePort(OracleConfig(lattice="D3Q27", collision="ELBM", alpha_mode=ALPHA_RESIDUAL,
+                                   newton_tolerance=1e-12, newton_max_iterations=0,
+                                   bisection_max_iterations=50, deviation_threshold=0.0,
+                                   tau=0.50025, size=shape))
+    port.init_equilibrium(rho, u)
+    port.step(4)
+    if storage == "f64":
+        assert np.array_equal(f, port.populations())
+        assert np.array_equal(fl["alpha"], port.fields()["alpha"])
+        assert port.counters()["bisections"] > 0
+    else:
+        assert rel(fl["u"], port.fields()["u"]) <= 1e-4

@@ -101,6 +101,25 @@ def test_sync_gives_up_after_its_timeout():
 
 
 @pytest.mark.gpu
+def test_cpp_routine_wait_is_bounded(tmp_path):
+    """The C++ drop-in's iterate (called with the reference's signature:
+    streams and events) bounds its wait for the device: with a zero limit the
+    first step's wait gives up with MLBM_ERR_TIMEOUT, reported as exit 6, and
+    the process ends cleanly."""
+    import subprocess
+    from metalbm_gb300 import build, fields
+    exe = build.build_routine()
+    shape = (128, 128, 128)
+    rho, u = fields.taylor_green(shape, u0=0.05)
+    np.concatenate([rho.ravel(), u.ravel()]).tofile(tmp_path / "in.bin")
+    args = [str(exe), str(tmp_path / "in.bin"), str(tmp_path / "out.bin"), "3", "2", "1", "0",
+            "0", repr(0.5005), "0", "0", "0", "1", "1", "1", "128", "128", "128", "0", "1"]
+    r = subprocess.run(args, capture_output=True, text=True, timeout=300)
+    assert r.returncode == 6, (r.returncode, r.stderr)
+    assert "not finished after 0 ms" in r.stderr
+
+
+@pytest.mark.gpu
 def test_registered_host_buffers_round_trip():
     """Fields through page-locked, huge-page host arrays equal those through
     ordinary numpy arrays."""

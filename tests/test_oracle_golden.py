@@ -190,3 +190,38 @@ def test_spectral_force_restatement_matches_reference(case):
     assert np.abs(port.populations() - g["f"]).max() <= 1e-13 * np.abs(g["f"]).max()
     assert np.abs(fl["u"] - g["u"]).max() <= 1e-12 * np.abs(g["u"]).max()
     assert np.abs(fl["rho"] - g["rho"]).max() <= 1e-13
+
+
+def _bisection_golden():
+    z = np.load(GOLDEN / "bisection" / "d3q27_nodes.npz")
+    return {k: z[k] for k in z.files if k != "meta"}, json.loads(str(z["meta"]))
+
+
+def residual_bound(g, tol):
+    """|alpha - alpha_ref| allowed between a solve that stops at |F| <= tol
+    and the reference's, which stops at |step| <= tol: tol / |F'(alpha_ref)|
+    plus two step tolerances."""
+    _, w = lattice_tables("D3Q27")
+    gq = g["f"] - g["alpha"][:, None] * g["fneq"]
+    dF = np.sum(g["fneq"] * (1.0 + np.log(gq / w)), axis=1)
+    return tol / np.abs(dF) + 2 * tol
+
+
+def test_oracle_bisection_matches_reference_solver():
+    """The oracle's bracketed solver, forced (Newton capped at 0, so every
+    node goes through the bisection-Newton update), against the reference's
+    own Bisection_NewtonRaphsonSolver with its EntropicStepFunctor
+    (EntropicStep.h:15-63, 142-220) on the same node data: every node
+    converges in both, to the same root within the two stopping rules."""
+    from oracle.port import solve_alpha_nodes
+    g, meta = _bisection_golden()
+    assert g["converged"].all()
+    tol = meta["tolerance"]
+    a, flags = solve_alpha_nodes("D3Q27", g["f"], g["fneq"], np.full(len(g["f"]), 2.0), tol,
+                                 newton_maxit=0, bisect_maxit=meta["iteration_max"])
+    assert (flags == 2).all()  # bracketed solver on every node, no fallback
+    assert (np.abs(a - g["alpha"]) <= residual_bound(g, tol)).all()
+    # with Newton first (the default caps) the same roots
+    a2, flags2 = solve_alpha_nodes("D3Q27", g["f"], g["fneq"], np.full(len(g["f"]), 2.0), tol)
+    assert not (flags2 & 4).any()
+    assert (np.abs(a2 - g["alpha"]) <= residual_bound(g, tol)).all()
