@@ -105,6 +105,17 @@ def initial_field(name: str, shape):
     return fields.perturbed_rest(shape, 3, 1e-4, seed=1)
 
 
+def arithmetic_of(name: str) -> str:
+    """What the workload computes in, beside its storage type (`dtype`)."""
+    w = WORKLOADS[name]
+    if w["collisionT"] != "BGK":
+        return ("populations stored and updated in FP32; f_neq, B1 and M2 of the entropy "
+                "function in double-float FP32, its evaluation and the alpha solve in FP64")
+    return {"f64": "FP64 (the reference's operation order)",
+            "f32": "FP32 storage and collision (deviations from the weights)",
+            "f16_shifted": "FP16 storage of (f - w) 2^k, FP32 collision"}[w["storage"]]
+
+
 def deck_for(name: str, **over):
     from metalbm_gb300 import InputDeck
     w = {k: v for k, v in WORKLOADS[name].items() if k != "bytes_per_node"}
@@ -215,6 +226,36 @@ def time_steps(lat, steps: int, torch, dist=None, store_each: bool = False):
     return e0.elapsed_time(e1), launches
 
 
+def time_steps_perfect_guess(lat, steps: int, torch, dist=None):
+    """The perfect-guess bound of the alpha solve: before each timed step an
+    untimed trial step from the same populations (mlbm_testing_step_in_place)
+    leaves every node's solved alpha in the alpha field, so the timed step
+    (previous-alpha guess) starts each node from its root. Returns (total ms
+    of the timed steps, summed solver counters of the timed steps)."""
+    stream = torch.cuda.ExternalStream(lat.stream)
+    lib = lat._lib
+    lat.sync()
+    if dist is not None:
+        dist.barrier()
+    torch.cuda.synchronize()
+    total, sums = 0.0, {}
+    for _ in range(steps):
+        lat._check(lib.mlbm_testing_step_in_place(lat.handle))
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        lat.step(1)
+        e1.record(stream)
+        d = lat.diagnostics()  # synchronizes
+        total += e0.elapsed_time(e1)
+        for k in ("solved_nodes", "newton_iterations", "guess_hits", "bisection_nodes",
+                  "fallback_nodes", "series_nodes", "learned_nodes"):
+            sums[k] = sums.get(k, 0) + d[k]
+    torch.cuda.synchronize()
+    if dist is not None:
+        dist.barrier()
+    return total, sums
+
+
 def solver_stats(d: dict) -> dict:
     """Per-solved-node statistics of the alpha solve over the timed steps."""
     solved = max(d["solved_nodes"], 1)
@@ -222,7 +263,8 @@ def solver_stats(d: dict) -> dict:
             "guess_hit_fraction": d["guess_hits"] / solved,
             "fallback_fraction": 1.0 - d["guess_hits"] / solved,
             "bisection_nodes": d["bisection_nodes"], "alpha2_fallback_nodes": d["fallback_nodes"],
-            "series_form_fraction": d["series_nodes"] / solved}
+            "series_form_fraction": d["series_nodes"] / solved,
+            "network_guess_fraction": d.get("learned_nodes", 0) / solved}
 
 
 def load_or_train_model(deck, torch):
@@ -244,12 +286,21 @@ class PortRun:
     field restated with numpy FFTs before every step from the stored fields,
     which stay the initial ones (no step stores, as in the timed GPU steps)."""
 
-    def __init__(self, name: str, shape, threads: int):
-        from oracle import ALPHA_REFERENCE, OracleConfig, OraclePort
+    def __init__(self, name: str, shape, threads: int, alpha: str = "workload", fields=None):
+        """alpha: "workload" solves alpha as the GPU arm does (the residual
+        solver at the workload's tolerance), "reference" with the reference's
+        Newton (tolerance 1e-8, alpha = 2 fallback, deviation shortcut 1e-3)."""
+        from oracle import ALPHA_REFERENCE, ALPHA_RESIDUAL, OracleConfig, OraclePort
         w = WORKLOADS[name]
         self.w, self.shape = w, shape
         self.spectral = w.get("forceT") in SPECTRAL_FORCES
-        self.rho, self.u = initial_field(name, shape)
+        self.rho, self.u = fields if fields is not None else initial_field(name, shape)
+        solver = {}
+        if w["collisionT"] != "BGK" and alpha == "workload":
+            solver = dict(alpha_mode=ALPHA_RESIDUAL, newton_tolerance=w["newtonTolerance"],
+                          deviation_threshold=w["deviationThreshold"])
+        elif w["collisionT"] != "BGK":
+            solver = dict(alpha_mode=ALPHA_REFERENCE)
         cfg = OracleConfig(lattice=w["latticeT"],
                            collision="ELBM" if w["collisionT"] != "BGK" else "BGK",
                            forcing=w.get("forcingSchemeT", "None"),
@@ -257,9 +308,12 @@ class PortRun:
                            tau=w["relaxationTime"], amplitude=w.get("forceAmplitude", (0, 0, 0)),
                            wavelength=w.get("forceWaveLength", (1, 1, 1)),
                            kolmogorov_axis=w.get("kolmogorovAxis", 1), size=shape,
-                           alpha_mode=ALPHA_REFERENCE, threads=threads)
+                           threads=threads, **solver)
         self.port = OraclePort(cfg)
         self.port.init_equilibrium(self.rho, self.u)
+
+    def close(self):
+        self.port.close()
 
     def step(self, n: int):
         if not self.spectral:
@@ -283,14 +337,49 @@ class PortRun:
             self.port.step(1, store_last=False)
 
 
-def cpu_baseline_port(name: str, threads: int, seconds_budget: float = 20.0) -> dict:
-    """The oracle port (C restatement of the reference path) on the host
-    cores, on a bounded sample of the same workload."""
+# The reference CPU path's grid per workload: the workload's own, except the
+# 512^3 entropic one, whose 25 steps at the CPU path's ~5-10 MLUPS on 16 host
+# cores would take ~10 minutes; it runs the same construction on 256^3.
+REFERENCE_GRID = {"entropic_learned_512": (256, 256, 256)}
+
+
+def reference_shape(name: str, grid: int = 0):
+    if grid:
+        return (grid,) * 3
+    return REFERENCE_GRID.get(name, tuple(WORKLOADS[name]["globalLength"]))
+
+
+def reference_differences(name: str, shape) -> list[str]:
+    """Why the reference arm's configuration is not the GPU arm's (empty when
+    it is)."""
     w = WORKLOADS[name]
-    lat = w["latticeT"]
-    side = 64 if lat == "D3Q27" else 96
-    shape = (side, side, side)
-    run = PortRun(name, shape, threads)
+    out = []
+    if tuple(shape) != tuple(w["globalLength"]):
+        out.append(f"grid {'x'.join(map(str, shape))} instead of "
+                   f"{'x'.join(map(str, w['globalLength']))} (the CPU path's time)")
+    if w["storage"] != "f64":
+        out.append(f"FP64 populations (the reference has no {w['storage']} storage)")
+    return out
+
+
+def solver_words(name: str, alpha: str = "workload") -> str:
+    w = WORKLOADS[name]
+    if w["collisionT"] == "BGK":
+        return "BGK"
+    if alpha == "workload":
+        return (f"entropic, residual alpha solver |F| <= {w['newtonTolerance']:g} (the GPU arm's "
+                "solver)")
+    return "entropic, reference alpha solver (Newton to 1e-8, alpha = 2 fallback)"
+
+
+def cpu_baseline_port(name: str, shape, threads: int, fields=None,
+                      seconds_budget: float = 20.0) -> dict:
+    """The oracle port (C restatement of the reference path) on the host
+    cores, on the workload's own grid and initial field with the GPU arm's
+    alpha solver: one warm-up step, then steps until about `seconds_budget`
+    seconds (a bounded sample of the workload)."""
+    w = WORKLOADS[name]
+    run = PortRun(name, shape, threads, fields=fields)
     run.step(1)
     steps, t0 = 0, time.perf_counter()
     while True:
@@ -299,11 +388,13 @@ def cpu_baseline_port(name: str, threads: int, seconds_budget: float = 20.0) -> 
         dt = time.perf_counter() - t0
         if dt > seconds_budget or steps >= 50:
             break
+    run.close()
     V = int(np.prod(shape))
     extra = ", force field by numpy FFTs each step (1 thread)" if run.spectral else ""
     return {"value": V * steps / dt / 1e6, "unit": "MLUPS", "cores": threads, "kind": "port",
-            "sample": f"{lat} {w['collisionT']} FP64, reference alpha solver, {side}^3, "
-                      f"{steps} steps after 1 warm-up, {threads} threads{extra}"}
+            "sample": f"{w['latticeT']} FP64 {solver_words(name)}, the workload's "
+                      f"{'x'.join(map(str, shape))} grid and initial field, {steps} steps after "
+                      f"1 warm-up, {threads} threads{extra}"}
 
 
 # ---------------------------------------------------------------------------
@@ -356,14 +447,17 @@ def run_ours(args):
     lat.close()
     total_ms = max_over_ranks(total_ms, dist, f"cuda:{local}")
 
-    # --- arms 2 and 3: plain Newton from the previous step's alpha (the
-    # reference's guess, Algorithm.h:103-106) and from alpha = 2; same
-    # initial state, same residual tolerance, same GPU
+    # --- the other arms, same initial state, same residual tolerance, same
+    # GPU: plain Newton from the previous step's alpha (the reference's guess,
+    # Algorithm.h:103-106) and from alpha = 2, the network at every node, and
+    # the perfect-guess bound (every node starts from its root)
     if entropic:
         value_l = job_value(V, args.steps, world, total_ms)
         arms = {}
-        for guess in ("previous", "two"):
+        for guess in ("previous", "two", "learned_everywhere"):
             lat = Lattice(deck_for(name, device=local, alphaGuess=guess, **grid_over))
+            if guess.startswith("learned"):
+                lat.set_alpha_model(model)
             lat.init_equilibrium(rho, u)
             lat.step(args.warmup)
             ms, _ = time_steps(lat, args.steps, torch, dist)
@@ -372,13 +466,49 @@ def run_ours(args):
             ms = max_over_ranks(ms, dist, f"cuda:{local}")
             arms[guess] = {"value": job_value(V, args.steps, world, ms), "unit": "MLUPS",
                            "ms_per_step": ms / args.steps, **solver_stats(d)}
+        lat = Lattice(deck_for(name, device=local, alphaGuess="previous", **grid_over))
+        lat.init_equilibrium(rho, u)
+        lat.step(args.warmup)
+        ms, sums = time_steps_perfect_guess(lat, args.steps, torch, dist)
+        lat.close()
+        ms = max_over_ranks(ms, dist, f"cuda:{local}")
+        arms["perfect"] = {"value": job_value(V, args.steps, world, ms), "unit": "MLUPS",
+                           "ms_per_step": ms / args.steps, **solver_stats(sums),
+                           "what": "every timed step preceded by an untimed trial step from "
+                                   "the same populations (mlbm_testing_step_in_place), so each "
+                                   "node's guess is its solved alpha (to the FP32 alpha field's "
+                                   "precision, alpha - 2 in float)"}
+        # the first step from the initial state (alpha = 2 stored everywhere):
+        # the network guess against the constant 2 the reference starts from
+        cold = {}
+        for guess in ("learned", "two"):
+            lat = Lattice(deck_for(name, device=local, alphaGuess=guess, **grid_over))
+            if guess == "learned":
+                lat.set_alpha_model(model)
+            lat.init_equilibrium(rho, u)
+            lat.step(1)
+            cold[guess] = solver_stats(lat.diagnostics())
+            lat.close()
         sl = solver_stats(dl)
         extra = {
             "newton_alpha": arms["previous"],
             "newton_alpha_from_2": arms["two"],
-            "learned_alpha": {**sl, "model": model_src},
+            "learned_alpha": {**sl, "model": model_src,
+                              "guess": "the network where a node has no solved alpha from the "
+                                       "previous step (stored alpha exactly 2), the previous "
+                                       "alpha elsewhere"},
+            "learned_alpha_everywhere": {**arms["learned_everywhere"],
+                                         "guess": "the network at every solved node"},
+            "perfect_guess": arms["perfect"],
             "speedup_learned_vs_newton": value_l / arms["previous"]["value"],
             "speedup_learned_vs_newton_from_2": value_l / arms["two"]["value"],
+            "speedup_learned_everywhere_vs_newton":
+                arms["learned_everywhere"]["value"] / arms["previous"]["value"],
+            "speedup_perfect_guess_vs_newton": arms["perfect"]["value"] / arms["previous"]["value"],
+            "first_step_from_initial_state": {
+                "learned": cold["learned"], "alpha_2": cold["two"],
+                "what": "one step after mlbm_init_equilibrium (alpha = 2 stored everywhere): "
+                        "the network guess at every node against the reference's constant 2"},
             "newton_iterations_saved_per_solved_node": {
                 "vs_previous_alpha": arms["previous"]["newton_iterations_per_solved_node"]
                 - sl["newton_iterations_per_solved_node"],
@@ -450,18 +580,22 @@ def run_ours(args):
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
-        cpu = cpu_baseline_port(name, os.cpu_count() or 1)
+        # the reference arm's sample: its grid, initial field and alpha solver
+        rshape = reference_shape(name, args.grid)
+        cpu = cpu_baseline_port(name, rshape, os.cpu_count() or 1,
+                                fields=(rho, u) if tuple(rshape) == tuple(shape) else None)
 
     if rank == 0:
         line = {
             "metric": metric_for(name), "value": value, "unit": "MLUPS", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f64" if entropic or w["storage"] == "f64" else "f32",
+            "dtype": {"f64": "f64", "f32": "f32", "f16_shifted": "f16"}[w["storage"]],
             "data": "synthetic (Taylor-Green + seeded solenoidal perturbation)" if entropic
                     else "synthetic (seeded uniform velocity perturbation)",
             "config": {"workload": name, "lattice": deck.latticeT, "collision": deck.collisionT,
-                       "storage": deck.storage, "grid": list(shape), "beta": 1 / (2 * deck.relaxationTime),
+                       "storage": deck.storage, "arithmetic": arithmetic_of(name),
+                       "grid": list(shape), "beta": 1 / (2 * deck.relaxationTime),
                        "alpha_solver": deck.alphaSolver if entropic else None,
                        "parallelism": f"replicas x{world}",
                        "l2": f"populations {pop_gb:.1f} GB read and written per step > 129 MB L2, "
@@ -545,34 +679,51 @@ def _dp():
 # ---------------------------------------------------------------------------
 def run_reference(args):
     """The reference's CPU implementation of the path (the oracle port of
-    metaLBM's serial Algorithm loop, reference alpha solver), on the host
-    cores, same workload family and metric; rank 0 only."""
+    metaLBM's serial Algorithm loop, all host threads over x slabs) on the
+    GPU arm's workload: same grid, initial field, metric and alpha solver,
+    W warm-up and K timed steps; entropic workloads add one step with the
+    reference's own alpha solver. Rank 0 only."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
     name = args.workload
     w = WORKLOADS[name]
     threads = os.cpu_count() or 1
-    side = 96 if w["latticeT"] == "D3Q27" else 128
-    shape = (side, side, side)
-    run = PortRun(name, shape, threads)
+    shape = reference_shape(name, args.grid)
+    V = int(np.prod(shape))
+    fields = initial_field(name, shape)
+    differences = reference_differences(name, shape)
+    run = PortRun(name, shape, threads, fields=fields)
     run.step(args.warmup)
     t0 = time.perf_counter()
     run.step(args.steps)
     dt = time.perf_counter() - t0
-    V = int(np.prod(shape))
+    run.close()
     value = V * args.steps / dt / 1e6
-    sample = (f"{w['latticeT']} {w['collisionT']} FP64 with the reference alpha solver on a "
-              f"{side}^3 sample of the workload's initial field, {threads} threads (x slabs)")
-    print(json.dumps({
-        "impl": "reference", "metric": metric_for(name), "value": value, "unit": "MLUPS", "n_gpus": 1,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-        "data": "synthetic", "config": {"workload": name, "grid": list(shape)},
+    sample = (f"{w['latticeT']} FP64 {solver_words(name)}, the workload's "
+              f"{'x'.join(map(str, shape))} grid and initial field, {args.warmup} warm-up + "
+              f"{args.steps} timed steps, {threads} threads (x slabs)")
+    line = {
+        "impl": "reference", "metric": metric_for(name), "value": value, "unit": "MLUPS",
+        "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": dt / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": name, "grid": list(shape), "same_config": not differences,
+                   "differences": differences, "alpha_solver": solver_words(name)},
         "cpu_baseline": {"value": value, "unit": "MLUPS", "cores": threads, "kind": "port",
                          "sample": sample},
         "e2e": {"value": value, "unit": "MLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-    }), flush=True)
+    }
+    if w["collisionT"] != "BGK":
+        ref = PortRun(name, shape, threads, alpha="reference", fields=fields)
+        t0 = time.perf_counter()
+        ref.step(1)
+        dtr = time.perf_counter() - t0
+        ref.close()
+        line["reference_alpha_solver"] = {
+            "value": V / dtr / 1e6, "unit": "MLUPS",
+            "sample": f"one step of the same run with {solver_words(name, 'reference')}"}
+    print(json.dumps(line), flush=True)
 
 
 def main():

@@ -95,6 +95,23 @@ class AlgorithmGPU {
     check(mlbm_get_fields(h_, densityPtr, velocityPtr, alphaPtr, forcePtr, MLBM_LAYOUT_REFERENCE), h_);
   }
 
+  // The Routine's spectral analyses of the last stored fields
+  // (Routine.h:69-72, 126-131; AnalysisList.h:55-73, 135-171): vorticity into
+  // the FieldList's vorticity array (reference layout), total energy and
+  // enstrophy, and the shell energy spectrum (spectraSize() values); any
+  // pointer may be null.
+  void analyses(double* vorticityPtr, double* totalEnergy, double* totalEnstrophy,
+                double* energySpectra) {
+    check(mlbm_get_spectral_diagnostics(h_, vorticityPtr, totalEnergy, totalEnstrophy,
+                                        energySpectra, MLBM_LAYOUT_REFERENCE),
+          h_);
+  }
+  int spectraSize() const {
+    int n = 0;
+    check(mlbm_spectrum_shells(h_, &n), h_);
+    return n;
+  }
+
   mlbm_diag diagnostics() {
     mlbm_diag d;
     check(mlbm_get_diagnostics(h_, &d), h_);

@@ -111,8 +111,13 @@ enum { MLBM_STORAGE_F64 = 0, MLBM_STORAGE_F32 = 1, MLBM_STORAGE_F16_SHIFTED = 2 
 enum { MLBM_ALPHA_REFERENCE = 0, MLBM_ALPHA_RESIDUAL = 1 };
 /* Starting guess of the alpha solve: the node's alpha from the previous step
  * (the reference, Algorithm.h:103-106), the constant 2, or the learned model
- * installed with mlbm_set_alpha_model. */
-enum { MLBM_GUESS_PREVIOUS = 0, MLBM_GUESS_TWO = 1, MLBM_GUESS_LEARNED = 2 };
+ * installed with mlbm_set_alpha_model. LEARNED runs the model where a node has
+ * no solved alpha from the previous step (its stored alpha is exactly 2:
+ * after mlbm_init_equilibrium, a restart, or an alpha = 2 fallback) and takes
+ * the previous alpha elsewhere; LEARNED_EVERYWHERE runs the model at every
+ * solved node. Both need FP32 / FP16 storage. */
+enum { MLBM_GUESS_PREVIOUS = 0, MLBM_GUESS_TWO = 1, MLBM_GUESS_LEARNED = 2,
+       MLBM_GUESS_LEARNED_EVERYWHERE = 3 };
 
 /* Host array layouts.
  * DENSE: component-major, node index (x*Ly + y)*Lz + z (z fastest, the
@@ -182,7 +187,8 @@ typedef struct {
   unsigned int reserved0;
   long long series_nodes;      /* solved nodes of the FP32/FP16-storage kernels whose
                                   entropy function took the moment-series form */
-  double reserved[5];
+  long long learned_nodes;     /* solved nodes whose guess came from the learned model */
+  double reserved[4];
 } mlbm_diag;
 
 /* Learned alpha guess: an MLP in -> 32 -> 32 -> 1 with tanh hidden layers.
@@ -251,6 +257,26 @@ int mlbm_get_fields(mlbm_handle* h, double* rho, double* u, double* alpha, doubl
  * re-initialises alpha to 2 (Initialize.h:82-89, 118-145). Synchronize. */
 int mlbm_get_alpha(mlbm_handle* h, double* alpha, int layout);
 int mlbm_set_alpha(mlbm_handle* h, const double* alpha, int layout);
+
+/* Number of shells of the energy spectrum: the reference's maxWaveNumber()
+ * (FourierDomain.h:77-79), arrayMax(globalLength) / 2, whose recursion takes
+ * the minimum of the remaining lengths (Helpers.h:37-39), so
+ * max(L_x, min(L_y, L_z)) / 2 with L_z = 1 on 2-D lattices. */
+int mlbm_spectrum_shells(const mlbm_handle* h, int* nshells);
+
+/* The spectral analyses the reference's Routine runs on the fields stored by
+ * the last MLBM_STEP_STORE_FIELDS step (Routine.h:69-72, 126-131;
+ * AnalysisList.h:55-73, 135-171), on the device (cuFFT): the vorticity
+ * [2D-3][V] by the spectral curl omega_hat = i k x u_hat with integer
+ * wavenumbers (Curl, Transformer.h:118-295, including its extra 1/V of
+ * Curl::normalize and, in 2-D, its real part of i k x u_hat only), the total
+ * energy (1/V) sum 1/2 rho |u|^2 and enstrophy (1/V) sum 1/2 |omega|^2
+ * (TotalEnergy / TotalEnstrophy, Analysis.h:33-98) and the shell energy
+ * spectrum [mlbm_spectrum_shells] (PowerSpectra, Analysis.h:122-177). The
+ * transform buffers (about 2.5 V doubles a component) are allocated on the
+ * first call. Any output may be NULL. Synchronizes. */
+int mlbm_get_spectral_diagnostics(mlbm_handle* h, double* vorticity, double* energy,
+                                  double* enstrophy, double* spectrum, int layout);
 
 /* Diagnostics and solver counters of the last mlbm_step call. Synchronizes. */
 int mlbm_get_diagnostics(mlbm_handle* h, mlbm_diag* out);

@@ -41,6 +41,14 @@ int mlbm_testing_alpha_solve(int lattice, double tol, int newton_maxit, int bise
                              long long n, const double* f, const double* fneq,
                              const double* guess, double* alpha, int* flags);
 
+/* One step from the handle's current populations that leaves them current:
+ * the step's output goes to the spare buffer, the step count does not move,
+ * and the per-node alpha field holds the alpha this step solved for. A
+ * following mlbm_step with the previous-alpha guess then starts every node
+ * from its exact root: the perfect-guess bound of the alpha solve
+ * (benchmarks). Enqueued on the handle's stream. */
+int mlbm_testing_step_in_place(mlbm_handle* h);
+
 #ifdef __cplusplus
 }
 #endif

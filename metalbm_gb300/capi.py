@@ -22,7 +22,7 @@ FORCE_NONE, FORCE_CONSTANT, FORCE_SINUSOIDAL, FORCE_KOLMOGOROV = 0, 1, 2, 3
 FORCE_CONSTANT_SHELL, FORCE_ENERGY_REMOVAL, FORCE_TURBULENT_2D = 4, 5, 6
 STORAGE_F64, STORAGE_F32, STORAGE_F16_SHIFTED = 0, 1, 2
 ALPHA_REFERENCE, ALPHA_RESIDUAL = 0, 1
-GUESS_PREVIOUS, GUESS_TWO, GUESS_LEARNED = 0, 1, 2
+GUESS_PREVIOUS, GUESS_TWO, GUESS_LEARNED, GUESS_LEARNED_EVERYWHERE = 0, 1, 2, 3
 LAYOUT_DENSE, LAYOUT_REFERENCE = 0, 1
 STEP_STORE_FIELDS, STEP_DIAGNOSTICS, STEP_LOG_SAMPLES = 1, 2, 4
 MLP_HIDDEN, MLP_MAX_IN = 32, 27
@@ -34,10 +34,10 @@ EXPORTS = [
     "mlbm_set_sample_nodes", "mlbm_get_samples", "mlbm_set_alpha_model",
     "mlbm_train_alpha_model", "mlbm_alpha_model_gradient", "mlbm_alpha_model_predict",
     "mlbm_last_error", "mlbm_kernel_launch_count", "mlbm_step_f64_noalloc",
-    "mlbm_get_alpha", "mlbm_set_alpha",
+    "mlbm_get_alpha", "mlbm_set_alpha", "mlbm_spectrum_shells", "mlbm_get_spectral_diagnostics",
 ]
 TESTING_EXPORTS = ["mlbm_testing_fast_log", "mlbm_testing_entropy", "mlbm_testing_neq",
-                   "mlbm_testing_alpha_solve"]
+                   "mlbm_testing_alpha_solve", "mlbm_testing_step_in_place"]
 
 
 class Config(ct.Structure):
@@ -62,7 +62,7 @@ class Diag(ct.Structure):
                 ("fallback_nodes", ct.c_longlong), ("limited_nodes", ct.c_longlong),
                 ("shortcut_nodes", ct.c_longlong), ("error_word", ct.c_uint),
                 ("reserved0", ct.c_uint), ("series_nodes", ct.c_longlong),
-                ("reserved", ct.c_double * 5)]
+                ("learned_nodes", ct.c_longlong), ("reserved", ct.c_double * 4)]
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_ if not k.startswith("reserved")}
@@ -122,12 +122,15 @@ def load(path: Path | str | None = None):
         "mlbm_last_error": ([vp], ct.c_char_p),
         "mlbm_kernel_launch_count": ([], ct.c_ulonglong),
         "mlbm_step_f64_noalloc": ([ct.POINTER(Config), vp, vp, vp, vp, vp, vp], ct.c_int),
+        "mlbm_spectrum_shells": ([vp, ct.POINTER(ct.c_int)], ct.c_int),
+        "mlbm_get_spectral_diagnostics": ([vp, dp, dp, dp, dp, ct.c_int], ct.c_int),
         "mlbm_testing_fast_log": ([dp, dp, ct.c_longlong], ct.c_int),
         "mlbm_testing_entropy": ([ct.c_int, fp, dp, ct.c_longlong, dp, ct.c_int, ct.c_int, dp,
                                   dp, ct.POINTER(ct.c_int)], ct.c_int),
         "mlbm_testing_neq": ([ct.c_int, fp, ct.c_longlong, ct.c_int, dp], ct.c_int),
         "mlbm_testing_alpha_solve": ([ct.c_int, ct.c_double, ct.c_int, ct.c_int, ct.c_longlong,
                                       dp, dp, dp, dp, ct.POINTER(ct.c_int)], ct.c_int),
+        "mlbm_testing_step_in_place": ([vp], ct.c_int),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)

@@ -10,9 +10,12 @@
 //                    <Lx> <Ly> <Lz> [<sync timeout ms> [<alpha solver 0..1>]]
 //   in.bin : float64 rho[V], u[D][V] dense (index (x*Ly+y)*Lz+z)
 //   out.bin: float64 f[Q][V], rho[V], u[D][V], alpha[V], force[D][V], seconds
+//   out.bin.analysis: float64 vorticity[2D-3][V], energy, enstrophy, K, spectrum[K]
+//            (the Routine's analyses of the stored fields, Routine.h:126-131)
 // Exit status: 0 done, 5 an mlbm error, 6 a wait for the device timed out.
 #include <cstdio>
 #include <cstdlib>
+#include <string>
 #include <vector>
 
 #include "mlbm/Algorithm_gpu.h"
@@ -108,6 +111,26 @@ int main(int argc, char** argv) {
     FILE* fo = std::fopen(argv[2], "wb");
     if (!fo || std::fwrite(out.data(), sizeof(double), out.size(), fo) != out.size()) return 4;
     std::fclose(fo);
+
+    // the Routine's analyses after the stored step: vorticity into the
+    // FieldList layout, energy, enstrophy and the shell spectrum
+    const int DV = 2 * D - 3, K = algorithm.spectraSize();
+    std::vector<double> vorticity((size_t)DV * n, 0.0), spectra((size_t)K);
+    double energy = 0.0, enstrophy = 0.0;
+    algorithm.analyses(vorticity.data(), &energy, &enstrophy, spectra.data());
+    std::vector<double> an((size_t)DV * V + 3 + K);
+    for (long x = 0; x < lx; ++x)
+      for (long y = 0; y < ly; ++y)
+        for (long z = 0; z < lz; ++z)
+          for (int c = 0; c < DV; ++c) an[c * V + dense(x, y, z)] = vorticity[c * n + ref(x, y, z)];
+    an[(size_t)DV * V] = energy;
+    an[(size_t)DV * V + 1] = enstrophy;
+    an[(size_t)DV * V + 2] = (double)K;
+    for (int k = 0; k < K; ++k) an[(size_t)DV * V + 3 + k] = spectra[k];
+    const std::string apath = std::string(argv[2]) + ".analysis";
+    FILE* fa = std::fopen(apath.c_str(), "wb");
+    if (!fa || std::fwrite(an.data(), sizeof(double), an.size(), fa) != an.size()) return 4;
+    std::fclose(fa);
   } catch (const mlbm::Error& e) {
     std::fprintf(stderr, "mlbm error %d: %s\n", e.code, e.what());
     return e.code == MLBM_ERR_TIMEOUT ? 6 : 5;

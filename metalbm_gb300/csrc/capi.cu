@@ -95,6 +95,7 @@ struct mlbm_handle {
   bool fields_valid = false;
   StepParams base{};
   SpectralForce* spectral = nullptr;  // spectral forces (FP64 storage)
+  SpectralDiag* sdiag = nullptr;      // spectral analyses, created on first use
   // the stored fields changed since the time-dependent force was computed
   // from them (its only inputs): recompute before the next step
   bool force_stale = true;
@@ -254,6 +255,7 @@ static void release(mlbm_handle* h) {
   for (void* p : ptrs)
     if (p) cudaFree(p);
   spectral_force_destroy(h->spectral);
+  spectral_diag_destroy(h->sdiag);
   if (h->own_stream) cudaStreamDestroy(h->own_stream);
   delete h;
 }
@@ -281,18 +283,24 @@ static const HostLattice& host_lattice(int lattice) {
 }
 static const double* lattice_weights(int lattice) { return host_lattice(lattice).w; }
 
-// Fine log table (1024 x {RN(1/c_j), RN(ln(1/inv_j))}) followed by the
-// lattice's constants C_q(d) = d ln 2 - ln(m_q), w_q = m_q 2^e_q.
-struct FineTable {
-  LogEntryFine t[LOG_TABLE_FINE];
-  double lnw[LNW_CONSTS];
-};
+// Fine log tables (1024 x {RN(1/c_j), RN(ln(1/inv_j))} and its float
+// companion {RN_float(1/c_j), ln(1/inv_j) as a float pair}) with the
+// lattice's constants C_q(d) = d ln 2 - ln(m_q), w_q = m_q 2^e_q (FP64) and
+// -ln(m_q) as float pairs (fastlog.cuh FineTables).
+using FineTable = FineTables;
 static void make_log_table_fine(FineTable* ft, int lattice) {
+  std::memset(ft, 0, sizeof *ft);
   for (int j = 0; j < LOG_TABLE_FINE; ++j) {
     const double c = 1.0 + (j + 0.5) / (double)LOG_TABLE_FINE;
     const double inv = 1.0 / c;
     ft->t[j].inv = inv;
     ft->t[j].hi = (double)(-std::log((long double)inv));
+    const float invf = (float)(1.0L / (long double)c);
+    const long double T = -std::log((long double)invf);
+    const float hi = (float)T;
+    ft->tf[j].inv = invf;
+    ft->tf[j].hi = hi;
+    ft->tf[j].lo = (float)(T - (long double)hi);
   }
   const double* wl = lattice_weights(lattice);
   const int Q = kQ[lattice];
@@ -303,6 +311,9 @@ static void make_log_table_fine(FineTable* ft, int lattice) {
     for (int d = -1; d <= 1; ++d)
       ft->lnw[3 * q + d + 1] =
           (double)((long double)d * 0.693147180559945309417232121458176568L - std::log(mw));
+    const long double C = -std::log(mw);
+    ft->lnwf[q][0] = (float)C;
+    ft->lnwf[q][1] = (float)(C - (long double)(float)C);
   }
 }
 
@@ -331,7 +342,7 @@ static int fill_alpha(mlbm_handle* h, double value) {
     a64.assign((size_t)h->V, value);
     MLBM_CUDA(h, cudaMemcpy(h->alpha, a64.data(), sizeof(double) * h->V, cudaMemcpyHostToDevice));
   } else {
-    a32.assign((size_t)h->V, (float)value);
+    a32.assign((size_t)h->V, (float)(value - 2.0));  // the device keeps alpha - 2
     MLBM_CUDA(h, cudaMemcpy(h->alpha32, a32.data(), sizeof(float) * h->V, cudaMemcpyHostToDevice));
   }
   return MLBM_OK;
@@ -357,8 +368,11 @@ extern "C" int mlbm_create(const mlbm_config* cfg, mlbm_handle** out) {
   if (!(c.relaxation_time > 0.5) || !std::isfinite(c.relaxation_time))
     return fail(nullptr, MLBM_ERR_INVALID, "relaxation time must be > 0.5 (got %g)", c.relaxation_time);
   if (c.alpha_mode < 0 || c.alpha_mode > 1) return fail(nullptr, MLBM_ERR_INVALID, "bad alpha mode");
-  if (c.alpha_guess < 0 || c.alpha_guess > 2) return fail(nullptr, MLBM_ERR_INVALID, "bad alpha guess");
-  if (c.alpha_guess == MLBM_GUESS_LEARNED && c.storage == MLBM_STORAGE_F64)
+  if (c.alpha_guess < 0 || c.alpha_guess > MLBM_GUESS_LEARNED_EVERYWHERE)
+    return fail(nullptr, MLBM_ERR_INVALID, "bad alpha guess");
+  const bool learned = c.alpha_guess == MLBM_GUESS_LEARNED ||
+                       c.alpha_guess == MLBM_GUESS_LEARNED_EVERYWHERE;
+  if (learned && c.storage == MLBM_STORAGE_F64)
     return fail(nullptr, MLBM_ERR_INVALID, "the learned alpha guess runs with FP32/FP16 storage");
   if (c.newton_max_iterations < 0 || c.bisection_max_iterations < 0 || !(c.newton_tolerance >= 0))
     return fail(nullptr, MLBM_ERR_INVALID, "bad Newton parameters");
@@ -666,19 +680,34 @@ extern "C" int mlbm_get_populations(mlbm_handle* h, double* f, int layout) {
   return MLBM_OK;
 }
 
+static int enqueue_step(mlbm_handle* h, bool last, unsigned int flags, bool in_place);
+
 extern "C" int mlbm_step(mlbm_handle* h, int nsteps, unsigned int flags) {
   if (!h) return MLBM_ERR_INVALID;
   if (nsteps < 0) return fail(h, MLBM_ERR_INVALID, "negative step count");
   if (nsteps == 0) return MLBM_OK;
   if ((flags & MLBM_STEP_LOG_SAMPLES) && h->n_samples == 0)
     return fail(h, MLBM_ERR_STATE, "LOG_SAMPLES without sample nodes (mlbm_set_sample_nodes)");
-  if (h->cfg.alpha_guess == MLBM_GUESS_LEARNED && h->cfg.collision != MLBM_BGK && !h->have_model)
+  if ((h->cfg.alpha_guess == MLBM_GUESS_LEARNED ||
+       h->cfg.alpha_guess == MLBM_GUESS_LEARNED_EVERYWHERE) &&
+      h->cfg.collision != MLBM_BGK && !h->have_model)
     return fail(h, MLBM_ERR_STATE, "learned alpha guess without a model (mlbm_set_alpha_model)");
   MLBM_CUDA(h, cudaSetDevice(h->cfg.device));
   MLBM_CUDA(h, cudaMemsetAsync(h->counters, 0, sizeof(unsigned long long) * CNT_COUNT, h->stream));
-  const int collision = h->cfg.collision == MLBM_BGK ? 0 : 1;
   for (int s = 0; s < nsteps; ++s) {
-    const bool last = s == nsteps - 1;
+    int rc = enqueue_step(h, s == nsteps - 1, flags, false);
+    if (rc) return rc;
+  }
+  return MLBM_OK;
+}
+
+// One pull step from the current populations (the body of mlbm_step). With
+// in_place the result goes to the spare buffer and the handle keeps the
+// current populations (no swap, no step counted; the alpha field and the
+// stored fields are updated as by a step).
+static int enqueue_step(mlbm_handle* h, bool last, unsigned int flags, bool in_place) {
+  const int collision = h->cfg.collision == MLBM_BGK ? 0 : 1;
+  {
     StepParams p = h->base;
     p.parity = (int)(h->steps & 1);
     p.store = last && (flags & MLBM_STEP_STORE_FIELDS) ? 1 : 0;
@@ -715,8 +744,13 @@ extern "C" int mlbm_step(mlbm_handle* h, int nsteps, unsigned int flags) {
       count_launches(1);
       if (e != cudaSuccess) return fail(h, MLBM_ERR_CUDA, "samples: %s", cudaGetErrorString(e));
     }
-    h->cur = 1 - h->cur;  // std::swap(prev, next), Algorithm.h:336
-    ++h->steps;
+    if (!in_place) {
+      h->cur = 1 - h->cur;  // std::swap(prev, next), Algorithm.h:336
+      ++h->steps;
+    } else if (h->defer_count) {
+      // the next step has the same parity: its worklist starts empty again
+      MLBM_CUDA(h, cudaMemsetAsync(h->defer_count + (h->steps & 1), 0, sizeof(unsigned), h->stream));
+    }
     if (p.store) {
       h->fields_valid = true;
       h->force_stale = true;
@@ -724,6 +758,12 @@ extern "C" int mlbm_step(mlbm_handle* h, int nsteps, unsigned int flags) {
     if (p.diag) h->diag_valid = true;
   }
   return MLBM_OK;
+}
+
+extern "C" int mlbm_testing_step_in_place(mlbm_handle* h) {
+  if (!h) return MLBM_ERR_INVALID;
+  MLBM_CUDA(h, cudaSetDevice(h->cfg.device));
+  return enqueue_step(h, true, 0u, true);
 }
 
 extern "C" int mlbm_sync(mlbm_handle* h, int timeout_ms) {
@@ -764,11 +804,50 @@ extern "C" int mlbm_get_fields(mlbm_handle* h, double* rho, double* u, double* a
       std::vector<float> a((size_t)h->V);
       std::vector<double> ad((size_t)h->V);
       MLBM_CUDA(h, cudaMemcpy(a.data(), h->alpha32, sizeof(float) * h->V, cudaMemcpyDeviceToHost));
-      for (long long i = 0; i < h->V; ++i) ad[i] = a[i];
+      for (long long i = 0; i < h->V; ++i) ad[i] = 2.0 + (double)a[i];
       if (layout == MLBM_LAYOUT_DENSE) std::memcpy(alpha, ad.data(), sizeof(double) * h->V);
       else ref_from_dense(h, ad.data(), alpha, 1);
     }
   }
+  return MLBM_OK;
+}
+
+extern "C" int mlbm_spectrum_shells(const mlbm_handle* h, int* nshells) {
+  if (!h || !nshells) return MLBM_ERR_INVALID;
+  *nshells = spectral_diag_shells(h->D, (int)h->lx, (int)h->ly, (int)h->lz);
+  return MLBM_OK;
+}
+
+extern "C" int mlbm_get_spectral_diagnostics(mlbm_handle* h, double* vorticity, double* energy,
+                                             double* enstrophy, double* spectrum, int layout) {
+  if (!h) return MLBM_ERR_INVALID;
+  if (!valid_layout(layout)) return fail(h, MLBM_ERR_INVALID, "bad layout");
+  if (!h->fields_valid) return fail(h, MLBM_ERR_STATE, "no stored fields (use MLBM_STEP_STORE_FIELDS)");
+  MLBM_CUDA(h, cudaSetDevice(h->cfg.device));
+  char msg[256] = {0};
+  if (!h->sdiag && spectral_diag_create(&h->sdiag, h->D, (int)h->lx, (int)h->ly, (int)h->lz,
+                                        h->stream, msg, sizeof msg))
+    return fail(h, MLBM_ERR_CUDA, "spectral analyses: %s", msg);
+  if (spectral_diag_run(h->sdiag, h->rho, h->u, h->stream, msg, sizeof msg))
+    return fail(h, MLBM_ERR_CUDA, "spectral analyses: %s", msg);
+  const int ncomp = 2 * h->D - 3;  // 1 vorticity component in 2-D, 3 in 3-D
+  const long long stride = layout == MLBM_LAYOUT_DENSE ? h->V : ref_layout(h).volume;
+  int rc;
+  for (int c = 0; c < ncomp; ++c) {
+    if (spectral_diag_curl(h->sdiag, c, h->stream, msg, sizeof msg))
+      return fail(h, MLBM_ERR_CUDA, "spectral analyses: %s", msg);
+    if (vorticity && (rc = download(h, spectral_diag_vorticity(h->sdiag), vorticity + c * stride, 1,
+                                    layout)))
+      return rc;
+  }
+  const int ns = spectral_diag_nshells(h->sdiag);
+  std::vector<double> res((size_t)(2 + ns));
+  MLBM_CUDA(h, cudaMemcpyAsync(res.data(), spectral_diag_results(h->sdiag),
+                               sizeof(double) * res.size(), cudaMemcpyDeviceToHost, h->stream));
+  MLBM_CUDA(h, cudaStreamSynchronize(h->stream));
+  if (energy) *energy = res[0];
+  if (enstrophy) *enstrophy = res[1];
+  if (spectrum) std::memcpy(spectrum, res.data() + 2, sizeof(double) * ns);
   return MLBM_OK;
 }
 
@@ -797,6 +876,7 @@ extern "C" int mlbm_get_diagnostics(mlbm_handle* h, mlbm_diag* out) {
   out->limited_nodes = (long long)c[CNT_LIMITED];
   out->shortcut_nodes = (long long)c[CNT_SHORTCUT];
   out->series_nodes = (long long)c[CNT_SERIES];
+  out->learned_nodes = (long long)c[CNT_INFER];
   out->error_word = err;
   return MLBM_OK;
 }
@@ -810,7 +890,7 @@ extern "C" int mlbm_get_alpha(mlbm_handle* h, double* alpha, int layout) {
   std::vector<float> a((size_t)h->V);
   std::vector<double> ad((size_t)h->V);
   MLBM_CUDA(h, cudaMemcpy(a.data(), h->alpha32, sizeof(float) * h->V, cudaMemcpyDeviceToHost));
-  for (long long i = 0; i < h->V; ++i) ad[i] = a[i];
+  for (long long i = 0; i < h->V; ++i) ad[i] = 2.0 + (double)a[i];
   if (layout == MLBM_LAYOUT_DENSE) std::memcpy(alpha, ad.data(), sizeof(double) * h->V);
   else ref_from_dense(h, ad.data(), alpha, 1);
   return MLBM_OK;
@@ -825,7 +905,8 @@ extern "C" int mlbm_set_alpha(mlbm_handle* h, const double* alpha, int layout) {
   std::vector<double> ad((size_t)h->V);
   if (layout == MLBM_LAYOUT_DENSE) std::memcpy(ad.data(), alpha, sizeof(double) * h->V);
   else dense_from_ref(h, alpha, ad.data(), 1);
-  std::vector<float> a(ad.begin(), ad.end());
+  std::vector<float> a((size_t)h->V);
+  for (long long i = 0; i < h->V; ++i) a[i] = (float)(ad[i] - 2.0);  // the device keeps alpha - 2
   MLBM_CUDA(h, cudaMemcpy(h->alpha32, a.data(), sizeof(float) * h->V, cudaMemcpyHostToDevice));
   return MLBM_OK;
 }

@@ -14,7 +14,7 @@ enum : int { FS_NONE = 0, FS_GUO = 1, FS_SHANCHEN = 2, FS_EDM = 3 };
 enum : int { FORCE_NONE = 0, FORCE_CONSTANT = 1, FORCE_SINUSOIDAL = 2, FORCE_KOLMOGOROV = 3,
              FORCE_FIELD = 7 };
 enum : int { ALPHA_REFERENCE = 0, ALPHA_RESIDUAL = 1 };
-enum : int { GUESS_PREVIOUS = 0, GUESS_TWO = 1, GUESS_LEARNED = 2 };
+enum : int { GUESS_PREVIOUS = 0, GUESS_TWO = 1, GUESS_LEARNED = 2, GUESS_LEARNED_EVERYWHERE = 3 };
 
 enum : unsigned { ERR_NONFINITE = 1u, ERR_DENSITY = 2u };
 
@@ -73,7 +73,7 @@ struct StepParams {
   double* u_out;             // [D][V]
   double* force_out;         // [D][V]
   double* alpha_field;       // FP64 storage: per-node alpha (read guess, write result)
-  float* alpha_field_f32;    // FP32 storage: per-node alpha
+  float* alpha_field_f32;    // FP32/FP16 storage: per-node alpha - 2
   double* diag_partials;     // per block: mass, energy, max_mach, alpha_min, alpha_max
   unsigned long long* counters;  // solver counters (see CNT_*)
   unsigned* err_word;
@@ -90,7 +90,7 @@ struct StepParams {
 
 enum : int {
   CNT_SOLVED = 0, CNT_ITER = 1, CNT_HITS = 2, CNT_BISECT = 3, CNT_FALLBACK = 4,
-  CNT_LIMITED = 5, CNT_SHORTCUT = 6, CNT_SERIES = 7, CNT_COUNT = 8
+  CNT_LIMITED = 5, CNT_SHORTCUT = 6, CNT_SERIES = 7, CNT_INFER = 8, CNT_COUNT = 9
 };
 constexpr int DIAG_FIELDS = 5;
 

@@ -166,6 +166,34 @@ __device__ __forceinline__ void stage_log_table_fine(LogEntryFine* sh, double* s
   for (int i = threadIdx.x; i < LNW_CONSTS; i += blockDim.x) sh_lnw[i] = c[i];
 }
 
+// Float companion of the fine table for the double-float evaluation of B1
+// (FP32 storage, whose populations are floats): inv = RN_float(1/c_j) and
+// ln(1/inv) as a float pair hi + lo (about 48 significant bits). For a float
+// mantissa m in the j-th interval, m inv - 1 = (RN(m inv) - 1) + the FMA
+// residual exactly, |m inv - 1| < 4.9e-4.
+struct LogEntryFineF {
+  float inv, hi, lo, pad;
+};
+
+// Device layout of the fine tables (built on the host): the FP64 table and
+// the lattice's constants C_q(d) (FP64), then the float table and -ln(m_q) of
+// each population's weight significand as float pairs.
+struct FineTables {
+  LogEntryFine t[LOG_TABLE_FINE];
+  double lnw[LNW_CONSTS];
+  double pad;
+  LogEntryFineF tf[LOG_TABLE_FINE];
+  float lnwf[27][2];
+};
+
+__device__ __forceinline__ void stage_log_table_fine_f(LogEntryFineF* sh, float2* sh_c,
+                                                       const FineTables* __restrict__ g) {
+  const float4* src = reinterpret_cast<const float4*>(g->tf);
+  float4* dst = reinterpret_cast<float4*>(sh);
+  for (int i = threadIdx.x; i < LOG_TABLE_FINE; i += blockDim.x) dst[i] = src[i];
+  for (int i = threadIdx.x; i < 27; i += blockDim.x) sh_c[i] = make_float2(g->lnwf[i][0], g->lnwf[i][1]);
+}
+
 // Binary exponent e of a positive constant w = m 2^e, m in [1, 2).
 __host__ __device__ constexpr int exponent_of(double w) {
   int e = 0;

@@ -107,6 +107,23 @@ const float* spectral_force_field_f(const SpectralForce* sf);
 bool spectral_force_time_dependent(const SpectralForce* sf);
 void spectral_force_destroy(SpectralForce* sf);
 
+// Spectral analyses of the stored fields (spectral_diag.cu): vorticity,
+// energy, enstrophy, shell spectrum. Functions return 0 on success, else
+// write a message to err.
+struct SpectralDiag;
+int spectral_diag_shells(int D, int lx, int ly, int lz);
+int spectral_diag_create(SpectralDiag** out, int D, int lx, int ly, int lz, cudaStream_t s,
+                         char* err, size_t errlen);
+void spectral_diag_destroy(SpectralDiag* sd);
+int spectral_diag_nshells(const SpectralDiag* sd);
+long long spectral_diag_volume(const SpectralDiag* sd);
+// device [energy, enstrophy, spectrum[nshells]]
+const double* spectral_diag_results(const SpectralDiag* sd);
+const double* spectral_diag_vorticity(const SpectralDiag* sd);
+int spectral_diag_run(SpectralDiag* sd, const double* rho, const double* u, cudaStream_t s,
+                      char* err, size_t errlen);
+int spectral_diag_curl(SpectralDiag* sd, int c, cudaStream_t s, char* err, size_t errlen);
+
 // Per-lattice (and per-storage) entry points, one translation unit each.
 cudaError_t step_f64_L0(int collision, int forcing, const double* prev, double* next, const StepParams& p, cudaStream_t s);
 cudaError_t init_f64_L0(const double* rho, const double* u, double* f, long long V, cudaStream_t s);

@@ -324,7 +324,7 @@ __global__ void __launch_bounds__(128) elbm_f64_kernel(const double* __restrict_
   const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const bool active = idx < p.V;
   double mass = 0.0, energy = 0.0, mach = 0.0, amin = 1e300, amax = -1e300;
-  unsigned cnt[CNT_COUNT] = {0, 0, 0, 0, 0, 0, 0, 0};
+  unsigned cnt[CNT_COUNT] = {};
   if (active) {
     uint32_t x, y, z;
     node_coords(p, idx, x, y, z);
@@ -433,7 +433,7 @@ __global__ void __launch_bounds__(128) alpha_solve_test_kernel(
     fi[q] = f[i * L::Q + q];
     ni[q] = fneq[i * L::Q + q];
   }
-  unsigned c[CNT_COUNT] = {0, 0, 0, 0, 0, 0, 0, 0};
+  unsigned c[CNT_COUNT] = {};
   alpha[i] = entropic_alpha<LAT>(p, fi, ni, guess[i], c, s_log);
   flags[i] = (c[CNT_LIMITED] ? 1 : 0) | (c[CNT_BISECT] ? 2 : 0) | (c[CNT_FALLBACK] ? 4 : 0);
 }

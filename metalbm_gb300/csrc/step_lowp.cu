@@ -268,7 +268,7 @@ __device__ __forceinline__ void store_fields_f64(const StepParams& p, long long 
       p.u_out[(long long)k * p.V + idx] = uh[k];
       p.force_out[(long long)k * p.V + idx] = F[k];
     }
-    if (p.alpha_field_f32 && write_alpha) p.alpha_field_f32[idx] = narrow_rn(alpha);
+    if (p.alpha_field_f32 && write_alpha) p.alpha_field_f32[idx] = narrow_rn(alpha - 2.0);
   }
   if (p.diag) {
     double e = 0.0, s = 0.0;
@@ -645,12 +645,20 @@ __device__ __forceinline__ long long fixed64(double v) {
 // x (B1 + sum f_neq) with |ln(f/w)| <= 1: at most 2.5 x 2 x 4.6e-14 rho.
 constexpr float kNeqDflBound = 2.3e-13f;
 
+// FP32 storage forms B1 and M2 in double-float arithmetic (series_dfl): each
+// ln(f/w) is within 7e-14 (the float pair of ln(1/inv_j), the exact
+// reduction residual, the FP32 tail r'^2 (r'/3 - 1/2 - r'/4) with its
+// roundings), so B1 is within 7.5e-14 rho rmax (products and sums add
+// 2^-47 of the terms) and F within 2.5 times that; M2 carries a relative
+// 1e-13 (the truncated 1/f = y0 (1 + e), double-float roundings), at most
+// 3.2e-13 rho rmax^2 in F. FP16 storage keeps the FP64 sums (6e-13 rho rmax).
 template <int LAT, int ST>
 __device__ __forceinline__ double series_error_bound(float rabs, double rho) {
   const float r = rabs, rf = narrow_rn(rho);
   const float m = r <= kSeriesTierA ? 6.0e-6f * r * r * r : 1.2e-5f * (r * r) * (r * r) * r;
   const float dfl_term = (ST == ST_F32 && MLBM_NEQ_DFLOAT) ? kNeqDflBound : 0.0f;
-  return widen_exact(fmaf(rf, fmaf(6.0e-13f, r, m) + dfl_term, 1.0e-15f));
+  const float b1 = ST == ST_F32 ? fmaf(3.2e-13f, r, 2.0e-13f) * r : 6.0e-13f * r;
+  return widen_exact(fmaf(rf, (b1 + m) + dfl_term, 1.0e-15f));
 }
 
 // B1 and the moments (series form), or r_q in place of f_neq_q in n[]
@@ -743,6 +751,127 @@ __device__ __forceinline__ HLowp<LAT, ST, SERIES> make_entropy_eval(const Pulled
   }
   ev.D = HLowpDirect<LAT, ST>{&P, n, B1, (double)rabs, tab};
   return ev;
+}
+
+// The moment-series coefficients of an FP32-storage node from f_neq in
+// double-float form, with no FP64 arithmetic in the population loop:
+//   B1 = sum_q f_neq_q ln(f_q/w_q), ln(f/w) = d ln2 - ln(m_q) + ln(1/inv_j)
+//        + log1p(r'), r' = m inv_j - 1 (m the float mantissa of f, exact as
+//        RN(m inv_j) - 1 plus the FMA residual), log1p(r') = r' + r'^2 (r'/3
+//        - 1/2 - r'/4) with the tail in FP32; the d ln2 parts accumulate as
+//        sum_q d_q f_neq_q, and on lattices with one weight significand the
+//        -ln(m_q) parts cancel (sum_q f_neq_q = 0);
+//   M2 = sum_q f_neq_q^2 / f_q with 1/f = y0 (1 + e), y0 the SFU reciprocal,
+//        e = 1 - f y0 from one FMA;
+// both as double-float sums (TwoSum on the running high part), rounded once
+// to FP64 at the end. M3..M8 as in make_entropy_eval (FP32 sums in tier A,
+// M3 and M4 in FP64 in tier B). The error bound is series_error_bound.
+template <int LAT>
+__device__ __forceinline__ HSeries make_series_dfl(const Pulled<LAT, ST_F32>& P, const dfl nd[],
+                                                   float nfr[], float rabs,
+                                                   const LogEntryFineF* fine,
+                                                   const float2* mconst) {
+  using L = Lattice<LAT>;
+  constexpr bool kUniform = uniform_weight_significand<LAT>();
+  const bool tierB = rabs > kSeriesTierA;
+  float bh = 0.0f, bl = 0.0f;  // B1 without the exponent parts
+  float eh = 0.0f, el = 0.0f;  // sum_q d_q f_neq_q
+  float mh = 0.0f, ml = 0.0f;  // M2
+  double M3 = 0.0, M4 = 0.0;
+  float M3f = 0.0f, M4f = 0.0f, M5 = 0.0f, M6 = 0.0f, M7 = 0.0f, M8 = 0.0f;
+#pragma unroll
+  for (int q = 0; q < L::Q; ++q) {
+    const float f = P.v[q];
+    const dfl n = nd[q];
+    nfr[q] = n.hi;
+    // ln(f/w) without d ln2: -ln(m_q) + ln(1/inv_j) + log1p(r')
+    const uint32_t b = __float_as_uint(f);
+    const int d = (int)((b >> 23) & 0xffu) - (127 + exponent_of(L::w(q)));
+    const LogEntryFineF t = fine[(b >> 13) & (LOG_TABLE_FINE - 1)];
+    const float m = __uint_as_float((b & 0x7fffffu) | 0x3f800000u);
+    const float pr = __fmul_rn(m, t.inv);
+    const float pe = __fmaf_rn(m, t.inv, -pr);  // exact residual of the product
+    const float pm1 = __fsub_rn(pr, 1.0f);      // exact (pr within 2^-10 of 1)
+    const float rp = __fadd_rn(pm1, pe);
+    const float tail = __fmul_rn(__fmul_rn(rp, rp),
+                                 __fmaf_rn(rp, __fmaf_rn(rp, -0.25f, 1.0f / 3.0f), -0.5f));
+    float Lh, Le, lo;
+    if constexpr (kUniform) {
+      two_sum(t.hi, pm1, Lh, Le);
+      lo = __fadd_rn(__fadd_rn(__fadd_rn(t.lo, Le), pe), tail);
+    } else {
+      const float2 C = mconst[q];
+      float s1, e1;
+      two_sum(C.x, t.hi, s1, e1);
+      two_sum(s1, pm1, Lh, Le);
+      lo = __fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(C.y, t.lo), e1), Le), pe), tail);
+    }
+    // B1 += f_neq ln(f/w) (double-float product and sum)
+    {
+      const float tp = __fmul_rn(n.hi, Lh);
+      float te = __fmaf_rn(n.hi, Lh, -tp);
+      te = __fmaf_rn(n.hi, lo, __fmaf_rn(n.lo, Lh, te));
+      float e3;
+      two_sum(bh, tp, bh, e3);
+      bl = __fadd_rn(bl, __fadd_rn(e3, te));
+    }
+    // the exponent part: sum_q d_q f_neq_q (d small; the product's residual
+    // by FMA)
+    {
+      const float dd = __fsub_rn(__int_as_float(0x4B400000 + d), 12582912.0f);  // (float)d
+      const float tp = __fmul_rn(n.hi, dd);
+      const float te = __fmaf_rn(n.lo, dd, __fmaf_rn(n.hi, dd, -tp));
+      float e3;
+      two_sum(eh, tp, eh, e3);
+      el = __fadd_rn(el, __fadd_rn(e3, te));
+    }
+    // M2 += f_neq^2 y0 (1 + e)
+    const float y0 = rcp_sfu(f);
+    const float ee = __fmaf_rn(-f, y0, 1.0f);
+    {
+      const float sq = __fmul_rn(n.hi, n.hi);
+      const float sqe = __fmaf_rn(2.0f * n.hi, n.lo, __fmaf_rn(n.hi, n.hi, -sq));
+      const float tq = __fmul_rn(sq, y0);
+      float tqe = __fmaf_rn(sq, y0, -tq);
+      tqe = __fmaf_rn(tq, ee, __fmaf_rn(sqe, y0, tqe));
+      float e4;
+      two_sum(mh, tq, mh, e4);
+      ml = __fadd_rn(ml, __fadd_rn(e4, tqe));
+    }
+    // higher moments
+    const float rf = n.hi * y0;
+    float tt = n.hi * (rf * rf);  // f r^3
+    if (tierB) {
+      const double nq = widen_exact(n.hi) + widen_exact(n.lo);
+      const double y = widen_exact(y0);
+      const double g = nq * fma(y, widen_exact(ee), y);  // r_q
+      const double p2 = g * nq;
+      M3 = fma(p2, g, M3);
+      M4 = fma(p2 * g, g, M4);
+    } else {
+      M3f += tt;
+      M4f = fmaf(tt, rf, M4f);
+    }
+    tt *= rf * rf; M5 += tt;  // f r^5
+    tt *= rf; M6 += tt;
+    tt *= rf; M7 += tt;
+    tt *= rf; M8 += tt;
+  }
+  // B1 = (bh + bl) + ln2 (eh + el), M2 = mh + ml, each rounded once to FP64
+  dfl B{bh, bl}, E{eh, el}, M{mh, ml};
+  fast_two_sum(B.hi, B.lo, B.hi, B.lo);
+  fast_two_sum(E.hi, E.lo, E.hi, E.lo);
+  fast_two_sum(M.hi, M.lo, M.hi, M.lo);
+  constexpr float kLn2F = 0x1.62e43p-1f;                  // RN_float(ln 2)
+  constexpr float kLn2FLo = -0x1.05c610p-29f;             // ln 2 - kLn2F
+  B = dfl_add(B, dfl_mul(E, dfl{kLn2F, kLn2FLo}));
+  const double B1 = dfl_to_double(B);
+  const double M2 = dfl_to_double(M);
+  if (!tierB) { M3 = widen_exact(M3f); M4 = widen_exact(M4f); }
+  return HSeries{B1, M2 * 0.5, M3 * (1.0 / 6.0), M4 * (1.0 / 12.0), M2, M3 * 0.5,
+                 M4 * (1.0 / 3.0), M5 * (1.0f / 20.0f), M6 * (1.0f / 30.0f),
+                 M7 * (1.0f / 42.0f), M8 * (1.0f / 56.0f), M5 * 0.25f, M6 * 0.2f,
+                 M7 * (1.0f / 6.0f), M8 * (1.0f / 7.0f)};
 }
 
 // v * 2^60 as an exact integer for a float |v| < 4 (bits below 2^-60
@@ -843,7 +972,7 @@ __device__ __forceinline__ void neq_pairs(const Pulled<LAT, ST>& P, double rho, 
 // cycles than the FP64 form.
 template <int LAT>
 __device__ __forceinline__ void neq_pairs_dfl(const Pulled<LAT, ST_F32>& P, double rho,
-                                              const double u[3], double n[]) {
+                                              const double u[3], dfl n[]) {
   using L = Lattice<LAT>;
   const dfl r = dfl_from(rho);
   const dfl ux = dfl_from(u[0]), uy = dfl_from(u[1]), uz = dfl_from(u[2]);
@@ -862,7 +991,7 @@ __device__ __forceinline__ void neq_pairs_dfl(const Pulled<LAT, ST_F32>& P, doub
   {
     const dfl rw = rw_of(0);
     const dfl feq = dfl_add(rw, dfl_mul(rw, common));
-    n[0] = dfl_to_double(dfl_add_f(dfl_neg(feq), P.v[0]));
+    n[0] = dfl_add_f(dfl_neg(feq), P.v[0]);
   }
 #pragma unroll
   for (int q = 1; q < L::Q; ++q) {
@@ -883,10 +1012,20 @@ __device__ __forceinline__ void neq_pairs_dfl(const Pulled<LAT, ST_F32>& P, doub
       const dfl rw = rw_of(q);
       const dfl A1 = dfl_add(rw, dfl_mul(rw, E));  // rho w (1 + E)
       const dfl B1 = dfl_mul(rw, O);               // rho w O
-      n[q] = dfl_to_double(dfl_sub(dfl_add_f(dfl_neg(A1), P.v[q]), B1));
-      n[qb] = dfl_to_double(dfl_add(dfl_add_f(dfl_neg(A1), P.v[qb]), B1));
+      n[q] = dfl_sub(dfl_add_f(dfl_neg(A1), P.v[q]), B1);
+      n[qb] = dfl_add(dfl_add_f(dfl_neg(A1), P.v[qb]), B1);
     }
   }
+}
+
+// The same rounded once to FP64 (tests).
+template <int LAT>
+__device__ __forceinline__ void neq_pairs_dfl(const Pulled<LAT, ST_F32>& P, double rho,
+                                              const double u[3], double n[]) {
+  dfl nd[Lattice<LAT>::Q];
+  neq_pairs_dfl<LAT>(P, rho, u, nd);
+#pragma unroll
+  for (int q = 0; q < Lattice<LAT>::Q; ++q) n[q] = dfl_to_double(nd[q]);
 }
 
 // The entropic step runs as two kernels. The main pass completes every node
@@ -903,7 +1042,8 @@ __device__ __forceinline__ void elbm_node(const typename Storage<ST>::T* __restr
                                           typename Storage<ST>::T* __restrict__ next,
                                           const StepParams& p, bool active, long long idx,
                                           const LogEntry* s_log, const LogEntryFine* s_fine,
-                                          const double* s_lnw, unsigned cnt[], bool& defer,
+                                          const double* s_lnw, const LogEntryFineF* s_finef,
+                                          const float2* s_mconst, unsigned cnt[], bool& defer,
                                           double& mass,
                                           double& energy, double& mach, double& amin,
                                           double& amax) {
@@ -923,11 +1063,22 @@ __device__ __forceinline__ void elbm_node(const typename Storage<ST>::T* __restr
 #pragma unroll
     for (int q = 0; q < L::Q; ++q) P.v[q] = ST == ST_F32 ? (float)L::w(q) : 0.0f;
   }
-  // Learned guess: every thread of the block takes part (tile inference), on
-  // features f_neq / rho from the FP32 deviations (computed before the FP64
-  // part, so that the inference and the FP64 f_neq are not live together)
+  // Learned guess: the network runs for the nodes without a solved alpha
+  // from the previous step (the stored alpha is exactly 2 after
+  // initialisation, a restart or an alpha = 2 fallback; a solved root is not
+  // 2 to the last bit), or for every node with GUESS_LEARNED_EVERYWHERE; the
+  // previous alpha is the guess elsewhere (the field holds alpha - 2, so
+  // exactly 0 there). The inference is a warp tile
+  // (every lane of a warp that has such a node takes part), on features
+  // f_neq / rho from the FP32 deviations (computed before the FP64 part, so
+  // that the inference and the FP64 f_neq are not live together).
   float learned = 0.0f;
+  bool need_learned = false;
   if (LEARNED) {
+    need_learned = active && (p.guess_mode == GUESS_LEARNED_EVERYWHERE ||
+                              p.alpha_field_f32[idx] == 0.0f);
+  }
+  if (LEARNED && __any_sync(0xffffffffu, need_learned)) {
     float dv[L::Q], rhopf, rf, uf[3], deq[L::Q];
 #pragma unroll
     for (int q = 0; q < L::Q; ++q) dv[q] = P.dev(q);
@@ -946,14 +1097,22 @@ __device__ __forceinline__ void elbm_node(const typename Storage<ST>::T* __restr
   const double ir = recip_refined(rho, narrow_rn(rho));
 #pragma unroll
   for (int k = 0; k < 3; ++k) u[k] = j[k] * ir;
-  double n[L::Q];
-  if constexpr (MODE == ELBM_MAIN && ST == ST_F32 && MLBM_NEQ_DFLOAT) neq_pairs_dfl<LAT>(P, rho, u, n);
+  // FP32 storage, main pass: f_neq stays in double-float form and the
+  // series sums run on the FP32 pipe (make_series_dfl); otherwise FP64 f_neq
+  constexpr bool kDfl = MODE == ELBM_MAIN && ST == ST_F32 && MLBM_NEQ_DFLOAT;
+  double n[kDfl ? 1 : L::Q];
+  dfl nd[kDfl ? L::Q : 1];
+  if constexpr (kDfl) neq_pairs_dfl<LAT>(P, rho, u, nd);
   else neq_pairs<LAT, ST>(P, rho, rhop, u, n);
+  auto nf_of = [&](int q) {
+    if constexpr (kDfl) return nd[q].hi;
+    else return narrow_rn(n[q]);
+  };
   // r_q = n_q / f_q in FP32 for the bracket and the tests
   float rpos = 0.0f, rabs = 0.0f;
 #pragma unroll
   for (int q = 0; q < L::Q; ++q) {
-    const float rq = narrow_rn(n[q]) * rcp_sfu(P.f32(q));
+    const float rq = nf_of(q) * rcp_sfu(P.f32(q));
     rpos = fmaxf(rpos, rq);
     rabs = fmaxf(rabs, fabsf(rq));
   }
@@ -970,12 +1129,12 @@ __device__ __forceinline__ void elbm_node(const typename Storage<ST>::T* __restr
     ++cnt[CNT_SHORTCUT];
     alpha = 2.0;
 #pragma unroll
-    for (int q = 0; q < L::Q; ++q) nf[q] = narrow_rn(n[q]);
+    for (int q = 0; q < L::Q; ++q) nf[q] = nf_of(q);
   } else if (MODE == ELBM_MAIN && alphaMax < 2.0) {
     ++cnt[CNT_LIMITED];
     alpha = 0.95 * alphaMax;
 #pragma unroll
-    for (int q = 0; q < L::Q; ++q) nf[q] = narrow_rn(n[q]);
+    for (int q = 0; q < L::Q; ++q) nf[q] = nf_of(q);
   }
   else {
     const bool series = MODE == ELBM_MAIN && rabs <= kSeriesRmax;
@@ -985,10 +1144,16 @@ __device__ __forceinline__ void elbm_node(const typename Storage<ST>::T* __restr
       ++cnt[CNT_SOLVED];
       if (series) ++cnt[CNT_SERIES];
       direct = !series;
-      const double prevA = widen_exact(p.alpha_field_f32[idx]);
+      const double prevA = 2.0 + widen_exact(p.alpha_field_f32[idx]);
       const double plain = p.guess_mode == GUESS_TWO ? 2.0 : prevA;
-      const double guess = LEARNED ? 2.0 + widen_exact(learned) : plain;
-      if constexpr (MODE == ELBM_MAIN) {
+      const double guess = LEARNED && need_learned ? 2.0 + widen_exact(learned) : plain;
+      if (LEARNED && need_learned) ++cnt[CNT_INFER];
+      if constexpr (kDfl) {
+        const HSeries ev = make_series_dfl<LAT>(P, nd, nf, rabs, s_finef, s_mconst);
+        const double tol = p.newton_tol - series_error_bound<LAT, ST>(rabs, rho);
+        alpha = residual_alpha_solve<HSeries, true>(ev, guess, plain, alphaMax, tol,
+                                                    p.newton_maxit, p.bisect_maxit, cnt);
+      } else if constexpr (MODE == ELBM_MAIN) {
         const auto ev = make_entropy_eval<LAT, ST, true>(P, n, nf, rabs, s_log, s_fine, s_lnw);
         const double tol = p.newton_tol - series_error_bound<LAT, ST>(rabs, rho);
         alpha = residual_alpha_solve<decltype(ev), true>(ev, guess, plain, alphaMax, tol,
@@ -1053,18 +1218,23 @@ __device__ __forceinline__ void elbm_node(const typename Storage<ST>::T* __restr
     }
 #pragma unroll
     for (int q = 0; q < L::Q; ++q) {
-      const float nfq = direct ? narrow_rn(n[q] * P.f64(q)) : nf[q];
+      float nfq = nf[q];
+      if constexpr (!kDfl) {
+        if (direct) nfq = narrow_rn(n[q] * P.f64(q));
+      }
       float rr = fmaf(-ab, nfq, P.v[q]);  // f (F32) or f - w (F16)
       if (FS == FS_GUO || FS == FS_EDM) rr += src[q];
       auto* dst = pop(next, p.V, q) + (uint32_t)idx;
       if constexpr (ST == ST_F32) *dst = rr;
       else *dst = __float2half_rn(rr * (float)(1 << shift_exponent<LAT>(q)));
     }
-    const float stored = narrow_rn(alpha);  // alpha persists in FP32
+    // alpha persists as alpha - 2 in FP32: near 2 its rounding is ~1e-11
+    // absolute, so the previous alpha stays a guess to FP64 accuracy
+    const float stored = narrow_rn(alpha - 2.0);
     p.alpha_field_f32[idx] = stored;
     if (p.diag) {
-      amin = fmin(amin, widen_exact(stored));
-      amax = fmax(amax, widen_exact(stored));
+      amin = fmin(amin, 2.0 + widen_exact(stored));
+      amax = fmax(amax, 2.0 + widen_exact(stored));
     }
   }
   if (MODE == ELBM_MAIN) {
@@ -1096,9 +1266,17 @@ template <int LAT, int FS, int ST, bool LEARNED>
 __global__ void __launch_bounds__(128, LEARNED ? MLBM_ELBM_MIN_BLOCKS_LEARNED : MLBM_ELBM_MIN_BLOCKS) elbm_lowp_kernel(const typename Storage<ST>::T* __restrict__ prev,
                                                         typename Storage<ST>::T* __restrict__ next,
                                                         StepParams p) {
-  __shared__ LogEntryFine s_fine[LOG_TABLE_FINE];
-  __shared__ double s_lnw[LNW_CONSTS];
-  stage_log_table_fine(s_fine, s_lnw, reinterpret_cast<const LogEntryFine*>(p.log_table_fine));
+  // FP32 storage: the float table of the double-float series sums; FP16
+  // storage: the FP64 table
+  constexpr bool kDfl = ST == ST_F32 && MLBM_NEQ_DFLOAT;
+  __shared__ __align__(16) LogEntryFineF s_finef[kDfl ? LOG_TABLE_FINE : 1];
+  __shared__ float2 s_mconst[kDfl ? 27 : 1];
+  __shared__ LogEntryFine s_fine[kDfl ? 1 : LOG_TABLE_FINE];
+  __shared__ double s_lnw[kDfl ? 1 : LNW_CONSTS];
+  if constexpr (kDfl)
+    stage_log_table_fine_f(s_finef, s_mconst, reinterpret_cast<const FineTables*>(p.log_table_fine));
+  else
+    stage_log_table_fine(s_fine, s_lnw, reinterpret_cast<const LogEntryFine*>(p.log_table_fine));
   // the worklist counter of the next step (its last reader was the previous
   // step's second pass, which has completed)
   if (blockIdx.x == 0 && threadIdx.x == 0) p.defer_count[p.parity ^ 1] = 0u;
@@ -1106,10 +1284,11 @@ __global__ void __launch_bounds__(128, LEARNED ? MLBM_ELBM_MIN_BLOCKS_LEARNED : 
   const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const bool active = idx < p.V;
   double mass = 0.0, energy = 0.0, mach = 0.0, amin = 1e300, amax = -1e300;
-  unsigned cnt[CNT_COUNT] = {0, 0, 0, 0, 0, 0, 0, 0};
+  unsigned cnt[CNT_COUNT] = {};
   bool defer = false;
   elbm_node<LAT, FS, ST, LEARNED, ELBM_MAIN>(prev, next, p, active, idx, nullptr, s_fine, s_lnw,
-                                             cnt, defer, mass, energy, mach, amin, amax);
+                                             s_finef, s_mconst, cnt, defer, mass, energy, mach,
+                                             amin, amax);
   // warp-aggregated append to the worklist
   const unsigned m = __ballot_sync(0xffffffffu, defer);
   if (m) {
@@ -1133,7 +1312,7 @@ __global__ void __launch_bounds__(128) elbm_lowp_deferred_kernel(const typename 
   __syncthreads();
   const long long count = (long long)p.defer_count[p.parity];
   double mass = 0.0, energy = 0.0, mach = 0.0, amin = 1e300, amax = -1e300;
-  unsigned cnt[CNT_COUNT] = {0, 0, 0, 0, 0, 0, 0, 0};
+  unsigned cnt[CNT_COUNT] = {};
   for (long long b = (long long)blockIdx.x * blockDim.x; b < count;
        b += (long long)gridDim.x * blockDim.x) {
     const long long i = b + threadIdx.x;
@@ -1141,8 +1320,8 @@ __global__ void __launch_bounds__(128) elbm_lowp_deferred_kernel(const typename 
     const long long idx = active ? (long long)p.defer_list[i] : 0;
     bool defer = false;
     elbm_node<LAT, FS, ST, LEARNED, ELBM_DEFERRED>(prev, next, p, active, idx, s_log, nullptr,
-                                                   nullptr, cnt, defer, mass, energy, mach, amin,
-                                                   amax);
+                                                   nullptr, nullptr, nullptr, cnt, defer, mass,
+                                                   energy, mach, amin, amax);
   }
   add_counters(p.counters, cnt);
   if (p.diag)
@@ -1163,10 +1342,10 @@ __global__ void entropy_test_kernel(const float* __restrict__ f, const double* _
                                     int* __restrict__ series_out) {
   using L = Lattice<LAT>;
   __shared__ LogEntry s_log[LOG_TABLE];
-  __shared__ LogEntryFine s_fine[LOG_TABLE_FINE];
-  __shared__ double s_lnw[LNW_CONSTS];
+  __shared__ __align__(16) LogEntryFineF s_finef[LOG_TABLE_FINE];
+  __shared__ float2 s_mconst[27];
   stage_log_table(s_log, table);
-  stage_log_table_fine(s_fine, s_lnw, table_fine);
+  stage_log_table_fine_f(s_finef, s_mconst, reinterpret_cast<const FineTables*>(table_fine));
   __syncthreads();
   const long long s = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= nodes) return;
@@ -1182,10 +1361,15 @@ __global__ void entropy_test_kernel(const float* __restrict__ f, const double* _
   }
   const bool series = mode == 2 || (mode == 0 && rabs <= kSeriesRmax);
   if (series) {
-    const auto ev = make_entropy_eval<LAT, ST_F32, true>(P, n, nf, rabs, s_log, s_fine, s_lnw);
+    // the main pass's form: f_neq as double-float pairs, B1 and M2 in
+    // double-float arithmetic
+    dfl nd[L::Q];
+#pragma unroll
+    for (int q = 0; q < L::Q; ++q) nd[q] = dfl_from(n[q]);
+    const HSeries ev = make_series_dfl<LAT>(P, nd, nf, rabs, s_finef, s_mconst);
     for (int i = 0; i < nx; ++i) ev(xs[i], Fo[s * nx + i], Do[s * nx + i]);
   } else {
-    const auto ev = make_entropy_eval<LAT, ST_F32, false>(P, n, nf, rabs, s_log, s_fine, s_lnw);
+    const auto ev = make_entropy_eval<LAT, ST_F32, false>(P, n, nf, rabs, s_log, nullptr, nullptr);
     for (int i = 0; i < nx; ++i) ev(xs[i], Fo[s * nx + i], Do[s * nx + i]);
   }
   series_out[s] = series ? 1 : 0;
@@ -1294,7 +1478,7 @@ __global__ void samples_lowp_kernel(const typename Storage<ST>::T* __restrict__ 
     if (fabs(fn[q]) > p.deviation_threshold * f[q]) small = false;
     if (fn[q] > 0.0) alphaMax = fmin(alphaMax, f[q] / fn[q]);
   }
-  alpha[s] = (double)p.alpha_field_f32[idx];
+  alpha[s] = 2.0 + (double)p.alpha_field_f32[idx];
   solved[s] = (!small && alphaMax >= 2.0) ? 1 : 0;
 }
 
@@ -1315,7 +1499,7 @@ static cudaError_t launch_lowp(int collision, const void* prev, void* next, cons
   } else {
     const int bs = 128;
     const unsigned grid = (unsigned)((p.V + bs - 1) / bs);
-    if (p.guess_mode == GUESS_LEARNED) {
+    if (p.guess_mode == GUESS_LEARNED || p.guess_mode == GUESS_LEARNED_EVERYWHERE) {
       elbm_lowp_kernel<LAT, FS, ST, true><<<grid, bs, 0, s>>>((const T*)prev, (T*)next, p);
       elbm_lowp_deferred_kernel<LAT, FS, ST, true><<<p.defer_blocks, bs, 0, s>>>((const T*)prev, (T*)next, p);
     } else {

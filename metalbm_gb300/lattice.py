@@ -33,7 +33,8 @@ _FORCES = {"None": capi.FORCE_NONE, "Constant": capi.FORCE_CONSTANT,
 _STORAGES = {"f64": capi.STORAGE_F64, "f32": capi.STORAGE_F32,
              "f16_shifted": capi.STORAGE_F16_SHIFTED}
 _ALPHA = {"reference": capi.ALPHA_REFERENCE, "residual": capi.ALPHA_RESIDUAL}
-_GUESS = {"previous": capi.GUESS_PREVIOUS, "two": capi.GUESS_TWO, "learned": capi.GUESS_LEARNED}
+_GUESS = {"previous": capi.GUESS_PREVIOUS, "two": capi.GUESS_TWO, "learned": capi.GUESS_LEARNED,
+          "learned_everywhere": capi.GUESS_LEARNED_EVERYWHERE}
 # default limit of Lattice.sync (a bounded poll; -1 waits without limit)
 SYNC_TIMEOUT_MS = 600_000
 Q_OF = {"D2Q9": 9, "D3Q19": 19, "D3Q27": 27, "D3Q15": 15, "D2Q13": 13, "D3Q33": 33}
@@ -356,6 +357,20 @@ class Lattice:
         self._check(self._lib.mlbm_get_fields(self._h, _dptr(rho), _dptr(u), _dptr(alpha),
                                               _dptr(force), capi.LAYOUT_DENSE))
         return {"rho": rho, "u": u, "alpha": alpha, "force": force}
+
+    def spectral_diagnostics(self, vorticity: bool = True) -> dict:
+        """The reference Routine's spectral analyses of the last stored fields,
+        computed on the device (mlbm_get_spectral_diagnostics): vorticity
+        [2D-3, V], energy, enstrophy and the shell spectrum."""
+        n = ct.c_int()
+        self._check(self._lib.mlbm_spectrum_shells(self._h, ct.byref(n)))
+        w = np.empty((2 * self.D - 3, self.V)) if vorticity else None
+        e, z = ct.c_double(), ct.c_double()
+        spec = np.empty(n.value)
+        self._check(self._lib.mlbm_get_spectral_diagnostics(
+            self._h, _dptr(w) if w is not None else None, ct.byref(e), ct.byref(z),
+            _dptr(spec) if n.value else None, capi.LAYOUT_DENSE))
+        return {"vorticity": w, "energy": e.value, "enstrophy": z.value, "spectrum": spec}
 
     def diagnostics(self) -> dict:
         d = capi.Diag()

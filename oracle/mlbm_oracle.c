@@ -285,14 +285,33 @@ typedef struct {
   const double* fneq; /* f - f_eq */
   const double* w;
   int Q;
+  int perturb; /* oracle_config.log_ulp_perturbation */
 } hfun_t;
+
+/* The reference's log (libm), or with log_ulp_perturbation the libm result
+ * moved by one ulp on about half of the arguments (chosen by a hash of the
+ * argument's bits): a stand-in for another correctly working logarithm, to
+ * measure how far the reference algorithm's result depends on the last bit
+ * of its logarithms. */
+static double ref_log(double x, int perturb) {
+  const double l = log(x);
+  if (!perturb) return l;
+  uint64_t b;
+  memcpy(&b, &x, sizeof b);
+  b ^= b >> 29;
+  b *= 0xbf58476d1ce4e5b9ULL;
+  b ^= b >> 32;
+  if ((b & 3) == 0) return nextafter(l, INFINITY);
+  if ((b & 3) == 1) return nextafter(l, -INFINITY);
+  return l;
+}
 
 static double h_function(const hfun_t* h, double alpha) {
   double r = 0.0;
   for (int q = 0; q < h->Q; ++q) {
     const double f = h->f[q];
     const double g = f - alpha * h->fneq[q];
-    r += f * log(f / h->w[q]) - g * log(g / h->w[q]);
+    r += f * ref_log(f / h->w[q], h->perturb) - g * ref_log(g / h->w[q], h->perturb);
   }
   return r;
 }
@@ -301,7 +320,7 @@ static double h_derivative(const hfun_t* h, double alpha) {
   double r = 0.0;
   for (int q = 0; q < h->Q; ++q) {
     const double g = h->f[q] - alpha * h->fneq[q];
-    r += h->fneq[q] * (1 + log(g / h->w[q]));
+    r += h->fneq[q] * (1 + ref_log(g / h->w[q], h->perturb));
   }
   return r;
 }
@@ -537,7 +556,7 @@ static double entropic_alpha(const oracle_state* s, const double* f, const doubl
     }
   }
   if (alphaMax < 2.) return 0.95 * alphaMax;
-  const hfun_t h = {f, fneq, s->L.w, Q};
+  const hfun_t h = {f, fneq, s->L.w, Q, c->log_ulp_perturbation};
   if (c->guess_mode == ORACLE_GUESS_TWO) guess = 2.0;
   if (c->alpha_mode == ORACLE_ALPHA_RESIDUAL)
     return solve_residual(f, fneq, s->L.w, Q, c->newton_tolerance, c->newton_max_iterations,

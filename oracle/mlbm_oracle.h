@@ -63,6 +63,9 @@ typedef struct {
   double deviation_threshold; /* reference: 1e-3 (Collision.h:357) */
   int threads;                /* host threads sharing the sweep (>=1) */
   int bisection_max_iterations; /* RESIDUAL: cap of the bracketed solver (0: the Newton cap) */
+  /* REFERENCE mode, sensitivity tests only: nonzero moves the libm logarithm
+   * of the entropy function by one ulp on about half of its arguments. */
+  int log_ulp_perturbation;
 } oracle_config;
 
 typedef struct oracle_state oracle_state;

@@ -5,10 +5,11 @@ and the bracketed alpha solver against the reference's own function.
 * D3Q19 BGK FP64, tau 0.55, Guo, Kolmogorov F_x(z) = 1e-6 sin(2 pi 2 z / L)
   (two periods along the contiguous axis), rho0 = 1, u ~ U[-1e-4, 1e-4]
   (seed 1): 500 steps at 64^3 and 5 steps at 256^3, bit-identical.
-* D3Q27 entropic FP64, beta = 0.9995, Taylor-Green U0 = 0.05, the reference
-  alpha solver (Newton to |step| <= 1e-8, alpha = 2 fallback): 2000 steps at
-  64^3 and 3 steps at 256^3, within 1e-12 (max |a - b| / max |b|) in f, rho
-  and u.
+* D3Q27 entropic FP64, beta = 0.9995, Taylor-Green U0 = 0.05: 2000 steps at
+  64^3 and 3 steps at 256^3; with the residual solver at 1e-12 bit-identical
+  to the oracle; with the reference alpha solver (Newton to |step| <= 1e-8,
+  alpha = 2 fallback) within the envelope that a one-ulp change of the
+  logarithm opens in the reference algorithm itself.
 * D3Q27 entropic, FP32 storage, learned alpha guess, residual solver at
   1e-12, Taylor-Green + solenoidal perturbation (1e-3 on 8 <= |k| <= 10,
   seed 2) at 256^3: u within 1e-6 of the FP64 step after 200 steps.
@@ -78,35 +79,73 @@ def taylor_green_entropic(L, **deck_kw):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("L,steps,chunk", [(64, 2000, 250), (256, 3, 3)])
+@pytest.mark.parametrize("L,steps", [(64, 2000), (256, 3)])
+def test_d3q27_entropic_residual_mode_bit_identical(L, steps):
+    """The bracketed solver at |F| <= 1e-12 (Newton from the previous alpha,
+    bisection-Newton fallback, every node solved): the FP64 GPU step equals
+    the oracle bit for bit in f and alpha at the full sizes."""
+    from metalbm_gb300 import Lattice
+    from oracle import ALPHA_RESIDUAL, OracleConfig, OraclePort
+    deck, rho, u = taylor_green_entropic(L, alphaSolver="residual", newtonTolerance=1e-12,
+                                         deviationThreshold=0.0)
+    with Lattice(deck) as lat:
+        lat.init_equilibrium(rho, u)
+        lat.step(steps, store=True, diagnostics=True)
+        f = lat.populations()
+        alpha = lat.fields()["alpha"]
+        d = lat.diagnostics()
+    port = OraclePort(OracleConfig(lattice="D3Q27", collision="ELBM", tau=TAU_ENTROPIC,
+                                   size=(L, L, L), alpha_mode=ALPHA_RESIDUAL,
+                                   newton_tolerance=1e-12, deviation_threshold=0.0,
+                                   threads=threads()))
+    port.init_equilibrium(rho, u)
+    port.step(steps)
+    assert d["fallback_nodes"] == 0 and d["solved_nodes"] == L ** 3
+    assert np.array_equal(alpha, port.fields()["alpha"])
+    assert np.array_equal(f, port.populations())
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("L,steps,chunk", [(64, 2000, 250), (256, 3, 1)])
 def test_d3q27_entropic_reference_mode_matches_oracle(L, steps, chunk):
-    """Reference alpha solver (tolerance 1e-8, 50 iterations, alpha = 2
-    fallback, deviation shortcut 1e-3): CUDA's FP64 log against the host
-    libm's is the only difference. Compared every `chunk` steps."""
+    """The reference alpha solver (Newton to |step| <= 1e-8, 50 iterations,
+    alpha = 2 fallback, deviation shortcut 1e-3; NewtonRaphsonSolver,
+    EntropicStep.h:111-140) returns its iterate once |F/F'| <= 1e-8 without
+    taking that step, so alpha is fixed only to ~1e-8 and which iterate is
+    returned depends on the last bit of the logarithms: the oracle against
+    itself with its libm logarithm moved by one ulp on half of the arguments
+    already differs by ~1e-11 in f after one step (f_neq ~ 1e-3 f), and the
+    flow (Re ~ 4e4) amplifies such differences over the run. The GPU step,
+    whose only difference from the oracle is CUDA's FP64 log against libm's,
+    is held to that envelope at every comparison: within 10x the perturbed
+    oracle's difference (and within 1e-12 where that one is smaller)."""
     from metalbm_gb300 import Lattice
     from oracle import OracleConfig, OraclePort
     deck, rho, u = taylor_green_entropic(L)
-    port = OraclePort(OracleConfig(lattice="D3Q27", collision="ELBM", tau=TAU_ENTROPIC,
-                                   size=(L, L, L), threads=threads()))
-    port.init_equilibrium(rho, u)
-    errs = []
+    ports = [OraclePort(OracleConfig(lattice="D3Q27", collision="ELBM", tau=TAU_ENTROPIC,
+                                     size=(L, L, L), threads=threads(), log_ulp_perturbation=k))
+             for k in (0, 1)]
+    for port in ports:
+        port.init_equilibrium(rho, u)
+    rows = []
     with Lattice(deck) as lat:
         lat.init_equilibrium(rho, u)
         done = 0
         while done < steps:
             n = min(chunk, steps - done)
             lat.step(n, store=True)
-            port.step(n)
+            for port in ports:
+                port.step(n)
             done += n
-            fl, pf = lat.fields(), port.fields()
-            e = {"step": done, "f": rel(lat.populations(), port.populations()),
-                 "rho": rel(fl["rho"], pf["rho"]), "u": rel(fl["u"], pf["u"]),
-                 "alpha": float(np.abs(fl["alpha"] - pf["alpha"]).max())}
-            errs.append(e)
-        d = lat.diagnostics()
-    assert d["fallback_nodes"] >= 0
-    worst = max(max(e["f"], e["rho"], e["u"]) for e in errs)
-    assert worst <= 1e-12, json.dumps(errs)
+            ref, pert = ports[0], ports[1]
+            g, r, q = lat.fields(), ref.fields(), pert.fields()
+            fg, fr, fq = lat.populations(), ref.populations(), pert.populations()
+            rows.append({"step": done,
+                         "gpu": [rel(fg, fr), rel(g["rho"], r["rho"]), rel(g["u"], r["u"])],
+                         "ulp_log": [rel(fq, fr), rel(q["rho"], r["rho"]), rel(q["u"], r["u"])]})
+    for row in rows:
+        for e_gpu, e_pert in zip(row["gpu"], row["ulp_log"]):
+            assert e_gpu <= max(10.0 * e_pert, 1e-12), json.dumps(rows)
 
 
 @pytest.mark.gpu

@@ -21,11 +21,11 @@ F_BOUND = 4e-15  # absolute, 0.4% of the residual tolerance 1e-12 (log1p form)
 
 
 def series_bound(rmax, rho):
-    """The series form's evaluation-error bound (the kernel's
-    series_error_bound): FP32 M3 below rmax = 2.5e-3, FP32 M5 above, the B1
-    logarithms and FP64 rounding."""
+    """The series form's evaluation-error bound for FP32 storage (the kernel's
+    series_error_bound): FP32 M3 below rmax = 2.5e-3, FP32 M5 above, B1 and
+    M2 in double-float arithmetic, FP64 rounding."""
     m = np.where(rmax <= 0.0025, 6.0e-6 * rmax ** 3, 1.2e-5 * rmax ** 5)
-    return rho * (m + 6e-13 * rmax) + 1e-15
+    return rho * (m + 2.0e-13 * rmax + 3.2e-13 * rmax ** 2) + 1e-15
 
 
 def make_nodes(lattice, rmax_targets, seed):

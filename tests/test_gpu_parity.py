@@ -346,8 +346,10 @@ def test_error_word_and_timeout_paths():
                                   "d2q13_bgk_guo_kolmogorov", "d3q33_elbm_none_none"])
 def test_cpp_routine_drop_in(case, tmp_path):
     """The C++ Routine-shaped host loop on include/mlbm/Algorithm_gpu.h
-    (initialize, iterate with isStored on the last step, pack, storeFields in
-    the reference's padded layout) reproduces the reference."""
+    (initialize, iterate with the reference's signature and isStored on the
+    last step, pack, storeFields in the reference's padded layout, then the
+    Routine's analyses) reproduces the reference's state and its vorticity,
+    energy, enstrophy and shell spectrum."""
     import subprocess
     from metalbm_gb300 import build
     g, meta = load(case)
@@ -371,6 +373,15 @@ def test_cpp_routine_drop_in(case, tmp_path):
         assert np.array_equal(f, g["f"]) and np.array_equal(rho, g["rho"])
     else:
         assert rel(f, g["f"]) <= TOL_F64 and rel(rho, g["rho"]) <= TOL_F64
+    # the Routine's analyses of the stored fields through the drop-in
+    an = np.fromfile(str(tmp_path / "out.bin") + ".analysis")
+    DV = g["vorticity"].shape[0]
+    tol = 1e-13 if meta["collision"] == "BGK" else 1e-11
+    assert rel(an[:DV * V].reshape(DV, V), g["vorticity"]) <= tol
+    assert abs(an[DV * V] - float(g["energy"])) <= tol * float(g["energy"])
+    assert abs(an[DV * V + 1] - float(g["enstrophy"])) <= tol * float(g["enstrophy"])
+    K = int(an[DV * V + 2])
+    assert K == g["spectrum"].size and rel(an[DV * V + 3:], g["spectrum"]) <= tol
 
 
 @pytest.mark.gpu

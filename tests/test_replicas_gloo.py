@@ -35,7 +35,8 @@ def test_max_over_ranks_and_job_value_two_ranks():
     assert out[0][2] == pytest.approx(2 * 1000 * 10 / 0.150 / 1e6)
 
 
-@pytest.mark.parametrize("workload", ["bgk_d3q19_f64_256", "turbulent_d3q27_f32_256"])
+@pytest.mark.parametrize("workload", ["bgk_d3q19_f64_256", "turbulent_d3q27_f32_256",
+                                      "entropic_learned_512"])
 def test_reference_arm_prints_the_contract_line(workload):
     """`bench.py --impl reference` (the reference's CPU algorithm, the C
     restatement, on the host cores): one JSON line with the arm's metric,
@@ -45,7 +46,7 @@ def test_reference_arm_prints_the_contract_line(workload):
     import sys
     from conftest import ROOT
     r = subprocess.run([sys.executable, str(ROOT / "bench.py"), "--impl", "reference",
-                        "--workload", workload, "--steps", "1", "--warmup", "3"],
+                        "--workload", workload, "--steps", "1", "--warmup", "3", "--grid", "24"],
                        capture_output=True, text=True, timeout=600, cwd=str(ROOT))
     assert r.returncode == 0, r.stderr[-2000:]
     lines = [l for l in r.stdout.splitlines() if l.startswith("{")]
@@ -55,4 +56,9 @@ def test_reference_arm_prints_the_contract_line(workload):
     assert d["cpu_baseline"]["value"] == d["value"] and d["cpu_baseline"]["kind"] == "port"
     assert d["e2e"] == {"value": d["value"], "unit": "MLUPS", "h2d_bytes_per_step": 0,
                         "d2h_bytes_per_step": 0}
-    assert d["config"]["workload"] == workload
+    assert d["config"]["workload"] == workload and d["config"]["grid"] == [24, 24, 24]
+    # a grid other than the workload's is named as the difference
+    assert d["config"]["same_config"] is False and "grid 24x24x24" in d["config"]["differences"][0]
+    if workload.startswith("entropic"):  # the GPU arm's solver, and one reference-solver step
+        assert "residual" in d["config"]["alpha_solver"]
+        assert d["reference_alpha_solver"]["value"] > 0
