@@ -66,6 +66,14 @@ WORKLOADS = {
                               forceAmplitude=(1e-6, 0.0, 0.0), forceWaveLength=(128.0, 1.0, 1.0),
                               kolmogorovAxis=2, globalLength=(256, 256, 256), storage="f64",
                               bytes_per_node=2 * 19 * 8),
+    # the same with the fixed-point FP64 collision (exact integer moments and
+    # equilibrium on the integer pipe, the update rounded once to FP64)
+    "bgk_d3q19_f64_fixed_256": dict(latticeT="D3Q19", collisionT="BGK", relaxationTime=0.55,
+                                    forcingSchemeT="Guo", forceT="Kolmogorov",
+                                    forceAmplitude=(1e-6, 0.0, 0.0),
+                                    forceWaveLength=(128.0, 1.0, 1.0), kolmogorovAxis=2,
+                                    globalLength=(256, 256, 256), storage="f64",
+                                    fp64Arithmetic="fixed", bytes_per_node=2 * 19 * 8),
     "bgk_d3q19_f32_256": dict(latticeT="D3Q19", collisionT="BGK", relaxationTime=0.55,
                               forcingSchemeT="Guo", forceT="Kolmogorov",
                               forceAmplitude=(1e-6, 0.0, 0.0), forceWaveLength=(128.0, 1.0, 1.0),
@@ -111,6 +119,9 @@ def arithmetic_of(name: str) -> str:
     if w["collisionT"] != "BGK":
         return ("populations stored and updated in FP32; f_neq, B1 and M2 of the entropy "
                 "function in double-float FP32, its evaluation and the alpha solve in FP64")
+    if w.get("fp64Arithmetic") == "fixed":
+        return ("FP64 storage; moments, equilibrium and update in 64-bit fixed point on the "
+                "integer pipe, rounded once to FP64")
     return {"f64": "FP64 (the reference's operation order)",
             "f32": "FP32 storage and collision (deviations from the weights)",
             "f16_shifted": "FP16 storage of (f - w) 2^k, FP32 collision"}[w["storage"]]
@@ -558,7 +569,8 @@ def run_ours(args):
                 "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs, burst copy)"
                 if peak_src == "measured" else "fallback 6.8 TB/s",
                 "bytes_per_node": bpn, "kernel": "elbm_lowp_kernel" if entropic else
-                ("bgk_f64_kernel" if w["storage"] == "f64" else "bgk_lowp_kernel"),
+                (("bgk_f64x_kernel" if w.get("fp64Arithmetic") == "fixed" else "bgk_f64_kernel")
+                 if w["storage"] == "f64" else "bgk_lowp_kernel"),
                 "traffic_source": prof.get("source")}
     if "fp64_inst_per_node" in prof:
         # the kernel's binding roof: GB300's FP64 pipe (no FP64 figure in

@@ -96,6 +96,8 @@ enum {
  * with a per-population power of two k_q (k_q = round(log2(1024 / w_q))).
  * F32 and F16_SHIFTED collide in float, in deviation variables f_q - w_q. */
 enum { MLBM_STORAGE_F64 = 0, MLBM_STORAGE_F32 = 1, MLBM_STORAGE_F16_SHIFTED = 2 };
+/* mlbm_config.fp64_arithmetic */
+enum { MLBM_F64_REFERENCE_ORDER = 0, MLBM_F64_FIXED_POINT = 1 };
 
 /* Entropic alpha solver.
  * REFERENCE: Collision.h:284-375 with NewtonRaphsonSolver (EntropicStep.h:111-140):
@@ -166,7 +168,13 @@ typedef struct {
    * both solvers, Collision.h:336-341, 892-897). With newton_max_iterations = 0
    * every node whose guess fails goes straight to the bracketed solver. */
   int bisection_max_iterations;
-  int reserved[3];
+  /* FP64 storage, BGK: MLBM_F64_REFERENCE_ORDER (the reference's operations
+   * in its order, bit-identical results) or MLBM_F64_FIXED_POINT (the same
+   * update with exact fixed-point moments and equilibrium on the integer
+   * pipe, within a few FP64 ulp a step; D2Q9, D3Q19, D3Q27, D3Q15 with
+   * forcing None, Guo or Shan-Chen, otherwise the reference order). */
+  int fp64_arithmetic;
+  int reserved[2];
 } mlbm_config;
 
 typedef struct {

@@ -27,7 +27,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
           "--expt-relaxed-constexpr",
           "-Xptxas", "-v", f"-I{INCLUDE}", f"-I{CSRC}"]
-PER_FILE = {"step_f64.cu": ["-fmad=false"]}
+PER_FILE = {"step_f64.cu": ["-fmad=false"], "step_f64x.cu": ["-fmad=false"]}
 
 
 def units() -> list[tuple[Path, list[str], str]]:
@@ -38,6 +38,8 @@ def units() -> list[tuple[Path, list[str], str]]:
         extra = PER_FILE.get(src.name, [])
         if src.name == "step_f64.cu":
             out += [(src, extra + [f"-DMLBM_LAT={l}"], f"{src.stem}_L{l}") for l in range(6)]
+        elif src.name == "step_f64x.cu":  # D2Q9, D3Q19, D3Q27, D3Q15
+            out += [(src, extra + [f"-DMLBM_LAT={l}"], f"{src.stem}_L{l}") for l in range(4)]
         elif src.name == "step_lowp.cu":
             out += [(src, extra + [f"-DMLBM_LAT={l}", f"-DMLBM_ST={st}"], f"{src.stem}_L{l}_S{st}")
                     for l in range(4) for st in (1, 2)]  # D2Q9, D3Q19, D3Q27, D3Q15

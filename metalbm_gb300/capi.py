@@ -51,7 +51,7 @@ class Config(ct.Structure):
                 ("device", ct.c_int), ("force_kmin", ct.c_int), ("force_kmax", ct.c_int),
                 ("removal_kmin", ct.c_int), ("removal_kmax", ct.c_int),
                 ("removal_amplitude", ct.c_double * 3), ("bisection_max_iterations", ct.c_int),
-                ("reserved", ct.c_int * 3)]
+                ("fp64_arithmetic", ct.c_int), ("reserved", ct.c_int * 2)]
 
 
 class Diag(ct.Structure):

@@ -374,6 +374,8 @@ extern "C" int mlbm_create(const mlbm_config* cfg, mlbm_handle** out) {
                        c.alpha_guess == MLBM_GUESS_LEARNED_EVERYWHERE;
   if (learned && c.storage == MLBM_STORAGE_F64)
     return fail(nullptr, MLBM_ERR_INVALID, "the learned alpha guess runs with FP32/FP16 storage");
+  if (c.fp64_arithmetic != MLBM_F64_REFERENCE_ORDER && c.fp64_arithmetic != MLBM_F64_FIXED_POINT)
+    return fail(nullptr, MLBM_ERR_INVALID, "bad fp64_arithmetic %d", c.fp64_arithmetic);
   if (c.newton_max_iterations < 0 || c.bisection_max_iterations < 0 || !(c.newton_tolerance >= 0))
     return fail(nullptr, MLBM_ERR_INVALID, "bad Newton parameters");
   const int D = kD[c.lattice];
@@ -576,6 +578,20 @@ extern "C" int mlbm_create(const mlbm_config* cfg, mlbm_handle** out) {
   p.alpha_mode = c.alpha_mode;
   p.guess_mode = c.alpha_guess;
   p.newton_tol = c.newton_tolerance;
+  {
+    // the fixed-point BGK kernel's omega = 2 beta = a + sign m 2^-64 with
+    // |omega - a| <= 1/2 (omega - a is exact), and Guo's factors in 2^62
+    const double om = p.bgk_b;
+    const int a = om < 0.5 ? 0 : (om < 1.5 ? 1 : 2);
+    const double r = om - a;
+    long double m = std::fabs((long double)r) * 18446744073709551616.0L;
+    if (m > 9223372036854775807.0L) m = 9223372036854775807.0L;
+    p.fx_omega_a = a;
+    p.fx_omega_sign = r < 0 ? -1 : 1;
+    p.fx_omega_m = (long long)std::llround(m);
+    for (int q = 0; q < h->Q; ++q)
+      p.fx_guo62[q] = (long long)std::llround((long double)p.guo_k[q] * 4611686018427387904.0L);
+  }
   p.newton_maxit = c.newton_max_iterations;
   p.bisect_maxit = c.bisection_max_iterations > 0 ? c.bisection_max_iterations
                                                   : c.newton_max_iterations;
@@ -723,7 +739,12 @@ static int enqueue_step(mlbm_handle* h, bool last, unsigned int flags, bool in_p
         return fail(h, MLBM_ERR_CUDA, "spectral force: %s", msg);
       h->force_stale = false;
     }
-    cudaError_t e = h->storage == MLBM_STORAGE_F64
+    const bool fixed = h->storage == MLBM_STORAGE_F64 &&
+                       h->cfg.fp64_arithmetic == MLBM_F64_FIXED_POINT &&
+                       f64x_supported(h->cfg.lattice, collision, h->cfg.forcing_scheme);
+    cudaError_t e = fixed ? step_f64x(h->cfg.lattice, h->cfg.forcing_scheme, (const double*)prev,
+                                      (double*)next, p, h->stream)
+                    : h->storage == MLBM_STORAGE_F64
                         ? step_f64(h->cfg.lattice, collision, h->cfg.forcing_scheme,
                                    (const double*)prev, (double*)next, p, h->stream)
                         : step_lowp(h->cfg.lattice, collision, h->cfg.forcing_scheme, h->storage,

@@ -59,6 +59,11 @@ struct StepParams {
   float amp_f[3];
   float bgk_b_f;             // 2 beta
   float guo_kt_f;            // (1 - 1/(2 tau)) 3; S_q = kt w_q [...]
+  // FP64 BGK in fixed point (step_f64x.cu): omega T = a T + sign
+  // mulhi_rn(T, m), and ((1 - 1/(2 tau)) w_q inv_cs2) 2^62
+  long long fx_omega_m;
+  int fx_omega_a, fx_omega_sign;
+  long long fx_guo62[kMaxQ];
   // entropic solver
   int alpha_mode, guess_mode;
   double newton_tol;

@@ -7,6 +7,18 @@
 
 namespace mlbm {
 
+// FP64 storage, BGK collision in fixed point (step_f64x.cu): lattices 0-3,
+// forcing None / Guo / Shan-Chen.
+cudaError_t step_f64x(int lattice, int forcing, const double* prev, double* next,
+                      const StepParams& p, cudaStream_t s);
+inline bool f64x_supported(int lattice, int collision, int forcing) {
+  return collision == 0 && lattice >= 0 && lattice <= 3 && forcing != FS_EDM;
+}
+cudaError_t step_f64x_L0(int forcing, const double* prev, double* next, const StepParams& p, cudaStream_t s);
+cudaError_t step_f64x_L1(int forcing, const double* prev, double* next, const StepParams& p, cudaStream_t s);
+cudaError_t step_f64x_L2(int forcing, const double* prev, double* next, const StepParams& p, cudaStream_t s);
+cudaError_t step_f64x_L3(int forcing, const double* prev, double* next, const StepParams& p, cudaStream_t s);
+
 // FP64 storage, reference arithmetic (step_f64.cu).
 cudaError_t step_f64(int lattice, int collision, int forcing, const double* prev, double* next,
                      const StepParams& p, cudaStream_t s);

@@ -104,6 +104,13 @@ cudaError_t alpha_solve_test(int lattice, const double* f, const double* fneq,
   MLBM_BY_LAT6(lattice, alpha_solve_test, (f, fneq, guess, n, p, alpha, flags, s))
 }
 
+cudaError_t step_f64x(int lattice, int forcing, const double* prev, double* next,
+                      const StepParams& p, cudaStream_t s) {
+  MLBM_BY_LAT4(lattice, step_f64x_L0(forcing, prev, next, p, s),
+               step_f64x_L1(forcing, prev, next, p, s), step_f64x_L2(forcing, prev, next, p, s),
+               step_f64x_L3(forcing, prev, next, p, s))
+}
+
 cudaError_t step_f64(int lattice, int collision, int forcing, const double* prev, double* next,
                      const StepParams& p, cudaStream_t s) {
   MLBM_BY_LAT6(lattice, step_f64, (collision, forcing, prev, next, p, s))

@@ -76,6 +76,9 @@ class InputDeck:
     newtonMaxIterations: int = 50
     # cap of the residual solver's bisection-Newton (0: newtonMaxIterations)
     bisectionMaxIterations: int = 0
+    # FP64 BGK arithmetic: "reference" (the reference's order, bit-identical)
+    # or "fixed" (fixed-point moments and equilibrium on the integer pipe)
+    fp64Arithmetic: str = "reference"
     deviationThreshold: float = 1e-3
     device: int = 0
 
@@ -203,6 +206,7 @@ class InputDeck:
         c.newton_tolerance = float(self.newtonTolerance)
         c.newton_max_iterations = int(self.newtonMaxIterations)
         c.bisection_max_iterations = int(self.bisectionMaxIterations)
+        c.fp64_arithmetic = {"reference": 0, "fixed": 1}[self.fp64Arithmetic]
         c.deviation_threshold = float(self.deviationThreshold)
         c.device = int(self.device)
         return c

@@ -405,3 +405,59 @@ def test_fast_log_accuracy():
     assert (np.abs(out - ref) <= absbound).all(), np.abs(out - ref).max()
     away = np.abs(ref) >= 0.5
     assert (np.abs(out - ref)[away] <= 2 * np.spacing(np.abs(ref[away]))).all()
+
+
+FIXED_LATTICES = ("D2Q9", "D3Q19", "D3Q27", "D3Q15")
+FIXED_CASES = [c for c in CASES if c.split("_")[0].upper() in FIXED_LATTICES and "_bgk_" in c]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", FIXED_CASES)
+def test_f64_fixed_point_matches_reference(case):
+    """The FP64 BGK step with fixed-point moments and equilibrium
+    (fp64Arithmetic="fixed": exact integer sums, the update rounded once to
+    FP64; exact-difference forcing runs in the reference order) against the
+    reference's goldens: within 1e-13 in f, rho, u after the golden's 20
+    steps, the force field unchanged."""
+    from metalbm_gb300 import Lattice
+    g, meta = load(case)
+    with Lattice(deck_for(meta, fp64Arithmetic="fixed")) as lat:
+        lat.init_equilibrium(g["rho0"], g["u0"])
+        lat.step(meta["steps"], store=True, diagnostics=True)
+        f = lat.populations()
+        fl = lat.fields()
+    tol = 1e-13
+    assert rel(f, g["f"]) <= tol, rel(f, g["f"])
+    assert rel(fl["rho"], g["rho"]) <= tol and rel(fl["u"], g["u"]) <= tol
+    if meta["force"] not in SPECTRAL_FORCES:
+        assert np.array_equal(fl["force"], g["force"])
+    if meta["forcing"] == "ExactDifferenceMethod":  # the reference-order kernel
+        assert np.array_equal(f, g["f"])
+
+
+@pytest.mark.gpu
+def test_f64_fixed_point_falls_back_out_of_range():
+    """Nodes outside the fixed-point ranges (here a population above 2 and a
+    node at |u| > 0.1) take the reference-order arithmetic for their warp:
+    the whole step stays within 1e-13 of the oracle, and a state entirely in
+    range differs from the reference order by rounding only."""
+    from metalbm_gb300 import InputDeck, Lattice, fields
+    from oracle import OracleConfig, OraclePort
+    shape = (16, 12, 10)
+    rho, u = fields.perturbed_rest(shape, 3, 0.02, seed=21, rho_amplitude=0.01)
+    u[:, 37] = (0.12, -0.05, 0.02)   # |u| > 0.1
+    port = OraclePort(OracleConfig(lattice="D3Q19", forcing="Guo", force="Kolmogorov", tau=0.6,
+                                   amplitude=(1e-4, 0, 0), wavelength=(6.0, 1, 1), size=shape))
+    port.init_equilibrium(rho, u)
+    f0 = port.populations()
+    f0[0, 500] = 2.5                  # a population above 2
+    port.set_populations(f0)
+    deck = InputDeck(latticeT="D3Q19", forcingSchemeT="Guo", forceT="Kolmogorov",
+                     relaxationTime=0.6, forceAmplitude=(1e-4, 0, 0), forceWaveLength=(6.0, 1, 1),
+                     globalLength=shape, fp64Arithmetic="fixed")
+    with Lattice(deck) as lat:
+        lat.set_populations(f0)
+        lat.step(3, store=True)
+        f = lat.populations()
+    port.step(3)
+    assert rel(f, port.populations()) <= 1e-13
