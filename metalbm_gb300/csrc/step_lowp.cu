@@ -504,6 +504,71 @@ __global__ void __launch_bounds__(256) bgk_f16_pair_kernel(const __half* __restr
   if (p.diag) block_reduce_diag(mass, energy, mach, 2.0, 2.0, p.diag_partials);
 }
 
+// FP16-shifted storage, four z-adjacent nodes a thread (z a multiple of 4,
+// Lz a multiple of 4): every population loads as one aligned 8-byte word of
+// the four source values at z .. z+3 of its source line, plus, when c_z != 0,
+// the one value that falls outside it (z - 1 or z + 4, periodic): 29 loads for
+// four D3Q19 nodes instead of 58 with two nodes a thread. Each pair of nodes
+// is collided and stored as half2, as in bgk_f16_pair_kernel.
+template <int LAT, int FS>
+__global__ void __launch_bounds__(256, 2) bgk_f16_quad_kernel(const __half* __restrict__ prev,
+                                                              __half* __restrict__ next,
+                                                              StepParams p) {
+  using L = Lattice<LAT>;
+  const long long idx = 4 * ((long long)blockIdx.x * blockDim.x + threadIdx.x);
+  const bool active = idx < p.V;
+  double mass = 0.0, energy = 0.0, mach = 0.0;
+  if (active) {
+    uint32_t x, y, z;
+    node_coords(p, idx, x, y, z);  // z a multiple of 4
+    const PullOffsets o = pull_offsets(p, x, y, z);
+    const uint32_t zm = o.oz[2];                          // z - 1, periodic
+    const uint32_t z4 = (z + 4 == p.lz) ? 0 : z + 4;      // z + 4, periodic
+    uint2 raw[L::Q];
+    __half edge[L::Q];
+#pragma unroll
+    for (int q = 0; q < L::Q; ++q) {
+      const __half* src = pop(prev, p.V, q) + o.ox[L::c(q, 0) + 1] + o.oy[L::c(q, 1) + 1];
+      raw[q] = __ldg(reinterpret_cast<const uint2*>(src + z));
+      if (L::c(q, 2) > 0) edge[q] = __ldg(src + zm);
+      if (L::c(q, 2) < 0) edge[q] = __ldg(src + z4);
+    }
+    // node k reads its population q at z + k - c_z: element k - c_z of the
+    // word, or the edge value when that falls outside 0 .. 3
+    auto val = [&](int q, int k) -> float {
+      const int e = k - L::c(q, 2);
+      if (e < 0 || e > 3) return __half2float(edge[q]);
+      const uint32_t w = e < 2 ? raw[q].x : raw[q].y;
+      return __half2float(__ushort_as_half((unsigned short)((e & 1) ? (w >> 16) : (w & 0xffffu))));
+    };
+#pragma unroll
+    for (int kk = 0; kk < 4; kk += 2) {
+      float d0[L::Q], d1[L::Q];
+#pragma unroll
+      for (int q = 0; q < L::Q; ++q) {
+        d0[q] = val(q, kk);
+        d1[q] = val(q, kk + 1);
+      }
+      float rho0, u0[3], rho1, u1[3];
+      bgk_node<LAT, FS, ST_F16>(p, x, y, z + kk, d0, rho0, u0);
+      bgk_node<LAT, FS, ST_F16>(p, x, y, z + kk + 1, d1, rho1, u1);
+#pragma unroll
+      for (int q = 0; q < L::Q; ++q)
+        *reinterpret_cast<__half2*>(pop(next, p.V, q) + (uint32_t)(idx + kk)) =
+            __floats2half2_rn(d0[q], d1[q]);
+      double m0 = 0.0, e0 = 0.0, a0 = 0.0, m1 = 0.0, e1 = 0.0, a1 = 0.0;
+      bgk_node_fields<LAT, FS, ST_F16>(p, idx + kk, x, y, z + kk, rho0, u0, m0, e0, a0);
+      bgk_node_fields<LAT, FS, ST_F16>(p, idx + kk + 1, x, y, z + kk + 1, rho1, u1, m1, e1, a1);
+      if (p.diag) {  // FP64 only on diagnostics steps
+        mass += m0 + m1;
+        energy += e0 + e1;
+        mach = fmax(mach, fmax(a0, a1));
+      }
+    }
+  }
+  if (p.diag) block_reduce_diag(mass, energy, mach, 2.0, 2.0, p.diag_partials);
+}
+
 // ---- Entropic SRT with an FP64 alpha solve --------------------------------
 // The alpha solve needs f_neq with the exact mass and momentum of the stored
 // state, so rho, u, f_eq and f_neq are formed in FP64 from the exact stored
@@ -1489,7 +1554,10 @@ static cudaError_t launch_lowp(int collision, const void* prev, void* next, cons
   using T = typename Storage<ST>::T;
   if (collision == 0) {
     const int bs = 256;
-    if (bgk_pairs(LAT, ST, p.lz)) {
+    if (bgk_quads(LAT, ST, p.lz)) {
+      const unsigned grid = (unsigned)bgk_step_blocks(LAT, ST, p.V, p.lz);
+      bgk_f16_quad_kernel<LAT, FS><<<grid, bs, 0, s>>>((const __half*)prev, (__half*)next, p);
+    } else if (bgk_pairs(LAT, ST, p.lz)) {
       const unsigned grid = (unsigned)bgk_step_blocks(LAT, ST, p.V, p.lz);
       bgk_f16_pair_kernel<LAT, FS><<<grid, bs, 0, s>>>((const __half*)prev, (__half*)next, p);
     } else {

@@ -461,3 +461,30 @@ def test_f64_fixed_point_falls_back_out_of_range():
         f = lat.populations()
     port.step(3)
     assert rel(f, port.populations()) <= 1e-13
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("lattice", ["D3Q19", "D3Q27", "D3Q15"])
+@pytest.mark.parametrize("forcing,force", [("Guo", "Kolmogorov"), ("ExactDifferenceMethod", "Sinusoidal")])
+def test_f16_four_nodes_a_thread_tracks_f64(lattice, forcing, force):
+    """FP16-shifted storage on a lattice whose Lz is a multiple of 4 (the
+    four-nodes-a-thread kernel, with the periodic edge values of the z lines)
+    against the FP64 kernel, to the storage tolerance of the two-node kernel."""
+    from metalbm_gb300 import InputDeck, Lattice, fields
+    shape = (10, 6, 16)
+    rho, u = fields.perturbed_rest(shape, 3, 0.02, seed=8, rho_amplitude=0.005)
+    out = {}
+    for st in ("f64", "f16_shifted"):
+        with Lattice(InputDeck(latticeT=lattice, forcingSchemeT=forcing, forceT=force,
+                               relaxationTime=0.6, forceAmplitude=(1e-4, -5e-5, 2e-5),
+                               forceWaveLength=(5.0, 6.0, 8.0), kolmogorovAxis=2,
+                               globalLength=shape, storage=st)) as lat:
+            lat.init_equilibrium(rho, u)
+            lat.step(20, store=True, diagnostics=True)
+            out[st] = lat.fields()
+            out[st + "_d"] = lat.diagnostics()
+    assert rel(out["f16_shifted"]["u"], out["f64"]["u"]) <= 5e-3
+    assert rel(out["f16_shifted"]["rho"], out["f64"]["rho"]) <= 5e-5
+    d16, d64 = out["f16_shifted_d"], out["f64_d"]
+    assert abs(d16["energy"] - d64["energy"]) <= 2e-2 * d64["energy"]
+    assert abs(d16["mass"] - d64["mass"]) <= 1e-6 * d64["mass"]
