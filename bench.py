@@ -590,6 +590,14 @@ def run_ours(args):
     e2e = run_e2e(name, deck_l, rho, u, model if entropic else None, args.steps, args.warmup, torch,
                   dist, world)
 
+    # the BGK kernels of the other workloads, device-timed in the same run
+    # (their own lines come from --workload NAME)
+    others = {}
+    if name == "entropic_learned_512" and not args.grid and not args.no_others:
+        for oname in ("bgk_d3q19_f64_256", "bgk_d3q19_f64_fixed_256", "bgk_d3q19_f32_256",
+                      "bgk_d3q19_f16_256"):
+            others[oname] = quick_workload(oname, local, torch, dist, world, peaks)
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         # the reference arm's sample: its grid, initial field and alpha solver
@@ -615,9 +623,32 @@ def run_ours(args):
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
             "clocks": clk.summary(), **extra,
         }
+        if others:
+            line["other_workloads"] = others
         print(json.dumps(line), flush=True)
     if dist is not None:
         dist.destroy_process_group()
+
+
+def quick_workload(name, local, torch, dist, world, peaks, steps=10, warmup=3):
+    """A BGK workload device-timed as in its own run (warm-up, then `steps`
+    steps of one mlbm_step call between CUDA events), for the default line."""
+    from metalbm_gb300 import Lattice
+    w = WORKLOADS[name]
+    deck = deck_for(name, device=local)
+    V = int(np.prod(deck.shape))
+    rho, u = initial_field(name, deck.shape)
+    with Lattice(deck) as lat:
+        lat.init_equilibrium(rho, u)
+        lat.step(warmup)
+        ms, _ = time_steps(lat, steps, torch, dist)
+    ms = max_over_ranks(ms, dist, f"cuda:{local}")
+    value = job_value(V, steps, world, ms)
+    gbs = w["bytes_per_node"] * V * steps / (ms * 1e-3) / 1e9  # one GPU's lattice
+    return {"value": value, "unit": "MLUPS", "ms_per_step": ms / steps, "steps": steps,
+            "warmup": warmup, "arithmetic": arithmetic_of(name),
+            "hbm": {"achieved": gbs, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                    "frac": gbs / peaks["hbm_gbs"], "bytes_per_node": w["bytes_per_node"]}}
 
 
 def run_e2e(name, deck, rho, u, model, steps, warmup, torch, dist, world):
@@ -746,6 +777,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="entropic_learned_512", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
+    ap.add_argument("--no-others", action="store_true",
+                    help="skip the other workloads' device timings in the default line")
     ap.add_argument("--grid", type=int, default=0,
                     help="cubic grid side overriding the workload's (profiling captures of a "
                          "smaller case; not a bench configuration)")

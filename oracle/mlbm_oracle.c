@@ -306,6 +306,23 @@ static double ref_log(double x, int perturb) {
   return l;
 }
 
+/* With population_ulp_perturbation: a BGK result moved by one ulp, up or
+ * down, on about half of the stores (chosen by a hash of its bits and its
+ * index): a stand-in for another FP64 evaluation of the same update with a
+ * different rounding, to measure how far the state over many steps depends on
+ * the last bit of each population. */
+static double ulp_nudge(double r, uint64_t key) {
+  uint64_t b;
+  memcpy(&b, &r, sizeof b);
+  b ^= key * 0x9e3779b97f4a7c15ULL;
+  b ^= b >> 31;
+  b *= 0xbf58476d1ce4e5b9ULL;
+  b ^= b >> 29;
+  if ((b & 3) == 0) return nextafter(r, INFINITY);
+  if ((b & 3) == 1) return nextafter(r, -INFINITY);
+  return r;
+}
+
 static double h_function(const hfun_t* h, double alpha) {
   double r = 0.0;
   for (int q = 0; q < h->Q; ++q) {
@@ -614,7 +631,9 @@ static void node_update(oracle_state* s, unsigned x, unsigned y, unsigned z, int
     const double a = 1. - 2. * s->beta, b = 2. * s->beta;
     for (int q = 0; q < Q; ++q) {
       const double eq = equilibrium(L, rho, u, u2, q);
-      nxt[(long)q * V + idx] = a * f[q] + b * eq + collision_source(s, F, rho, u, eq, q);
+      double r = a * f[q] + b * eq + collision_source(s, F, rho, u, eq, q);
+      if (c->population_ulp_perturbation) r = ulp_nudge(r, (uint64_t)q * (uint64_t)V + (uint64_t)idx);
+      nxt[(long)q * V + idx] = r;
     }
   } else {
     /* Collision<ELBM>::calculateRelaxationTime (Collision.h:227-241) and

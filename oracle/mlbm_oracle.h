@@ -66,6 +66,9 @@ typedef struct {
   /* REFERENCE mode, sensitivity tests only: nonzero moves the libm logarithm
    * of the entropy function by one ulp on about half of its arguments. */
   int log_ulp_perturbation;
+  /* BGK, sensitivity tests only: nonzero moves each new population by one
+   * ulp, up or down, on about half of the stores. */
+  int population_ulp_perturbation;
 } oracle_config;
 
 typedef struct oracle_state oracle_state;

@@ -39,7 +39,8 @@ class _Cfg(ct.Structure):
                 ("lz", ct.c_int), ("alpha_mode", ct.c_int), ("guess_mode", ct.c_int),
                 ("newton_tolerance", ct.c_double), ("newton_max_iterations", ct.c_int),
                 ("deviation_threshold", ct.c_double), ("threads", ct.c_int),
-                ("bisection_max_iterations", ct.c_int), ("log_ulp_perturbation", ct.c_int)]
+                ("bisection_max_iterations", ct.c_int), ("log_ulp_perturbation", ct.c_int),
+                ("population_ulp_perturbation", ct.c_int)]
 
 
 def build_port(force: bool = False) -> Path:
@@ -122,6 +123,7 @@ class OracleConfig:
     threads: int = 1
     bisection_max_iterations: int = 0  # 0: the Newton cap
     log_ulp_perturbation: int = 0  # sensitivity tests: libm log moved by one ulp
+    population_ulp_perturbation: int = 0  # sensitivity tests: BGK results moved by one ulp
 
 
 class OraclePort:
@@ -141,7 +143,7 @@ class OraclePort:
                  cfg.kolmogorov_component, lx, ly, lz, cfg.alpha_mode, cfg.guess_mode,
                  cfg.newton_tolerance, cfg.newton_max_iterations, cfg.deviation_threshold,
                  max(1, cfg.threads), int(cfg.bisection_max_iterations),
-                 int(cfg.log_ulp_perturbation))
+                 int(cfg.log_ulp_perturbation), int(cfg.population_ulp_perturbation))
         self._lib = _load()
         self._h = self._lib.oracle_create(ct.byref(c))
         if not self._h:

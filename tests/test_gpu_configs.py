@@ -54,8 +54,14 @@ def d3q19_kolmogorov(L):
 @pytest.mark.parametrize("L,steps", [(64, 500), (256, 5)])
 def test_d3q19_bgk_f64_fixed_point_matches_oracle(L, steps):
     """The same configuration with the fixed-point FP64 collision (exact
-    integer moments and equilibrium, the update rounded once to FP64):
-    within 1e-12 (max |a - b| / max |b|) of the oracle in f, rho and u."""
+    integer moments and equilibrium, the update rounded once to FP64): f and
+    rho within 1e-12 (max |a - b| / max |b|) of the oracle. The velocity,
+    |u| ~ 1e-4 out of momenta summed from populations ~ 0.05, carries the
+    cancellation of that sum: its bound is 10x the difference that moving
+    half of the oracle's own BGK results by one ulp makes over the same run
+    (1.7e-11 at 64^3 x 500, 3.0e-12 at 256^3 x 5), and never below 1e-12."""
+    import dataclasses
+
     from metalbm_gb300 import Lattice
     from oracle import OraclePort
     deck, pcfg, rho, u = d3q19_kolmogorov(L)
@@ -70,7 +76,13 @@ def test_d3q19_bgk_f64_fixed_point_matches_oracle(L, steps):
     port.step(steps)
     pf = port.fields()
     assert rel(f, port.populations()) <= 1e-12
-    assert rel(fl["rho"], pf["rho"]) <= 1e-12 and rel(fl["u"], pf["u"]) <= 1e-12
+    assert rel(fl["rho"], pf["rho"]) <= 1e-12
+    nudged = OraclePort(dataclasses.replace(pcfg, population_ulp_perturbation=1))
+    nudged.init_equilibrium(rho, u)
+    nudged.step(steps)
+    envelope = rel(nudged.fields()["u"], pf["u"])
+    assert 0.0 < envelope < 1e-9
+    assert rel(fl["u"], pf["u"]) <= max(1e-12, 10.0 * envelope)
 
 
 @pytest.mark.gpu

@@ -149,7 +149,7 @@ def test_reference_2d_curl_keeps_real_part_only():
     kx = np.where(np.arange(16) <= 8, np.arange(16), np.arange(16) - 16)[:, None]
     ky = np.arange(7)[None, :]
     re = (1j * (kx * uh[1] - ky * uh[0])).real
-    expect = np.fft.irfftn(re + 0j, s=(16, 12)).ravel() / (16 * 12)
+    expect = np.fft.irfftn(re + 0j, s=(16, 12), axes=(0, 1)).ravel() / (16 * 12)
     assert np.abs(w[0] - expect).max() < 1e-14
 
 
