@@ -581,6 +581,8 @@ def run_ours(args):
                                  "unit": "G FP64 instr/s", "frac": gops / prof["fp64_peak_gops"],
                                  "instructions_per_node": prof["fp64_inst_per_node"],
                                  "peak_source": "measured DFMA throughput (profiles/fp64_throughput_gb300.md)"}
+    if "limiter" in prof:
+        roofline["limiter"] = prof["limiter"]
     if "fp64_pipe_busy_pct" in prof:
         # ncu's FP64-pipe occupancy also counts the compares, conversions
         # and reciprocal seeds that run on the pipe besides the arithmetic

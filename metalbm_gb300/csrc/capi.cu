@@ -579,18 +579,25 @@ extern "C" int mlbm_create(const mlbm_config* cfg, mlbm_handle** out) {
   p.guess_mode = c.alpha_guess;
   p.newton_tol = c.newton_tolerance;
   {
-    // the fixed-point BGK kernel's omega = 2 beta = a + sign m 2^-64 with
-    // |omega - a| <= 1/2 (omega - a is exact), and Guo's factors in 2^62
+    // the fixed-point BGK kernel's omega = 2 beta = a + (omega - a), a the
+    // integer nearest omega in {0, 1, 2}, and Guo's factors: values times
+    // 2^62 (exact: products of doubles and a power of two) as 31-bit halves
     const double om = p.bgk_b;
     const int a = om < 0.5 ? 0 : (om < 1.5 ? 1 : 2);
     const double r = om - a;
-    long double m = std::fabs((long double)r) * 18446744073709551616.0L;
-    if (m > 9223372036854775807.0L) m = 9223372036854775807.0L;
+    p.fx_ok = std::fabs(r) <= 0.5 ? 1 : 0;
     p.fx_omega_a = a;
-    p.fx_omega_sign = r < 0 ? -1 : 1;
-    p.fx_omega_m = (long long)std::llround(m);
-    for (int q = 0; q < h->Q; ++q)
-      p.fx_guo62[q] = (long long)std::llround((long double)p.guo_k[q] * 4611686018427387904.0L);
+    auto halves = [](double v, int out[2]) {
+      const long long x = std::llround(std::ldexp(v, 62));
+      out[0] = (int)(x >> 31);
+      out[1] = (int)(x & 0x7fffffffLL);
+    };
+    halves(p.fx_ok ? r : 0.0, p.fx_omega_s31);
+    for (int q = 0; q < h->Q; ++q) {
+      const bool in = std::fabs(p.guo_k[q]) < 1.0;
+      if (!in && c.forcing_scheme == MLBM_FORCING_GUO) p.fx_ok = 0;
+      halves(in ? p.guo_k[q] : 0.0, p.fx_guo_s31[q]);
+    }
   }
   p.newton_maxit = c.newton_max_iterations;
   p.bisect_maxit = c.bisection_max_iterations > 0 ? c.bisection_max_iterations
@@ -740,7 +747,7 @@ static int enqueue_step(mlbm_handle* h, bool last, unsigned int flags, bool in_p
       h->force_stale = false;
     }
     const bool fixed = h->storage == MLBM_STORAGE_F64 &&
-                       h->cfg.fp64_arithmetic == MLBM_F64_FIXED_POINT &&
+                       h->cfg.fp64_arithmetic == MLBM_F64_FIXED_POINT && p.fx_ok &&
                        f64x_supported(h->cfg.lattice, collision, h->cfg.forcing_scheme);
     cudaError_t e = fixed ? step_f64x(h->cfg.lattice, h->cfg.forcing_scheme, (const double*)prev,
                                       (double*)next, p, h->stream)

@@ -59,11 +59,14 @@ struct StepParams {
   float amp_f[3];
   float bgk_b_f;             // 2 beta
   float guo_kt_f;            // (1 - 1/(2 tau)) 3; S_q = kt w_q [...]
-  // FP64 BGK in fixed point (step_f64x.cu): omega T = a T + sign
-  // mulhi_rn(T, m), and ((1 - 1/(2 tau)) w_q inv_cs2) 2^62
-  long long fx_omega_m;
-  int fx_omega_a, fx_omega_sign;
-  long long fx_guo62[kMaxQ];
+  // FP64 BGK in fixed point (step_f64x.cu): omega = a + (omega - a) with
+  // (omega - a) 2^62 as 31-bit halves (high, low), and
+  // ((1 - 1/(2 tau)) w_q inv_cs2) 2^62 likewise; fx_ok = 0 when
+  // |omega - a| > 1/2 or a Guo factor is not below 1 (the kernel's ranges)
+  int fx_ok;
+  int fx_omega_a;
+  int fx_omega_s31[2];
+  int fx_guo_s31[kMaxQ][2];
   // entropic solver
   int alpha_mode, guess_mode;
   double newton_tol;

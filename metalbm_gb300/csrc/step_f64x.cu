@@ -5,33 +5,39 @@
 // operations a node) is bound by that pipe at a few percent of HBM. This
 // kernel keeps the FP64 populations in HBM and computes the same update,
 //   f'_q = f_q + omega (f_eq_q - f_q) + S_q   (Collision.h:134-151, omega = 2 beta),
-// in 64-bit fixed point on the integer pipe:
-//   * F_q = f_q 2^60 (exact for f_q >= 2^-8, rounded below), D_q = F_q - W_q
-//     with W_q = w_q 2^60, the reference's double weights exactly;
+// in 64-bit fixed point:
+//   * F_q = f_q 2^60 from the double's bits (exact for f_q >= 2^-8, rounded
+//     below);
 //   * rho and j = sum_q c_q f_q as exact integer sums (Moment.h:13-47);
-//   * 1/rho by two Newton steps in 2^62 fixed point, u = j/rho in 2^64
-//     fixed point;
-//   * f_eq_q - f_q = [w_q rho - f_q + 3 w_q c_q.j] + w_q rho R_q, the linear
-//     part of Equilibrium<TruncationMa3> (Equilibrium.h:17-33) exact from j,
+//   * 1/rho by two Newton steps in 2^61 fixed point from an FP32 seed,
+//     u = j / rho in 2^62 fixed point;
+//   * f_eq_q - f_q = w_q rho (1 + 3 s + R_q) - f_q with s = c_q.u and
 //     R_q = 4.5 s^2 - 1.5 u^2 + 4.5 s^3 - 4.5 s u^2 + 1.125 u^4 - 6.75 s^2 u^2
-//     + 3.375 s^4 (s = c_q.u) in 2^64 fixed point, the pair (q, -q) sharing
-//     its even and odd parts;
+//     + 3.375 s^4, Equilibrium<TruncationMa3> (Equilibrium.h:17-33), in 2^62
+//     fixed point, w_q rho from the reference's double weights exactly, the
+//     pair (q, -q) sharing the even and odd parts of 3 s + R_q;
 //   * Guo's source ((1 - 1/(2 tau)) w_q 3) [(c_q - u).F + 3 (c_q.u)(c_q.F)]
-//     (ForcingScheme.h:81-118) in fixed point;
-//   * f'_q rounded once to FP64, to nearest even.
-// Each fixed-point product carries at most 2^-64 relative to O(1) or one unit
-// of 2^-60 absolute, so a population's update is within a few 2^-60 of the
-// exact value of the reference's formula: within a few FP64 ulp of the
-// reference's own result for populations above 2^-6 (the tests hold it to
-// 1e-12 relative over hundreds of steps).
+//     (ForcingScheme.h:81-118);
+//   * f'_q 2^62 = 4 F_q + a T_q + (omega - a) T_q + S_q (T_q = f_eq_q - f_q,
+//     a the integer nearest omega), rounded once to FP64, to nearest even.
+// Every product is of two values below 2^62 in magnitude held as 31-bit
+// halves, (a_h 2^31 + a_l)(b_h 2^31 + b_l) 2^-62 = a_h b_h + (a_h b_l + a_l b_h)
+// 2^-31 with the product of the low halves dropped: three 32 x 32 -> 64-bit
+// integer multiply-adds, within one unit of 2^-62 of the exact product (GB300
+// emulates a 64 x 64-bit high product in several times as many
+// instructions). A population's update is then within a few units of 2^-62 of
+// the exact value of the reference's formula, about one FP64 ulp of the
+// smallest populations (the tests hold the state to 1e-12 relative over
+// hundreds of steps).
 //
-// Nodes outside the fixed-point ranges (a population outside [0, 2),
-// |f_q - w_q| >= 1/4, rho outside (0.53, 2), |u| >= 0.1, |F_d| >= 1/8, or a
-// non-finite value) take the reference-order arithmetic of ref_node.cuh: a
+// Nodes outside the fixed-point ranges (a population outside [0, 1/2) for
+// Q > 15, [0, 1) for D2Q9 and D3Q15, so that the unsigned sum of the F_q stays
+// below 2^64; rho outside (0.53, 2); |j| >= 1/4; |u| >= 0.1; |F_d| >= 1/8; a new
+// population outside [2^-30, 1); or a non-finite value) take the reference-order arithmetic of ref_node.cuh: a
 // warp with such a node computes all its nodes that way (bit-identical to the
-// reference for them). Lattices D2Q9, D3Q19, D3Q27, D3Q15 (reach 1,
-// inv_cs2 = 3); forcing None, Guo, Shan-Chen (EDM uses the reference-order
-// kernel).
+// reference for them), rewriting whatever the fixed-point pass stored.
+// Lattices D2Q9, D3Q19, D3Q27, D3Q15 (reach 1, inv_cs2 = 3); forcing None,
+// Guo, Shan-Chen (EDM uses the reference-order kernel).
 //
 // This unit is compiled with -fmad=false for the reference-order fallback.
 
@@ -44,45 +50,60 @@ namespace fx {
 
 // ---- 64-bit fixed-point helpers ---------------------------------------------
 
-// high 64 bits of the signed 128-bit product (floor)
-__device__ __forceinline__ long long mulhi(long long a, long long b) { return __mul64hi(a, b); }
-
-// (a b + 2^63) >> 64: the product's high part rounded to nearest
-__device__ __forceinline__ long long mulhi_rn(long long a, long long b) {
-  const unsigned long long lo = (unsigned long long)a * (unsigned long long)b;
-  return __mul64hi(a, b) + (long long)(lo >> 63);
+// x = h 2^31 + l with 0 <= l < 2^31, for |x| < 2^62
+struct S31 {
+  int h, l;
+};
+__device__ __forceinline__ S31 split(long long x) {
+  return S31{(int)(x >> 31), (int)((unsigned)x & 0x7fffffffu)};
+}
+__host__ __device__ constexpr S31 csplit(long long x) {
+  return S31{(int)(x >> 31), (int)(x & 0x7fffffffLL)};
 }
 
-// (a b) >> k for 0 < k < 64, from the signed 128-bit product (floor)
-__device__ __forceinline__ long long mulshr(long long a, long long b, int k) {
-  const unsigned long long lo = (unsigned long long)a * (unsigned long long)b;
-  const long long hi = __mul64hi(a, b);
-  return (long long)(((unsigned long long)hi << (64 - k)) | (lo >> k));
+// a b 2^-62 within one unit (|error| < 1): the low halves' product dropped,
+// the middle terms' sum rounded
+__device__ __forceinline__ long long mul62(S31 a, S31 b) {
+  const long long mid = (long long)a.h * b.l + ((long long)a.l * b.h + (1LL << 30));
+  return (long long)a.h * b.h + (mid >> 31);
+}
+// a b 2^-60 within one unit
+__device__ __forceinline__ long long mul60(S31 a, S31 b) {
+  const long long mid = (long long)a.h * b.l + ((long long)a.l * b.h + (1LL << 28));
+  return ((long long)a.h * b.h << 2) + (mid >> 29);
 }
 
-// v 2^S rounded to nearest for a double v; `bad` when v is not finite or
-// |v| 2^S >= 2^62.
+// x >> s for any s (PTX clamps shift amounts above 64: 0)
+__device__ __forceinline__ unsigned long long shr_u64(unsigned long long x, unsigned s) {
+  unsigned long long r;
+  asm("shr.b64 %0, %1, %2;" : "=l"(r) : "l"(x), "r"(s));
+  return r;
+}
+
+// |v| 2^S rounded to nearest (ties away) from the double's bits b, for
+// |v| 2^S < 2^62 (the caller checks the exponent range); zero and
+// subnormals give 0.
 template <int S>
-__device__ __forceinline__ long long to_fixed(double v, bool& bad) {
-  const long long b = __double_as_longlong(v);
-  const int e = (int)((b >> 52) & 0x7ff);
-  const long long m = (b & 0x000fffffffffffffLL) | 0x0010000000000000LL;  // |v| = m 2^(e - 1075)
-  const int sh = e - 1075 + S;                                             // |v| 2^S = m 2^sh
-  long long a;
-  if (sh >= 0) {
-    bad |= sh > 8;  // m < 2^53: m 2^8 < 2^61
-    a = m << (sh & 15);
-  } else if (sh > -62) {
-    a = (m + (1LL << (-sh - 1))) >> (-sh);
-  } else {
-    a = 0;
-  }
-  if (e == 0) a = 0;  // zero and subnormals
-  bad |= e == 0x7ff;
-  return b < 0 ? -a : a;
+__device__ __forceinline__ unsigned long long abs_to_fixed(unsigned long long b) {
+  const unsigned e = (unsigned)(b >> 52) & 0x7ffu;
+  const unsigned long long t = (b << 11) | 0x8000000000000000ULL;  // 1.m 2^63
+  // |v| 2^S = t 2^(e - 1086 + S)
+  return (shr_u64(t, 1085u - S - e) + 1ULL) >> 1;
 }
 
-// v 2^-S rounded to the nearest double (ties to even), |v| < 2^63.
+// X 2^-62 rounded to the nearest double (ties to even) for X in [2^32, 2^62);
+// `bad` otherwise.
+__device__ __forceinline__ double fixed62_to_double(long long X, bool& bad) {
+  const unsigned hi = (unsigned)((unsigned long long)X >> 32);
+  bad |= hi - 1u >= 0x3fffffffu;
+  const int lz = __clz((int)hi);                                  // 2..31
+  const unsigned long long m = (unsigned long long)X << ((lz - 1) & 31);  // 1.x 2^62
+  const unsigned long long r = m + 0x1ffULL + ((m >> 10) & 1ULL);
+  return __longlong_as_double((long long)((r >> 10) + ((unsigned long long)(1023 - lz) << 52)));
+}
+
+// v 2^-S rounded to the nearest double (ties to even), any |v| < 2^63 (the
+// stored fields and diagnostics).
 template <int S>
 __device__ __forceinline__ double to_double(long long v) {
   if (v == 0) return 0.0;
@@ -106,34 +127,23 @@ __device__ __forceinline__ double to_double(long long v) {
 template <int LAT>
 struct FxConst {
   using L = Lattice<LAT>;
-  // w_q 2^60 (exact: the double weight times a power of two is an integer)
-  static constexpr long long W60(int q) { return (long long)(L::w(q) * 1152921504606846976.0); }
-  // w_q 2^64 (< 2^63 for w_q < 1/2)
-  static constexpr long long W64(int q) { return (long long)(L::w(q) * 18446744073709551616.0); }
-  // 3 w_q 2^64 (moving populations: 3 w_q < 1/2)
-  static constexpr long long W3_64(int q) {
-    return (long long)(3.0 * L::w(q) * 18446744073709551616.0);
-  }
-  static constexpr long long sumW() {
-    long long s = 0;
-    for (int q = 0; q < L::Q; ++q) s += W60(q);
-    return s;
-  }
-  // w_q sum_q' W_q' - W_q = w_q (sum W - 2^60): the rounding of the weights'
-  // sum spread over the populations (a few units of 2^-60)
-  static constexpr long long C(int q) {
-    const double t = L::w(q) * (double)(sumW() - 1152921504606846976LL);
-    return (long long)(t >= 0 ? t + 0.5 : t - 0.5);
-  }
+  // w_q 2^63 (exact: the double weight times a power of two is an integer;
+  // < 2^62 for w_q < 1/2)
+  static constexpr long long W63(int q) { return (long long)(L::w(q) * 9223372036854775808.0); }
+  // populations below 2^-1 (Q > 15) or 2^0: the high word's bound, and the
+  // new populations' bound in 2^62 fixed point
+  static constexpr unsigned kFmaxHi = L::Q > 15 ? 0x3fe00000u : 0x3ff00000u;
 };
 
-// The reference's BGK coefficients as fixed-point multipliers: omega T =
-// a T + sign mulhi_rn(T, m) with m < 2^63 (StepParams fx_omega_*), and
-// Guo's ((1 - 1/(2 tau)) w_q inv_cs2) in 2^62 fixed point (fx_guo62).
+// The reference's BGK coefficients in fixed point: omega T = a T + mul62(T,
+// omega - a) (StepParams fx_omega_a, fx_omega_s31), and Guo's
+// ((1 - 1/(2 tau)) w_q inv_cs2) 2^62 (fx_guo_s31), split on the host.
 
 // One node in fixed point. Returns false, for every lane of the warp, when a
-// lane of the warp is outside the fixed-point ranges (nothing is stored then);
-// every lane of the warp must call it (inactive lanes with f = w).
+// lane of the warp is outside the fixed-point ranges; every lane of the warp
+// must call it (inactive lanes with f = w). On false the caller recomputes the
+// warp's nodes in the reference order (populations this pass stored are
+// rewritten).
 template <int LAT, int FS>
 __device__ __forceinline__ bool bgk_node_fixed(const double f[], const double F[3],
                                                const StepParams& p, long long idx, bool active,
@@ -143,132 +153,137 @@ __device__ __forceinline__ bool bgk_node_fixed(const double f[], const double F[
   using L = Lattice<LAT>;
   using K = FxConst<LAT>;
   constexpr int Q = L::Q;
-  // populations as deviations from the weights, 2^60 fixed point
-  long long Dq[Q];
-  long long drho = 0, j[3] = {0, 0, 0};
+  // populations in 2^60 fixed point, their exact sums
+  unsigned long long Fq[Q];
+  unsigned long long rhoF = 0;
+  long long j[3] = {0, 0, 0};
 #pragma unroll
   for (int q = 0; q < Q; ++q) {
-    const long long Fq = to_fixed<60>(f[q], bad);
-    bad |= Fq < 0;
-    Dq[q] = Fq - K::W60(q);
-    const long long ad = Dq[q] < 0 ? -Dq[q] : Dq[q];
-    bad |= ad >= (1LL << 58);
-    drho += Dq[q];
+    const unsigned long long b = (unsigned long long)__double_as_longlong(f[q]);
+    bad |= (unsigned)(b >> 32) >= K::kFmaxHi;  // negative, too large, inf, NaN
+    Fq[q] = abs_to_fixed<60>(b);
+    rhoF += Fq[q];
 #pragma unroll
     for (int d = 0; d < L::D; ++d) {
-      if (L::c(q, d) > 0) j[d] += Dq[q];
-      if (L::c(q, d) < 0) j[d] -= Dq[q];
+      if (L::c(q, d) > 0) j[d] += (long long)Fq[q];
+      if (L::c(q, d) < 0) j[d] -= (long long)Fq[q];
     }
   }
-  const long long rhoF = K::sumW() + drho;  // rho 2^60
-  bad |= rhoF <= (1LL << 59) + (1LL << 55) || rhoF >= (1LL << 61);
+  constexpr unsigned long long kRhoLo = (1ULL << 59) + (1ULL << 55);  // rho > 0.53
+  bad |= rhoF - kRhoLo >= (1ULL << 61) - kRhoLo;                      // rho < 2
 #pragma unroll
-  for (int d = 0; d < L::D; ++d) bad |= (j[d] < 0 ? -j[d] : j[d]) >= (1LL << 58);  // |u| < 1/2
-  // forces, 2^64 fixed point
+  for (int d = 0; d < L::D; ++d)
+    bad |= (unsigned long long)(j[d] + (1LL << 58)) >= (1ULL << 59);  // |j| < 1/4
+  // forces, 2^62 fixed point
   long long Fx[3] = {0, 0, 0};
   if (FS == FS_GUO) {
 #pragma unroll
     for (int d = 0; d < L::D; ++d) {
-      Fx[d] = to_fixed<64>(F[d], bad);
-      const long long a = Fx[d] < 0 ? -Fx[d] : Fx[d];
-      bad |= a >= (1LL << 62);
+      const unsigned long long b = (unsigned long long)__double_as_longlong(F[d]);
+      bad |= ((unsigned)(b >> 32) & 0x7fffffffu) >= 0x3fc00000u;  // |F| < 1/8, finite
+      const long long a = (long long)abs_to_fixed<62>(b);
+      Fx[d] = (long long)b < 0 ? -a : a;
     }
   }
   if (__any_sync(0xffffffffu, bad)) return false;  // the warp takes the reference arithmetic
 
-  // 1/rho in 2^62: float seed (2^-22), two Newton steps in fixed point
+  // 1/rho in 2^61: FP32 seed (~2^-21), two Newton steps
+  const S31 rho61 = split((long long)(rhoF << 1));
   long long R;
   {
-    const float r = (float)(rhoF >> 37) * 0x1p-23f;  // rho to ~2^-22 (rhoF >> 37 < 2^24)
-    const float y = __frcp_rn(r);
-    R = (long long)__float2int_rn(y * 0x1p30f) << 32;  // y 2^62
+    const unsigned x = (unsigned)(rhoF >> 38);  // rho 2^22, < 2^23
+    const float rf = __uint_as_float(0x4b000000u | x) - 8388608.0f;
+    const float y = __frcp_rn(rf);              // 2^-22 / rho
+    R = (long long)__float2uint_rn(y * 0x1p53f) << 30;
 #pragma unroll
     for (int it = 0; it < 2; ++it) {
-      // e = (1 - rho R) 2^62 = (2^122 - rhoF R) >> 60
-      const unsigned long long lo = (unsigned long long)rhoF * (unsigned long long)R;
-      const long long hi = __mul64hi(rhoF, R);
-      const long long hd = (1LL << 58) - hi - (lo != 0ULL ? 1 : 0);
-      const unsigned long long ld = 0ULL - lo;
-      const long long e = (long long)(((unsigned long long)hd << 4) | (ld >> 60));
-      R += mulshr(R, e, 62);
+      const S31 Rs = split(R);
+      const long long e = (1LL << 62) - mul60(rho61, Rs);  // (1 - rho R) 2^62
+      R += mul62(Rs, split(e));
     }
   }
-  // u = j / rho in 2^64 fixed point: (j 2^60)(R 2^62) >> 58
+  // u = j / rho in 2^62 fixed point
+  const S31 Rs = split(R);
   long long u[3] = {0, 0, 0};
+  S31 us[3];
   long long u2 = 0;
 #pragma unroll
   for (int d = 0; d < L::D; ++d) {
-    u[d] = mulshr(j[d], R, 58);
-    u2 += mulhi(u[d], u[d]);
+    u[d] = mul62(split(j[d] << 3), Rs);
+    us[d] = split(u[d]);
+    u2 += mul62(us[d], us[d]);
   }
-  const bool fast = u2 < 184467440737095516LL;  // |u|^2 < 0.01
+  const bool fast = u2 < 46116860184273879LL;  // |u|^2 < 0.01
   if (!__all_sync(0xffffffffu, fast)) return false;
-  const long long u4 = mulhi(u2, u2);
-  // Guo: u.F (2^64)
+  const S31 u2s = split(u2);
+  const long long u4 = mul62(u2s, u2s);
+  // the node's part of R_q: -1.5 u^2 + 1.125 u^4
+  const long long P0 = ((-3 * u2) >> 1) + ((9 * u4) >> 3);
+  // Guo: u.F (2^62)
   long long uF = 0;
   if (FS == FS_GUO) {
 #pragma unroll
-    for (int d = 0; d < L::D; ++d) uF += mulhi(u[d], Fx[d]);
+    for (int d = 0; d < L::D; ++d) uF += mul62(us[d], split(Fx[d]));
   }
-  const long long drho_w = drho;  // w_q delta rho via W64
-  // omega multiplier
-  const long long om = p.fx_omega_m;
-  const int oa = p.fx_omega_a, os = p.fx_omega_sign;
+  const int oa = p.fx_omega_a;
+  const S31 om = S31{p.fx_omega_s31[0], p.fx_omega_s31[1]};
+  bool out_bad = false;
+  // new population q from T = (f_eq_q - f_q) 2^62 and the source S (2^62)
   auto update = [&](int q, long long T, long long S) {
-    const long long m = mulhi_rn(T, om);
-    long long dq = (oa == 0 ? 0 : (oa == 1 ? T : 2 * T)) + (os > 0 ? m : -m);
-    dq += S;
-    const long long Fq = K::W60(q) + Dq[q] + dq;
-    if (active) pop(next, p.V, q)[(uint32_t)idx] = to_double<60>(Fq);
+    // (f + omega T + S) 2^62, summed modulo 2^64: a value outside (-2, 2)
+    // wraps to one that fails the range check
+    const long long X = (long long)((Fq[q] << 2) + (unsigned long long)(oa * T) +
+                                    (unsigned long long)mul62(split(T), om) +
+                                    (unsigned long long)S);
+    const double r = fixed62_to_double(X, out_bad);
+    if (active) pop(next, p.V, q)[(uint32_t)idx] = r;
   };
   // rest population: s = 0, R_0 = -1.5 u^2 + 1.125 u^4
   {
-    const long long wr = mulhi(rhoF, K::W64(0));  // w_0 rho 2^60
-    const long long R0 = ((-3 * u2) >> 1) + ((9 * u4) >> 3);
-    const long long T1 = K::C(0) + mulhi_rn(drho_w, K::W64(0)) - Dq[0];
-    const long long T2 = mulhi_rn(wr, R0);
+    const long long wr = mul62(rho61, csplit(K::W63(0)));  // w_0 rho 2^62
+    const long long T = wr - (long long)(Fq[0] << 2) + mul62(split(wr), split(P0));
     long long S = 0;
-    if (FS == FS_GUO) S = (mulhi_rn(-uF, p.fx_guo62[0]) + 2) >> 2;
-    update(0, T1 + T2, S);
+    if (FS == FS_GUO) S = mul62(split(-uF), S31{p.fx_guo_s31[0][0], p.fx_guo_s31[0][1]});
+    update(0, T, S);
   }
 #pragma unroll
   for (int q = 1; q < Q; ++q) {
     if (!is_pair_leader<LAT>(q)) continue;
     const int qb = opposite<LAT>(q);
-    long long s = 0, cj = 0, cF = 0;
+    long long s = 0, cF = 0;
 #pragma unroll
     for (int d = 0; d < L::D; ++d) {
-      if (L::c(q, d) > 0) { s += u[d]; cj += j[d]; cF += Fx[d]; }
-      if (L::c(q, d) < 0) { s -= u[d]; cj -= j[d]; cF -= Fx[d]; }
+      if (L::c(q, d) > 0) { s += u[d]; cF += Fx[d]; }
+      if (L::c(q, d) < 0) { s -= u[d]; cF -= Fx[d]; }
     }
-    const long long s2 = mulhi(s, s);
-    const long long s2u2 = mulhi(s2, u2);
-    const long long s4 = mulhi(s2, s2);
-    // even part 4.5 s^2 - 1.5 u^2 + 1.125 u^4 - 6.75 s^2 u^2 + 3.375 s^4,
-    // odd part (without the linear term) 4.5 s (s^2 - u^2)
-    const long long E = ((9 * s2 - 3 * u2) >> 1) + ((9 * u4 - 54 * s2u2 + 27 * s4) >> 3);
-    const long long O = (9 * mulhi(s, s2 - u2)) >> 1;
-    const long long wr = mulhi(rhoF, K::W64(q));  // w_q rho 2^60
-    const long long Tp2 = mulhi_rn(wr, E + O), Tm2 = mulhi_rn(wr, E - O);
-    const long long lin = mulhi_rn(cj, K::W3_64(q));  // 3 w_q c_q.j 2^60
-    const long long base = K::C(q) + mulhi_rn(drho_w, K::W64(q));
-    const long long Tp1 = base - Dq[q] + lin, Tm1 = base - Dq[qb] - lin;
+    const S31 ss = split(s);
+    const long long s2 = mul62(ss, ss);
+    const S31 s2s = split(s2);
+    // even part 4.5 s^2 + P0 + s^2 (3.375 s^2 - 6.75 u^2), odd part
+    // 3 s + 4.5 s (s^2 - u^2)
+    const long long E = ((9 * s2) >> 1) + P0 + mul62(s2s, split((27 * s2 - 54 * u2) >> 3));
+    const long long O = 3 * s + ((9 * mul62(ss, split(s2 - u2))) >> 1);
+    const long long wrv = mul62(rho61, csplit(K::W63(q)));  // w_q rho 2^62 (w_q = w_-q)
+    const S31 wr = split(wrv);
+    const long long Tp = wrv - (long long)(Fq[q] << 2) + mul62(wr, split(E + O));
+    const long long Tm = wrv - (long long)(Fq[qb] << 2) + mul62(wr, split(E - O));
     long long Sp = 0, Sm = 0;
     if (FS == FS_GUO) {
-      // ((c - u) + 3 (c.u) c).F = c.F - u.F + 3 s c.F (2^64); times guo_k (2^62) >> 66
-      const long long e3 = 3 * mulhi(s, cF);
-      Sp = (mulhi_rn(cF - uF + e3, p.fx_guo62[q]) + 2) >> 2;
-      Sm = (mulhi_rn(-cF - uF + e3, p.fx_guo62[qb]) + 2) >> 2;
+      // ((c - u) + 3 (c.u) c).F = c.F - u.F + 3 s c.F
+      const long long e3 = 3 * mul62(ss, split(cF));
+      Sp = mul62(split(cF - uF + e3), S31{p.fx_guo_s31[q][0], p.fx_guo_s31[q][1]});
+      Sm = mul62(split(-cF - uF + e3), S31{p.fx_guo_s31[qb][0], p.fx_guo_s31[qb][1]});
     }
-    update(q, Tp1 + Tp2, Sp);
-    update(qb, Tm1 + Tm2, Sm);
+    update(q, Tp, Sp);
+    update(qb, Tm, Sm);
   }
+  if (__any_sync(0xffffffffu, out_bad)) return false;
   // stored fields and diagnostics (store / diagnostics steps only): FP64
   if (active && (p.store || p.diag)) {
-    const double rho = to_double<60>(rhoF);
+    const double rho = to_double<60>((long long)rhoF);
     double ud[3] = {0.0, 0.0, 0.0};
 #pragma unroll
-    for (int d = 0; d < L::D; ++d) ud[d] = to_double<64>(u[d]);
+    for (int d = 0; d < L::D; ++d) ud[d] = to_double<62>(u[d]);
     double Fd[3] = {F[0], F[1], F[2]};
     store_node_fields<LAT>(p, idx, rho, ud, Fd, FS != FS_NONE, 2.0, energy, mach);
     mass = rho;

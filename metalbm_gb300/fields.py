@@ -109,7 +109,7 @@ def solenoidal_shell(shape, kmin: float, kmax: float, amplitude: float, seed: in
     for d in range(3):
         spec = np.zeros((lx, ly, nz), np.complex128)
         spec[I, J, K] = c[d]
-        u[d] = np.fft.irfftn(spec, s=(lx, ly, lz))
+        u[d] = np.fft.irfftn(spec, s=(lx, ly, lz), axes=(0, 1, 2))
     peak = np.sqrt((u ** 2).sum(axis=0)).max()
     if peak > 0:
         u *= amplitude / peak
