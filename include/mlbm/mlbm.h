@@ -240,7 +240,13 @@ int mlbm_create(const mlbm_config* cfg, mlbm_handle** out);
 int mlbm_destroy(mlbm_handle* h);
 
 /* f = f_eq(rho, u) and alpha = 2 (Initialize.h:82-116, then Algorithm::unpack,
- * Algorithm.h:141-147). rho: [V], u: [D][V] in the given layout, FP64. */
+ * Algorithm.h:141-147). rho: [V], u: [D][V] in the given layout, FP64 host
+ * arrays.
+ * Every host array of this interface in the DENSE layout that kernels can
+ * address (page-locked memory, or any host memory on a device that accesses
+ * pageable memory through the host's page tables, as NVLink-C2C systems do)
+ * moves by a copy kernel over the host link; other arrays by the copy
+ * engines. */
 int mlbm_init_equilibrium(mlbm_handle* h, const double* rho, const double* u, int layout);
 
 /* Populations in and out, FP64, [Q][V] in the given layout (Algorithm::pack /

@@ -177,11 +177,51 @@ static void ref_from_dense(const mlbm_handle* h, const double* dense, double* re
               dense[(long long)c * h->V + ((long long)x * h->ly + y) * h->lz + z];
 }
 
-// Upload ncomp host components (given layout) into device dense memory.
+// The address through which kernels on `device` access the n doubles at
+// `host`, when they can: page-locked (registered) host memory whose
+// registration covers the first and the last element, or any host memory on
+// a device that accesses pageable memory through the host's page tables
+// (NVLink-C2C systems). nullptr otherwise (device memory included).
+static double* device_view(int device, const double* host, size_t n) {
+  int pageable = 0, host_tables = 0;
+  if (cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, device) != cudaSuccess ||
+      cudaDeviceGetAttribute(&host_tables, cudaDevAttrPageableMemoryAccessUsesHostPageTables,
+                             device) != cudaSuccess) {
+    cudaGetLastError();
+    pageable = host_tables = 0;
+  }
+  cudaPointerAttributes a{}, b{};
+  if (cudaPointerGetAttributes(&a, host) != cudaSuccess ||
+      cudaPointerGetAttributes(&b, host + (n - 1)) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  if (a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged) return nullptr;
+  if (a.type == cudaMemoryTypeHost && b.type == cudaMemoryTypeHost && a.devicePointer &&
+      b.devicePointer &&
+      (const char*)b.devicePointer - (const char*)a.devicePointer ==
+          (std::ptrdiff_t)((n - 1) * sizeof(double)))
+    return (double*)a.devicePointer;
+  if (pageable && host_tables && a.type == cudaMemoryTypeUnregistered &&
+      b.type == cudaMemoryTypeUnregistered)
+    return const_cast<double*>(host);
+  return nullptr;
+}
+
+// Upload ncomp host components (given layout) into device dense memory. A
+// dense array that kernels can read in place is moved by a copy kernel over
+// the host link (on GB300 systems several times the rate that the copy
+// engines reach from 64 KiB-page host memory); others by cudaMemcpyAsync.
 static int upload(mlbm_handle* h, const double* host, double* dev, int ncomp, int layout) {
   const size_t bytes = sizeof(double) * (size_t)h->V * ncomp;
   if (layout == MLBM_LAYOUT_DENSE) {
-    MLBM_CUDA(h, cudaMemcpyAsync(dev, host, bytes, cudaMemcpyHostToDevice, h->stream));
+    if (const double* view = device_view(h->cfg.device, host, (size_t)h->V * ncomp)) {
+      cudaError_t e = copy_doubles(view, dev, h->V * ncomp, h->stream);
+      count_launches(1);
+      if (e != cudaSuccess) return fail(h, MLBM_ERR_CUDA, "host copy: %s", cudaGetErrorString(e));
+    } else {
+      MLBM_CUDA(h, cudaMemcpyAsync(dev, host, bytes, cudaMemcpyHostToDevice, h->stream));
+    }
     MLBM_CUDA(h, cudaStreamSynchronize(h->stream));
     return MLBM_OK;
   }
@@ -198,7 +238,13 @@ static int upload(mlbm_handle* h, const double* host, double* dev, int ncomp, in
 static int download(mlbm_handle* h, const double* dev, double* host, int ncomp, int layout) {
   const size_t bytes = sizeof(double) * (size_t)h->V * ncomp;
   if (layout == MLBM_LAYOUT_DENSE) {
-    MLBM_CUDA(h, cudaMemcpyAsync(host, dev, bytes, cudaMemcpyDeviceToHost, h->stream));
+    if (double* view = device_view(h->cfg.device, host, (size_t)h->V * ncomp)) {
+      cudaError_t e = copy_doubles(dev, view, h->V * ncomp, h->stream);
+      count_launches(1);
+      if (e != cudaSuccess) return fail(h, MLBM_ERR_CUDA, "host copy: %s", cudaGetErrorString(e));
+    } else {
+      MLBM_CUDA(h, cudaMemcpyAsync(host, dev, bytes, cudaMemcpyDeviceToHost, h->stream));
+    }
     MLBM_CUDA(h, cudaStreamSynchronize(h->stream));
     return MLBM_OK;
   }
@@ -336,15 +382,10 @@ static double host_sin_profile(double amplitude, unsigned i, double lambda) {
 }
 
 static int fill_alpha(mlbm_handle* h, double value) {
-  std::vector<double> a64;
-  std::vector<float> a32;
-  if (h->alpha) {
-    a64.assign((size_t)h->V, value);
-    MLBM_CUDA(h, cudaMemcpy(h->alpha, a64.data(), sizeof(double) * h->V, cudaMemcpyHostToDevice));
-  } else {
-    a32.assign((size_t)h->V, (float)(value - 2.0));  // the device keeps alpha - 2
-    MLBM_CUDA(h, cudaMemcpy(h->alpha32, a32.data(), sizeof(float) * h->V, cudaMemcpyHostToDevice));
-  }
+  cudaError_t e = fill_alpha_field(h->alpha, h->alpha32, h->V, value, h->stream);
+  count_launches(1);
+  if (e != cudaSuccess) return fail(h, MLBM_ERR_CUDA, "alpha fill: %s", cudaGetErrorString(e));
+  MLBM_CUDA(h, cudaStreamSynchronize(h->stream));
   return MLBM_OK;
 }
 
@@ -477,7 +518,9 @@ extern "C" int mlbm_create(const mlbm_config* cfg, mlbm_handle** out) {
       return bail(rc);
     cudaMemsetAsync(h->defer_count, 0, 2 * sizeof(unsigned), h->stream);
   }
-  if ((rc = device_alloc(h, (void**)&h->partials, sizeof(double) * DIAG_FIELDS * h->partial_blocks)) ||
+  if ((rc = device_alloc(h, (void**)&h->partials,
+                         sizeof(double) * DIAG_FIELDS *
+                             (h->partial_blocks + finalize_diag_scratch(h->partial_blocks)))) ||
       (rc = device_alloc(h, (void**)&h->diag_dev, sizeof(double) * DIAG_FIELDS)) ||
       (rc = device_alloc(h, (void**)&h->counters, sizeof(unsigned long long) * CNT_COUNT)) ||
       (rc = device_alloc(h, (void**)&h->err_word, sizeof(unsigned))) ||
@@ -644,7 +687,8 @@ extern "C" int mlbm_init_equilibrium(mlbm_handle* h, const double* rho, const do
   if (!rho || !u || !valid_layout(layout)) return fail(h, MLBM_ERR_INVALID, "bad arguments");
   MLBM_CUDA(h, cudaSetDevice(h->cfg.device));
   int rc;
-  // rho and u go through the field buffers (overwritten by the next store).
+  // rho and u go through the field buffers (overwritten by the next store;
+  // a spectral force is formed from them before the first step).
   if ((rc = upload(h, rho, h->rho, 1, layout))) return rc;
   if ((rc = upload(h, u, h->u, h->D, layout))) return rc;
   cudaError_t e = h->storage == MLBM_STORAGE_F64
@@ -762,8 +806,8 @@ static int enqueue_step(mlbm_handle* h, bool last, unsigned int flags, bool in_p
       const int nb = collision ? (int)((h->V + 127) / 128) + h->defer_blocks
                                : (int)bgk_step_blocks(h->cfg.lattice, h->storage, h->V,
                                                       (unsigned)h->base.lz);
-      e = finalize_diag(h->partials, nb, h->diag_dev, h->stream);
-      count_launches(1);
+      e = finalize_diag_fold(h->partials, nb, h->diag_dev, h->stream);
+      count_launches(finalize_diag_launches(nb));
       if (e != cudaSuccess) return fail(h, MLBM_ERR_CUDA, "diagnostics: %s", cudaGetErrorString(e));
     }
     if (last && (flags & MLBM_STEP_LOG_SAMPLES)) {

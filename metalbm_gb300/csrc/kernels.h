@@ -92,7 +92,20 @@ cudaError_t neq_test_L1(const float* f, long long nodes, int dfloat, double* out
 cudaError_t neq_test_L2(const float* f, long long nodes, int dfloat, double* out, cudaStream_t s);
 
 // Diagnostics: sum the per-block partials in a fixed order (deterministic).
+// The per-block diagnostics partials folded in a fixed order into out[5] by
+// one block (finalize_diag); finalize_diag_fold does the same for long lists
+// with a first level of blocks that writes finalize_diag_scratch(nblocks)
+// partials behind the list (the buffer must hold them) and one block folding
+// those. finalize_diag_launches: the kernels finalize_diag_fold launches.
 cudaError_t finalize_diag(const double* partials, int nblocks, double* out, cudaStream_t s);
+cudaError_t finalize_diag_fold(double* partials, int nblocks, double* out, cudaStream_t s);
+int finalize_diag_scratch(int nblocks);
+int finalize_diag_launches(int nblocks);
+// n doubles from src to dst, both addresses kernels can access.
+cudaError_t copy_doubles(const double* src, double* dst, long long n, cudaStream_t s);
+// The alpha field filled with `value` (FP64 field a64, or alpha - 2 in the
+// float field a32 when a64 is null).
+cudaError_t fill_alpha_field(double* a64, float* a32, long long n, double value, cudaStream_t s);
 
 // Sample logger: (f_neq/rho [Q], alpha) at the given nodes, from the
 // pre-collision populations `prev` and the alpha field of the step just run.

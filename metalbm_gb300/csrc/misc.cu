@@ -1,6 +1,9 @@
 // Small kernels shared by every storage format: the fixed-order reduction of
 // the per-block diagnostics partials, and the sample-logger dispatch.
 
+#include <algorithm>
+#include <cstdint>
+
 #include "common.cuh"
 #include "fastlog.cuh"
 #include "kernels.h"
@@ -10,8 +13,8 @@ namespace mlbm {
 // One block of 256 threads: each thread folds a strided subset of the
 // partials in index order, then a fixed tree; the result does not depend on
 // scheduling, so a diagnostics value is reproducible run to run.
-__global__ void finalize_diag_kernel(const double* __restrict__ partials, int nblocks,
-                                     double* __restrict__ out) {
+__device__ __forceinline__ void finalize_diag_body(const double* __restrict__ partials, int nblocks,
+                                                   double* __restrict__ out, bool root) {
   __shared__ double sh[DIAG_FIELDS][256];
   double m = 0.0, e = 0.0, mach = 0.0, amin = 1e300, amax = -1e300;
   for (int b = threadIdx.x; b < nblocks; b += blockDim.x) {
@@ -39,8 +42,13 @@ __global__ void finalize_diag_kernel(const double* __restrict__ partials, int nb
     for (int k = 0; k < DIAG_FIELDS; ++k) out[k] = sh[k][0];
     // the nodes contribute |u|^2 / c_s^2; sqrt is monotonic and correctly
     // rounded, so the root of the maximum is the maximum of the roots
-    out[2] = sqrt(sh[2][0]);
+    if (root) out[2] = sqrt(sh[2][0]);
   }
+}
+
+__global__ void finalize_diag_kernel(const double* __restrict__ partials, int nblocks,
+                                     double* __restrict__ out) {
+  finalize_diag_body(partials, nblocks, out, true);
 }
 
 __global__ void fast_log_kernel(const double* __restrict__ x, double* __restrict__ out, long long n,
@@ -59,8 +67,90 @@ cudaError_t fast_log_eval(const double* x, double* out, long long n, const void*
   return cudaGetLastError();
 }
 
+// First level for long partial lists: block b folds the partials
+// [b * chunk, (b + 1) * chunk) with the same fixed-order fold and tree, into
+// one partial of its own; finalize_diag_kernel then folds those. The
+// partition depends only on the list's length, so the result is still the
+// same run to run.
+__global__ void fold_diag_kernel(const double* __restrict__ partials, int nblocks, int chunk,
+                                 double* __restrict__ folded) {
+  const int b0 = blockIdx.x * chunk;
+  const int n = min(chunk, nblocks - b0);
+  finalize_diag_body(partials + (size_t)b0 * DIAG_FIELDS, n, folded + (size_t)blockIdx.x * DIAG_FIELDS,
+                     false);
+}
+
+// Partial lists up to this length are folded by one block; longer ones by
+// kFoldBlocks blocks first (the handle's partials buffer has room for the
+// folded list behind the longest list it holds).
+constexpr int kFoldThreshold = 8192;
+constexpr int kFoldBlocks = 512;
+
+int finalize_diag_scratch(int nblocks) { return nblocks > kFoldThreshold ? kFoldBlocks : 0; }
+
 cudaError_t finalize_diag(const double* partials, int nblocks, double* out, cudaStream_t s) {
   finalize_diag_kernel<<<1, 256, 0, s>>>(partials, nblocks, out);
+  return cudaGetLastError();
+}
+
+cudaError_t finalize_diag_fold(double* partials, int nblocks, double* out, cudaStream_t s) {
+  if (nblocks <= kFoldThreshold) return finalize_diag(partials, nblocks, out, s);
+  const int chunk = (nblocks + kFoldBlocks - 1) / kFoldBlocks;
+  const int used = (nblocks + chunk - 1) / chunk;
+  double* folded = partials + (size_t)nblocks * DIAG_FIELDS;
+  fold_diag_kernel<<<used, 256, 0, s>>>(partials, nblocks, chunk, folded);
+  finalize_diag_kernel<<<1, 256, 0, s>>>(folded, used, out);
+  return cudaGetLastError();
+}
+
+int finalize_diag_launches(int nblocks) { return nblocks > kFoldThreshold ? 2 : 1; }
+
+// Fill of the per-node alpha field: FP64 storage keeps alpha, the other
+// storage formats alpha - 2 in float.
+__global__ void fill_alpha_kernel(double* __restrict__ a64, float* __restrict__ a32, long long n,
+                                  double v64, float v32) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  if (a64) a64[i] = v64;
+  else a32[i] = v32;
+}
+
+// Copy of n doubles between any two addresses kernels can access (device
+// memory, page-locked or, on NVLink-C2C systems, pageable host memory):
+// 16-byte accesses when both ends are 16-byte aligned, grid-stride over a
+// grid of a few blocks per SM.
+__global__ void copy_doubles_kernel(const double* __restrict__ src, double* __restrict__ dst,
+                                    long long n, int vec) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (vec) {
+    const long long n2 = n / 2;
+    const double2* s2 = reinterpret_cast<const double2*>(src);
+    double2* d2 = reinterpret_cast<double2*>(dst);
+    for (long long k = i; k < n2; k += stride) d2[k] = s2[k];
+    if (i == 0 && (n & 1)) dst[n - 1] = src[n - 1];
+  } else {
+    for (long long k = i; k < n; k += stride) dst[k] = src[k];
+  }
+}
+
+cudaError_t copy_doubles(const double* src, double* dst, long long n, cudaStream_t s) {
+  int dev = 0, sms = 1;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
+    cudaGetLastError();
+    sms = 1;
+  }
+  const int vec = ((reinterpret_cast<uintptr_t>(src) | reinterpret_cast<uintptr_t>(dst)) & 15) == 0;
+  const long long work = vec ? n / 2 : n;
+  const long long blocks = std::min<long long>((long long)sms * 8, std::max<long long>(1, (work + 255) / 256));
+  copy_doubles_kernel<<<(unsigned)blocks, 256, 0, s>>>(src, dst, n, vec);
+  return cudaGetLastError();
+}
+
+cudaError_t fill_alpha_field(double* a64, float* a32, long long n, double value, cudaStream_t s) {
+  fill_alpha_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(a64, a32, n, value,
+                                                                 (float)(value - 2.0));
   return cudaGetLastError();
 }
 

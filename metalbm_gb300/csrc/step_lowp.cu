@@ -271,14 +271,18 @@ __device__ __forceinline__ void store_fields_f64(const StepParams& p, long long 
     if (p.alpha_field_f32 && write_alpha) p.alpha_field_f32[idx] = narrow_rn(alpha - 2.0);
   }
   if (p.diag) {
-    double e = 0.0, s = 0.0;
+    // the node's kinetic energy and |u|^2 / c_s^2 (the square root is taken
+    // once, in finalize_diag) in FP32 from the FP64 rho and u: a relative
+    // rounding of ~1e-7, below that of the FP32 / FP16 populations themselves,
+    // without GB300's narrow FP64 pipe
+    float s = 0.0f;
 #pragma unroll
     for (int k = 0; k < L::D; ++k) {
-      e += 0.5 * r * uh[k] * uh[k];
-      s += uh[k] * uh[k];
+      const float v = narrow_rn(uh[k]);
+      s = fmaf(v, v, s);
     }
-    energy = e;
-    mach = 3.0 * s;  // |u|^2 / c_s^2; the square root is taken once, in finalize_diag
+    energy = widen_exact(0.5f * narrow_rn(r) * s);
+    mach = widen_exact(3.0f * s);
   }
 }
 
@@ -1298,8 +1302,14 @@ __device__ __forceinline__ void elbm_node(const typename Storage<ST>::T* __restr
     const float stored = narrow_rn(alpha - 2.0);
     p.alpha_field_f32[idx] = stored;
     if (p.diag) {
-      amin = fmin(amin, 2.0 + widen_exact(stored));
-      amax = fmax(amax, 2.0 + widen_exact(stored));
+      const double a = 2.0 + widen_exact(stored);
+      if (MODE == ELBM_MAIN) {  // one node a thread: no FP64 compares
+        amin = a;
+        amax = a;
+      } else {
+        amin = fmin(amin, a);
+        amax = fmax(amax, a);
+      }
     }
   }
   if (MODE == ELBM_MAIN) {
@@ -1464,25 +1474,66 @@ __global__ void neq_test_kernel(const float* __restrict__ f, long long nodes, in
 }
 
 // ---- init and conversions ---------------------------------------------------
-// f_eq(rho, u) formed in FP64 with the TruncationMa3 polynomial in its pair form
-// (Equilibrium.h:17-33), rounded once into the storage format with integer
-// operations (no FP64 conversion instruction).
+// f_eq(rho, u) of the TruncationMa3 polynomial (Equilibrium.h:17-33) in its
+// pair form, in double-float arithmetic (about 46 significant bits from the
+// FP64 rho and u), rounded once into the storage format: the correctly rounded
+// storage value of the exact equilibrium except for the rare values within
+// ~2^-44 of a rounding boundary. The same polynomial in FP64 takes GB300's
+// narrow FP64 pipe about ten times as long.
+template <int LAT>
+__device__ __forceinline__ dfl weight_dfl(int q) {
+  const double w = Lattice<LAT>::w(q);
+  const float h = (float)w;
+  return {h, (float)(w - (double)h)};
+}
+
 template <int LAT, int ST>
 __global__ void init_lowp_kernel(const double* __restrict__ rho, const double* __restrict__ u,
                                  typename Storage<ST>::T* __restrict__ f, long long V) {
   using L = Lattice<LAT>;
   const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= V) return;
-  double uu[3] = {0.0, 0.0, 0.0};
+  dfl uu[3] = {{0.0f, 0.0f}, {0.0f, 0.0f}, {0.0f, 0.0f}};
 #pragma unroll
-  for (int k = 0; k < L::D; ++k) uu[k] = u[(long long)k * V + idx];
-  double feq[L::Q];
-  feq_pairs_f64<LAT>(rho[idx], uu, feq);
+  for (int k = 0; k < L::D; ++k) uu[k] = dfl_from(u[(long long)k * V + idx]);
+  const dfl r = dfl_from(rho[idx]);
+  dfl u2 = dfl_mul(uu[0], uu[0]);
 #pragma unroll
-  for (int q = 0; q < L::Q; ++q) {
+  for (int k = 1; k < L::D; ++k) u2 = dfl_add(u2, dfl_mul(uu[k], uu[k]));
+  // u^2 (1.125 u^2 - 1.5), 4.5 - 6.75 u^2, 3 - 4.5 u^2
+  const dfl common = dfl_mul(u2, dfl_add_f(dfl_mul_f(u2, 1.125f), -1.5f));
+  const dfl A = dfl_add_f(dfl_mul_f(u2, -6.75f), 4.5f);
+  const dfl B = dfl_add_f(dfl_mul_f(u2, -4.5f), 3.0f);
+  auto put = [&](int q, dfl P) {  // f_q = rho w_q P
+    const dfl v = dfl_mul(dfl_mul(r, weight_dfl<LAT>(q)), P);
     auto* dst = pop(f, V, q) + (uint32_t)idx;
-    if constexpr (ST == ST_F32) *dst = narrow_rn(feq[q]);
-    else *dst = __float2half_rn(narrow_rn((feq[q] - L::w(q)) * (double)(1 << shift_exponent<LAT>(q))));
+    if constexpr (ST == ST_F32) {
+      *dst = __fadd_rn(v.hi, v.lo);
+    } else {
+      const dfl d = dfl_sub(v, weight_dfl<LAT>(q));
+      *dst = __float2half_rn(__fadd_rn(d.hi, d.lo) * (float)(1 << shift_exponent<LAT>(q)));
+    }
+  };
+  put(0, dfl_add_f(common, 1.0f));
+#pragma unroll
+  for (int q = 1; q < L::Q; ++q) {
+    if (is_pair_leader<LAT>(q)) {
+      const int qb = opposite<LAT>(q);
+      dfl cu = {0.0f, 0.0f};
+      bool first = true;
+#pragma unroll
+      for (int k = 0; k < L::D; ++k) {
+        if (L::c(q, k) == 0) continue;
+        const dfl t = L::c(q, k) > 0 ? uu[k] : dfl_neg(uu[k]);
+        cu = first ? t : dfl_add(cu, t);
+        first = false;
+      }
+      const dfl c2 = dfl_mul(cu, cu);
+      const dfl E = dfl_add(dfl_mul(c2, dfl_add(dfl_mul_f(c2, 3.375f), A)), common);
+      const dfl O = dfl_mul(cu, dfl_add(dfl_mul_f(c2, 4.5f), B));
+      put(q, dfl_add_f(dfl_add(E, O), 1.0f));
+      put(qb, dfl_add_f(dfl_sub(E, O), 1.0f));
+    }
   }
 }
 

@@ -145,6 +145,58 @@ def test_registered_host_buffers_round_trip():
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("storage", ["f32", "f16_shifted"])
+def test_init_in_place_and_rounding(storage):
+    """mlbm_init_equilibrium reads page-locked (and, where the device reads
+    pageable memory, ordinary) host arrays in place: the same populations as
+    from ordinary arrays; the FP32 equilibrium (double-float arithmetic) is
+    the FP64 equilibrium of the reference order rounded to float, at most one
+    float ulp off in rare near-tie cases; FP16-shifted within one half ulp of
+    the scaled deviation."""
+    from metalbm_gb300 import InputDeck, Lattice, fields
+    from metalbm_gb300.hostbuf import pinned_array
+    shape = (24, 20, 16)
+    V = 24 * 20 * 16
+    rho, u = fields.perturbed_rest(shape, 3, 0.08, seed=5, rho_amplitude=0.05)
+    h_rho, h_u = pinned_array((V,)), pinned_array((3, V))
+    h_rho[:] = rho
+    h_u[:] = u
+    out = {}
+    for st in ("f64", storage):
+        deck = InputDeck(latticeT="D3Q27", collisionT="ELBM", relaxationTime=0.50025,
+                         globalLength=shape, storage=st)
+        with Lattice(deck) as lat:
+            lat.init_equilibrium(h_rho, h_u)
+            a = lat.populations()
+            lat.init_equilibrium(rho, u)
+            b = lat.populations()
+        assert np.array_equal(a, b)
+        out[st] = a
+    f64 = out["f64"]
+    if storage == "f32":
+        ref = f64.astype(np.float32).astype(np.float64)
+        got = out["f32"]
+        ulps = np.abs(got - ref) / np.spacing(np.abs(ref).astype(np.float32)).astype(np.float64)
+        assert ulps.max() <= 1.0
+        assert (got == ref).mean() >= 0.9999
+    else:
+        from oracle import lattice_tables
+        _, w = lattice_tables("D3Q27")
+        # FP16-shifted storage: h = fp16(fp32((f - w_q) 2^k_q)), k_q =
+        # round(log2(1024 / w_q)); the same rounding of the FP64 equilibrium,
+        # one FP16 ulp apart in rare near-tie cases
+        k = np.select([w > 0.4, w > 0.3, w > 0.1, w > 0.06, w > 0.025, w > 0.01],
+                      [11, 12, 13, 14, 15, 16], 18).astype(np.float64)[:, None]
+        scale = 2.0 ** k
+        h_ref = ((f64 - w[:, None]) * scale).astype(np.float32).astype(np.float16)
+        h_got = ((out[storage] - w[:, None]) * scale).astype(np.float16)
+        ulp16 = np.spacing(np.abs(h_ref)).astype(np.float64)
+        diff = np.abs(h_got.astype(np.float64) - h_ref.astype(np.float64))
+        assert (diff <= ulp16).all()
+        assert (diff == 0).mean() >= 0.9999
+
+
+@pytest.mark.gpu
 def test_deck_initial_fields_step_like_the_oracle():
     """Lattice.initialize() from the deck's initDensityT = Peak and a
     homogeneous initVelocityVector (Initialize.h:19-116), then BGK steps with
