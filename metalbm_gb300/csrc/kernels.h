@@ -25,18 +25,13 @@ cudaError_t step_f64(int lattice, int collision, int forcing, const double* prev
 cudaError_t init_f64(int lattice, const double* rho, const double* u, double* f, long long V,
                      cudaStream_t s);
 
-// BGK with FP16-shifted storage on 3-D lattices runs four z-adjacent nodes a
-// thread when Lz is a multiple of 4 (bgk_f16_quad_kernel), two when it is
-// even (bgk_f16_pair_kernel); the number of 256-thread blocks of the BGK step
-// kernel, whose partials finalize_diag sums.
-inline bool bgk_quads(int lattice, int storage, unsigned lz) {
-  return storage == 2 && lattice != 0 && lz % 4 == 0;
-}
+// BGK with FP16-shifted storage on 3-D lattices runs two z-adjacent nodes a
+// thread when Lz is even (bgk_f16_pair_kernel); the number of 256-thread
+// blocks of the BGK step kernel, whose partials finalize_diag sums.
 inline bool bgk_pairs(int lattice, int storage, unsigned lz) {
   return storage == 2 && lattice != 0 && lz % 2 == 0;
 }
 inline long long bgk_step_blocks(int lattice, int storage, long long V, unsigned lz) {
-  if (bgk_quads(lattice, storage, lz)) return (V / 4 + 255) / 256;
   return bgk_pairs(lattice, storage, lz) ? (V / 2 + 255) / 256 : (V + 255) / 256;
 }
 

@@ -413,6 +413,146 @@ __device__ __forceinline__ void bgk_node(const StepParams& p, uint32_t x, uint32
   rho_out = rho;
 }
 
+// ---- two nodes in packed FP32x2 lanes -----------------------------------------
+// GB300 executes an FP32 add, multiply or FMA on a pair of floats as one
+// instruction (FADD2 / FMUL2 / FFMA2): the kernels that hold two nodes a
+// thread run bgk_node's arithmetic on both at half the issue slots. Every
+// operation is an explicit round-to-nearest one, so the two lanes get the
+// results of the scalar operations (bgk_node may contract a multiply and an
+// add into one FMA where this function rounds twice: the same formula within
+// FP32 rounding).
+__device__ __forceinline__ float2 f2(float s) { return make_float2(s, s); }
+__device__ __forceinline__ float2 f2add(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 f2sub(float2 a, float2 b) {
+  return __fadd2_rn(a, make_float2(-b.x, -b.y));
+}
+__device__ __forceinline__ float2 f2mul(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 f2fma(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+
+template <int LAT>
+__device__ __forceinline__ float2 cdotf2(int q, const float2 v[3]) {
+  using L = Lattice<LAT>;
+  float2 r = f2(0.0f);
+  bool first = true;
+#pragma unroll
+  for (int d = 0; d < L::D; ++d) {
+    const int c = L::c(q, d);
+    if (c == 0) continue;
+    if (first) r = c > 0 ? v[d] : make_float2(-v[d].x, -v[d].y);
+    else r = c > 0 ? f2add(r, v[d]) : f2sub(r, v[d]);
+    first = false;
+  }
+  return r;
+}
+
+// the even and odd parts of the TruncationMa3 polynomial for a pair,
+// A = 4.5 - 6.75 u^2 and B = 3 - 4.5 u^2 formed once a node
+__device__ __forceinline__ void poly_pair2(float2 cu, float2 A, float2 B, float2 common, float2& E,
+                                           float2& O) {
+  const float2 c2 = f2mul(cu, cu);
+  E = f2fma(c2, f2fma(f2(3.375f), c2, A), common);
+  O = f2mul(cu, f2fma(f2(4.5f), c2, B));
+}
+
+template <int D>
+__device__ __forceinline__ void node_force_float2(const StepParams& p, uint32_t x, uint32_t y,
+                                                  uint32_t z0, uint32_t z1, float2 F[3]) {
+  float a[3], b[3];
+  node_force_float<D>(p, x, y, z0, a);
+  node_force_float<D>(p, x, y, z1, b);
+#pragma unroll
+  for (int k = 0; k < 3; ++k) F[k] = make_float2(a[k], b[k]);
+}
+
+// bgk_node for the nodes (x, y, z0) and (x, y, z1) in the lanes of d.
+template <int LAT, int FS, int ST>
+__device__ __forceinline__ void bgk_node2(const StepParams& p, uint32_t x, uint32_t y, uint32_t z0,
+                                          uint32_t z1, float2 d[Lattice<LAT>::Q], float2& rho_out,
+                                          float2 u[3]) {
+  using L = Lattice<LAT>;
+  using S = Storage<ST>;
+  float2 rhop = f2(0.0f), j[3] = {f2(0.0f), f2(0.0f), f2(0.0f)};
+#pragma unroll
+  for (int q = 0; q < L::Q; ++q) {
+    const float is = 1.0f / S::template scale<LAT>(q);
+    rhop = f2fma(d[q], f2(is), rhop);
+#pragma unroll
+    for (int k = 0; k < L::D; ++k) {
+      if (L::c(q, k) > 0) j[k] = f2fma(d[q], f2(is), j[k]);
+      if (L::c(q, k) < 0) j[k] = f2fma(d[q], f2(-is), j[k]);
+    }
+  }
+  const float2 rho = f2add(f2(1.0f), rhop);
+  const float2 irho = make_float2(1.0f / rho.x, 1.0f / rho.y);
+#pragma unroll
+  for (int k = 0; k < 3; ++k) u[k] = f2mul(j[k], irho);
+  float2 F[3] = {f2(0.0f), f2(0.0f), f2(0.0f)};
+  if (FS != FS_NONE) node_force_float2<L::D>(p, x, y, z0, z1, F);
+  float2 u2 = f2mul(u[0], u[0]);
+#pragma unroll
+  for (int k = 1; k < L::D; ++k) u2 = f2fma(u[k], u[k], u2);
+  const float2 common = f2mul(u2, f2fma(f2(1.125f), u2, f2(-1.5f)));
+  const float2 A = f2fma(f2(-6.75f), u2, f2(4.5f));
+  const float2 B = f2fma(f2(-4.5f), u2, f2(3.0f));
+  const float2 b = f2(p.bgk_b_f);
+  float2 uF = f2(0.0f), v[3] = {f2(0.0f), f2(0.0f), f2(0.0f)};
+  float2 commonv = common, Av = A, Bv = B;
+  if (FS == FS_GUO) {
+    uF = f2mul(u[0], F[0]);
+#pragma unroll
+    for (int k = 1; k < L::D; ++k) uF = f2fma(u[k], F[k], uF);
+  }
+  if (FS == FS_EDM) {
+#pragma unroll
+    for (int k = 0; k < 3; ++k) v[k] = f2fma(F[k], irho, u[k]);
+    float2 v2 = f2mul(v[0], v[0]);
+#pragma unroll
+    for (int k = 1; k < L::D; ++k) v2 = f2fma(v[k], v[k], v2);
+    commonv = f2mul(v2, f2fma(f2(1.125f), v2, f2(-1.5f)));
+    Av = f2fma(f2(-6.75f), v2, f2(4.5f));
+    Bv = f2fma(f2(-4.5f), v2, f2(3.0f));
+  }
+  {  // rest population
+    const float ws = (float)L::w(0) * S::template scale<LAT>(0);
+    const float2 deq = f2mul(f2(ws), f2fma(rho, common, rhop));
+    float2 r = f2fma(b, f2sub(deq, d[0]), d[0]);
+    if (FS == FS_GUO) r = f2fma(f2(-(p.guo_kt_f * ws)), uF, r);
+    if (FS == FS_EDM) r = f2fma(f2mul(f2(ws), rho), f2sub(commonv, common), r);
+    d[0] = r;
+  }
+#pragma unroll
+  for (int q = 1; q < L::Q; ++q) {
+    if (is_pair_leader<LAT>(q)) {
+      const int qb = opposite<LAT>(q);
+      const float ws = (float)L::w(q) * S::template scale<LAT>(q);
+      const float2 cu = cdotf2<LAT>(q, u);
+      float2 E, O;
+      poly_pair2(cu, A, B, common, E, O);
+      const float2 dq = f2mul(f2(ws), f2fma(rho, f2add(E, O), rhop));
+      const float2 dqb = f2mul(f2(ws), f2fma(rho, f2sub(E, O), rhop));
+      float2 rq = f2fma(b, f2sub(dq, d[q]), d[q]);
+      float2 rqb = f2fma(b, f2sub(dqb, d[qb]), d[qb]);
+      if (FS == FS_GUO) {
+        const float2 cF = cdotf2<LAT>(q, F);
+        const float2 Es = f2fma(f2mul(f2(3.0f), cu), cF, make_float2(-uF.x, -uF.y));
+        const float2 kw = f2(p.guo_kt_f * ws);
+        rq = f2fma(kw, f2add(Es, cF), rq);
+        rqb = f2fma(kw, f2sub(Es, cF), rqb);
+      }
+      if (FS == FS_EDM) {
+        float2 Ev, Ov;
+        poly_pair2(cdotf2<LAT>(q, v), Av, Bv, commonv, Ev, Ov);
+        const float2 wr = f2mul(f2(ws), rho);
+        rq = f2fma(wr, f2sub(f2add(Ev, Ov), f2add(E, O)), rq);
+        rqb = f2fma(wr, f2sub(f2sub(Ev, Ov), f2sub(E, O)), rqb);
+      }
+      d[q] = rq;
+      d[qb] = rqb;
+    }
+  }
+  rho_out = rho;
+}
+
 template <int LAT, int FS, int ST>
 __device__ __forceinline__ void bgk_node_fields(const StepParams& p, long long idx, uint32_t x,
                                                 uint32_t y, uint32_t z, float rho,
@@ -456,10 +596,14 @@ __global__ void __launch_bounds__(256) bgk_lowp_kernel(const typename Storage<ST
 
 // FP16-shifted storage, two z-adjacent nodes a thread (z even, Lz even): the
 // populations with c_z = 0 load as one aligned half2 for both nodes, every
-// population stores as one half2, and the node's coordinates and periodic
-// offsets are formed once for the pair.
+// population stores as one half2, the node's coordinates and periodic
+// offsets are formed once for the pair, and the two collisions run in packed
+// FP32x2 lanes (bgk_node2). Three blocks of 256 threads a SM (80 registers).
+// Measured against four nodes a thread (one 8-byte load a population plus
+// the line-edge value, 128 registers, two blocks a SM): 0.270 against
+// 0.280 ms a step at 256^3 D3Q19.
 template <int LAT, int FS>
-__global__ void __launch_bounds__(256) bgk_f16_pair_kernel(const __half* __restrict__ prev,
+__global__ void __launch_bounds__(256, 3) bgk_f16_pair_kernel(const __half* __restrict__ prev,
                                                            __half* __restrict__ next,
                                                            StepParams p) {
   using L = Lattice<LAT>;
@@ -472,30 +616,29 @@ __global__ void __launch_bounds__(256) bgk_f16_pair_kernel(const __half* __restr
     const PullOffsets o = pull_offsets(p, x, y, z);
     // second node's z neighbours: z + 1 reads z + 2 (c_z = -1) and z (c_z = +1)
     const uint32_t z2p = (z + 2 == p.lz) ? 0 : z + 2;
-    float d0[L::Q], d1[L::Q];
+    float2 d[L::Q];
 #pragma unroll
     for (int q = 0; q < L::Q; ++q) {
       const __half* src = pop(prev, p.V, q);
       const int cx = L::c(q, 0), cy = L::c(q, 1), cz = L::c(q, 2);
       const uint32_t xy = o.ox[cx + 1] + o.oy[cy + 1];
       if (cz == 0) {
-        const __half2 h = __ldg(reinterpret_cast<const __half2*>(src + xy + z));
-        d0[q] = __low2float(h);
-        d1[q] = __high2float(h);
+        d[q] = __half22float2(__ldg(reinterpret_cast<const __half2*>(src + xy + z)));
       } else if (cz > 0) {  // reads z - 1 and z
-        d0[q] = __half2float(__ldg(src + xy + o.oz[2]));
-        d1[q] = __half2float(__ldg(src + xy + z));
+        d[q] = make_float2(__half2float(__ldg(src + xy + o.oz[2])),
+                           __half2float(__ldg(src + xy + z)));
       } else {  // reads z + 1 and z + 2
-        d0[q] = __half2float(__ldg(src + xy + o.oz[0]));
-        d1[q] = __half2float(__ldg(src + xy + z2p));
+        d[q] = make_float2(__half2float(__ldg(src + xy + o.oz[0])),
+                           __half2float(__ldg(src + xy + z2p)));
       }
     }
-    float rho0, u0[3], rho1, u1[3];
-    bgk_node<LAT, FS, ST_F16>(p, x, y, z, d0, rho0, u0);
-    bgk_node<LAT, FS, ST_F16>(p, x, y, z + 1, d1, rho1, u1);
+    float2 rho2, u2v[3];
+    bgk_node2<LAT, FS, ST_F16>(p, x, y, z, z + 1, d, rho2, u2v);
 #pragma unroll
     for (int q = 0; q < L::Q; ++q)
-      *reinterpret_cast<__half2*>(pop(next, p.V, q) + (uint32_t)idx) = __floats2half2_rn(d0[q], d1[q]);
+      *reinterpret_cast<__half2*>(pop(next, p.V, q) + (uint32_t)idx) = __float22half2_rn(d[q]);
+    const float rho0 = rho2.x, rho1 = rho2.y;
+    const float u0[3] = {u2v[0].x, u2v[1].x, u2v[2].x}, u1[3] = {u2v[0].y, u2v[1].y, u2v[2].y};
     double m1 = 0.0, e1 = 0.0, a1 = 0.0;
     bgk_node_fields<LAT, FS, ST_F16>(p, idx, x, y, z, rho0, u0, mass, energy, mach);
     bgk_node_fields<LAT, FS, ST_F16>(p, idx + 1, x, y, z + 1, rho1, u1, m1, e1, a1);
@@ -503,71 +646,6 @@ __global__ void __launch_bounds__(256) bgk_f16_pair_kernel(const __half* __restr
       mass += m1;
       energy += e1;
       mach = fmax(mach, a1);
-    }
-  }
-  if (p.diag) block_reduce_diag(mass, energy, mach, 2.0, 2.0, p.diag_partials);
-}
-
-// FP16-shifted storage, four z-adjacent nodes a thread (z a multiple of 4,
-// Lz a multiple of 4): every population loads as one aligned 8-byte word of
-// the four source values at z .. z+3 of its source line, plus, when c_z != 0,
-// the one value that falls outside it (z - 1 or z + 4, periodic): 29 loads for
-// four D3Q19 nodes instead of 58 with two nodes a thread. Each pair of nodes
-// is collided and stored as half2, as in bgk_f16_pair_kernel.
-template <int LAT, int FS>
-__global__ void __launch_bounds__(256, 2) bgk_f16_quad_kernel(const __half* __restrict__ prev,
-                                                              __half* __restrict__ next,
-                                                              StepParams p) {
-  using L = Lattice<LAT>;
-  const long long idx = 4 * ((long long)blockIdx.x * blockDim.x + threadIdx.x);
-  const bool active = idx < p.V;
-  double mass = 0.0, energy = 0.0, mach = 0.0;
-  if (active) {
-    uint32_t x, y, z;
-    node_coords(p, idx, x, y, z);  // z a multiple of 4
-    const PullOffsets o = pull_offsets(p, x, y, z);
-    const uint32_t zm = o.oz[2];                          // z - 1, periodic
-    const uint32_t z4 = (z + 4 == p.lz) ? 0 : z + 4;      // z + 4, periodic
-    uint2 raw[L::Q];
-    __half edge[L::Q];
-#pragma unroll
-    for (int q = 0; q < L::Q; ++q) {
-      const __half* src = pop(prev, p.V, q) + o.ox[L::c(q, 0) + 1] + o.oy[L::c(q, 1) + 1];
-      raw[q] = __ldg(reinterpret_cast<const uint2*>(src + z));
-      if (L::c(q, 2) > 0) edge[q] = __ldg(src + zm);
-      if (L::c(q, 2) < 0) edge[q] = __ldg(src + z4);
-    }
-    // node k reads its population q at z + k - c_z: element k - c_z of the
-    // word, or the edge value when that falls outside 0 .. 3
-    auto val = [&](int q, int k) -> float {
-      const int e = k - L::c(q, 2);
-      if (e < 0 || e > 3) return __half2float(edge[q]);
-      const uint32_t w = e < 2 ? raw[q].x : raw[q].y;
-      return __half2float(__ushort_as_half((unsigned short)((e & 1) ? (w >> 16) : (w & 0xffffu))));
-    };
-#pragma unroll
-    for (int kk = 0; kk < 4; kk += 2) {
-      float d0[L::Q], d1[L::Q];
-#pragma unroll
-      for (int q = 0; q < L::Q; ++q) {
-        d0[q] = val(q, kk);
-        d1[q] = val(q, kk + 1);
-      }
-      float rho0, u0[3], rho1, u1[3];
-      bgk_node<LAT, FS, ST_F16>(p, x, y, z + kk, d0, rho0, u0);
-      bgk_node<LAT, FS, ST_F16>(p, x, y, z + kk + 1, d1, rho1, u1);
-#pragma unroll
-      for (int q = 0; q < L::Q; ++q)
-        *reinterpret_cast<__half2*>(pop(next, p.V, q) + (uint32_t)(idx + kk)) =
-            __floats2half2_rn(d0[q], d1[q]);
-      double m0 = 0.0, e0 = 0.0, a0 = 0.0, m1 = 0.0, e1 = 0.0, a1 = 0.0;
-      bgk_node_fields<LAT, FS, ST_F16>(p, idx + kk, x, y, z + kk, rho0, u0, m0, e0, a0);
-      bgk_node_fields<LAT, FS, ST_F16>(p, idx + kk + 1, x, y, z + kk + 1, rho1, u1, m1, e1, a1);
-      if (p.diag) {  // FP64 only on diagnostics steps
-        mass += m0 + m1;
-        energy += e0 + e1;
-        mach = fmax(mach, fmax(a0, a1));
-      }
     }
   }
   if (p.diag) block_reduce_diag(mass, energy, mach, 2.0, 2.0, p.diag_partials);
@@ -1605,10 +1683,7 @@ static cudaError_t launch_lowp(int collision, const void* prev, void* next, cons
   using T = typename Storage<ST>::T;
   if (collision == 0) {
     const int bs = 256;
-    if (bgk_quads(LAT, ST, p.lz)) {
-      const unsigned grid = (unsigned)bgk_step_blocks(LAT, ST, p.V, p.lz);
-      bgk_f16_quad_kernel<LAT, FS><<<grid, bs, 0, s>>>((const __half*)prev, (__half*)next, p);
-    } else if (bgk_pairs(LAT, ST, p.lz)) {
+    if (bgk_pairs(LAT, ST, p.lz)) {
       const unsigned grid = (unsigned)bgk_step_blocks(LAT, ST, p.V, p.lz);
       bgk_f16_pair_kernel<LAT, FS><<<grid, bs, 0, s>>>((const __half*)prev, (__half*)next, p);
     } else {

@@ -468,10 +468,10 @@ def test_f64_fixed_point_falls_back_out_of_range():
 @pytest.mark.gpu
 @pytest.mark.parametrize("lattice", ["D3Q19", "D3Q27", "D3Q15"])
 @pytest.mark.parametrize("forcing,force", [("Guo", "Kolmogorov"), ("ExactDifferenceMethod", "Sinusoidal")])
-def test_f16_four_nodes_a_thread_tracks_f64(lattice, forcing, force):
-    """FP16-shifted storage on a lattice whose Lz is a multiple of 4 (the
-    four-nodes-a-thread kernel, with the periodic edge values of the z lines)
-    against the FP64 kernel, to the storage tolerance of the two-node kernel."""
+def test_f16_two_nodes_packed_tracks_f64(lattice, forcing, force):
+    """FP16-shifted storage (the two-nodes-a-thread kernel, both nodes'
+    collision in packed FP32x2 instructions, with the periodic ends of the z
+    lines) against the FP64 kernel, to the FP16 storage tolerance."""
     from metalbm_gb300 import InputDeck, Lattice, fields
     shape = (10, 6, 16)
     rho, u = fields.perturbed_rest(shape, 3, 0.02, seed=8, rho_amplitude=0.005)
