@@ -420,26 +420,18 @@ __device__ __forceinline__ void bgk_node(const StepParams& p, uint32_t x, uint32
 // operation is an explicit round-to-nearest one, so the two lanes get the
 // results of the scalar operations (bgk_node may contract a multiply and an
 // add into one FMA where this function rounds twice: the same formula within
-// FP32 rounding).
-__device__ __forceinline__ float2 f2(float s) { return make_float2(s, s); }
-__device__ __forceinline__ float2 f2add(float2 a, float2 b) { return __fadd2_rn(a, b); }
-__device__ __forceinline__ float2 f2sub(float2 a, float2 b) {
-  return __fadd2_rn(a, make_float2(-b.x, -b.y));
-}
-__device__ __forceinline__ float2 f2mul(float2 a, float2 b) { return __fmul2_rn(a, b); }
-__device__ __forceinline__ float2 f2fma(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
-
+// FP32 rounding). The packed helpers are those of dfloat.cuh.
 template <int LAT>
 __device__ __forceinline__ float2 cdotf2(int q, const float2 v[3]) {
   using L = Lattice<LAT>;
-  float2 r = f2(0.0f);
+  float2 r = bcast2(0.0f);
   bool first = true;
 #pragma unroll
   for (int d = 0; d < L::D; ++d) {
     const int c = L::c(q, d);
     if (c == 0) continue;
-    if (first) r = c > 0 ? v[d] : make_float2(-v[d].x, -v[d].y);
-    else r = c > 0 ? f2add(r, v[d]) : f2sub(r, v[d]);
+    if (first) r = c > 0 ? v[d] : neg2(v[d]);
+    else r = c > 0 ? add2(r, v[d]) : sub2(r, v[d]);
     first = false;
   }
   return r;
@@ -449,9 +441,9 @@ __device__ __forceinline__ float2 cdotf2(int q, const float2 v[3]) {
 // A = 4.5 - 6.75 u^2 and B = 3 - 4.5 u^2 formed once a node
 __device__ __forceinline__ void poly_pair2(float2 cu, float2 A, float2 B, float2 common, float2& E,
                                            float2& O) {
-  const float2 c2 = f2mul(cu, cu);
-  E = f2fma(c2, f2fma(f2(3.375f), c2, A), common);
-  O = f2mul(cu, f2fma(f2(4.5f), c2, B));
+  const float2 c2 = mul2(cu, cu);
+  E = fma2(c2, fma2(bcast2(3.375f), c2, A), common);
+  O = mul2(cu, fma2(bcast2(4.5f), c2, B));
 }
 
 template <int D>
@@ -471,53 +463,53 @@ __device__ __forceinline__ void bgk_node2(const StepParams& p, uint32_t x, uint3
                                           float2 u[3]) {
   using L = Lattice<LAT>;
   using S = Storage<ST>;
-  float2 rhop = f2(0.0f), j[3] = {f2(0.0f), f2(0.0f), f2(0.0f)};
+  float2 rhop = bcast2(0.0f), j[3] = {bcast2(0.0f), bcast2(0.0f), bcast2(0.0f)};
 #pragma unroll
   for (int q = 0; q < L::Q; ++q) {
     const float is = 1.0f / S::template scale<LAT>(q);
-    rhop = f2fma(d[q], f2(is), rhop);
+    rhop = fma2(d[q], bcast2(is), rhop);
 #pragma unroll
     for (int k = 0; k < L::D; ++k) {
-      if (L::c(q, k) > 0) j[k] = f2fma(d[q], f2(is), j[k]);
-      if (L::c(q, k) < 0) j[k] = f2fma(d[q], f2(-is), j[k]);
+      if (L::c(q, k) > 0) j[k] = fma2(d[q], bcast2(is), j[k]);
+      if (L::c(q, k) < 0) j[k] = fma2(d[q], bcast2(-is), j[k]);
     }
   }
-  const float2 rho = f2add(f2(1.0f), rhop);
+  const float2 rho = add2(bcast2(1.0f), rhop);
   const float2 irho = make_float2(1.0f / rho.x, 1.0f / rho.y);
 #pragma unroll
-  for (int k = 0; k < 3; ++k) u[k] = f2mul(j[k], irho);
-  float2 F[3] = {f2(0.0f), f2(0.0f), f2(0.0f)};
+  for (int k = 0; k < 3; ++k) u[k] = mul2(j[k], irho);
+  float2 F[3] = {bcast2(0.0f), bcast2(0.0f), bcast2(0.0f)};
   if (FS != FS_NONE) node_force_float2<L::D>(p, x, y, z0, z1, F);
-  float2 u2 = f2mul(u[0], u[0]);
+  float2 u2 = mul2(u[0], u[0]);
 #pragma unroll
-  for (int k = 1; k < L::D; ++k) u2 = f2fma(u[k], u[k], u2);
-  const float2 common = f2mul(u2, f2fma(f2(1.125f), u2, f2(-1.5f)));
-  const float2 A = f2fma(f2(-6.75f), u2, f2(4.5f));
-  const float2 B = f2fma(f2(-4.5f), u2, f2(3.0f));
-  const float2 b = f2(p.bgk_b_f);
-  float2 uF = f2(0.0f), v[3] = {f2(0.0f), f2(0.0f), f2(0.0f)};
+  for (int k = 1; k < L::D; ++k) u2 = fma2(u[k], u[k], u2);
+  const float2 common = mul2(u2, fma2(bcast2(1.125f), u2, bcast2(-1.5f)));
+  const float2 A = fma2(bcast2(-6.75f), u2, bcast2(4.5f));
+  const float2 B = fma2(bcast2(-4.5f), u2, bcast2(3.0f));
+  const float2 b = bcast2(p.bgk_b_f);
+  float2 uF = bcast2(0.0f), v[3] = {bcast2(0.0f), bcast2(0.0f), bcast2(0.0f)};
   float2 commonv = common, Av = A, Bv = B;
   if (FS == FS_GUO) {
-    uF = f2mul(u[0], F[0]);
+    uF = mul2(u[0], F[0]);
 #pragma unroll
-    for (int k = 1; k < L::D; ++k) uF = f2fma(u[k], F[k], uF);
+    for (int k = 1; k < L::D; ++k) uF = fma2(u[k], F[k], uF);
   }
   if (FS == FS_EDM) {
 #pragma unroll
-    for (int k = 0; k < 3; ++k) v[k] = f2fma(F[k], irho, u[k]);
-    float2 v2 = f2mul(v[0], v[0]);
+    for (int k = 0; k < 3; ++k) v[k] = fma2(F[k], irho, u[k]);
+    float2 v2 = mul2(v[0], v[0]);
 #pragma unroll
-    for (int k = 1; k < L::D; ++k) v2 = f2fma(v[k], v[k], v2);
-    commonv = f2mul(v2, f2fma(f2(1.125f), v2, f2(-1.5f)));
-    Av = f2fma(f2(-6.75f), v2, f2(4.5f));
-    Bv = f2fma(f2(-4.5f), v2, f2(3.0f));
+    for (int k = 1; k < L::D; ++k) v2 = fma2(v[k], v[k], v2);
+    commonv = mul2(v2, fma2(bcast2(1.125f), v2, bcast2(-1.5f)));
+    Av = fma2(bcast2(-6.75f), v2, bcast2(4.5f));
+    Bv = fma2(bcast2(-4.5f), v2, bcast2(3.0f));
   }
   {  // rest population
     const float ws = (float)L::w(0) * S::template scale<LAT>(0);
-    const float2 deq = f2mul(f2(ws), f2fma(rho, common, rhop));
-    float2 r = f2fma(b, f2sub(deq, d[0]), d[0]);
-    if (FS == FS_GUO) r = f2fma(f2(-(p.guo_kt_f * ws)), uF, r);
-    if (FS == FS_EDM) r = f2fma(f2mul(f2(ws), rho), f2sub(commonv, common), r);
+    const float2 deq = mul2(bcast2(ws), fma2(rho, common, rhop));
+    float2 r = fma2(b, sub2(deq, d[0]), d[0]);
+    if (FS == FS_GUO) r = fma2(bcast2(-(p.guo_kt_f * ws)), uF, r);
+    if (FS == FS_EDM) r = fma2(mul2(bcast2(ws), rho), sub2(commonv, common), r);
     d[0] = r;
   }
 #pragma unroll
@@ -528,23 +520,23 @@ __device__ __forceinline__ void bgk_node2(const StepParams& p, uint32_t x, uint3
       const float2 cu = cdotf2<LAT>(q, u);
       float2 E, O;
       poly_pair2(cu, A, B, common, E, O);
-      const float2 dq = f2mul(f2(ws), f2fma(rho, f2add(E, O), rhop));
-      const float2 dqb = f2mul(f2(ws), f2fma(rho, f2sub(E, O), rhop));
-      float2 rq = f2fma(b, f2sub(dq, d[q]), d[q]);
-      float2 rqb = f2fma(b, f2sub(dqb, d[qb]), d[qb]);
+      const float2 dq = mul2(bcast2(ws), fma2(rho, add2(E, O), rhop));
+      const float2 dqb = mul2(bcast2(ws), fma2(rho, sub2(E, O), rhop));
+      float2 rq = fma2(b, sub2(dq, d[q]), d[q]);
+      float2 rqb = fma2(b, sub2(dqb, d[qb]), d[qb]);
       if (FS == FS_GUO) {
         const float2 cF = cdotf2<LAT>(q, F);
-        const float2 Es = f2fma(f2mul(f2(3.0f), cu), cF, make_float2(-uF.x, -uF.y));
-        const float2 kw = f2(p.guo_kt_f * ws);
-        rq = f2fma(kw, f2add(Es, cF), rq);
-        rqb = f2fma(kw, f2sub(Es, cF), rqb);
+        const float2 Es = fma2(mul2(bcast2(3.0f), cu), cF, neg2(uF));
+        const float2 kw = bcast2(p.guo_kt_f * ws);
+        rq = fma2(kw, add2(Es, cF), rq);
+        rqb = fma2(kw, sub2(Es, cF), rqb);
       }
       if (FS == FS_EDM) {
         float2 Ev, Ov;
         poly_pair2(cdotf2<LAT>(q, v), Av, Bv, commonv, Ev, Ov);
-        const float2 wr = f2mul(f2(ws), rho);
-        rq = f2fma(wr, f2sub(f2add(Ev, Ov), f2add(E, O)), rq);
-        rqb = f2fma(wr, f2sub(f2sub(Ev, Ov), f2sub(E, O)), rqb);
+        const float2 wr = mul2(bcast2(ws), rho);
+        rq = fma2(wr, sub2(add2(Ev, Ov), add2(E, O)), rq);
+        rqb = fma2(wr, sub2(sub2(Ev, Ov), sub2(E, O)), rqb);
       }
       d[q] = rq;
       d[qb] = rqb;
@@ -913,108 +905,165 @@ __device__ __forceinline__ HLowp<LAT, ST, SERIES> make_entropy_eval(const Pulled
 // both as double-float sums (TwoSum on the running high part), rounded once
 // to FP64 at the end. M3..M8 as in make_entropy_eval (FP32 sums in tier A,
 // M3 and M4 in FP64 in tier B). The error bound is series_error_bound.
+// One population's terms of make_series_dfl in the lanes of float pairs:
+// lane x and lane y are two populations of the same weight (exponent d
+// offsets and table constants alike), each lane the scalar sequence of
+// operations, the sums kept per lane.
+struct SeriesAcc2 {
+  float2 bh, bl, eh, el, mh, ml, M3f, M4f, M5, M6, M7, M8;
+};
+
+template <int LAT>
+__device__ __forceinline__ void series_terms2(float2 f, dfl2 n, int expw, const LogEntryFineF* fine,
+                                              float2 C, bool tierB, SeriesAcc2& a, double& M3,
+                                              double& M4) {
+  constexpr bool kUniform = uniform_weight_significand<LAT>();
+  const uint32_t bx = __float_as_uint(f.x), by = __float_as_uint(f.y);
+  const int dx = (int)((bx >> 23) & 0xffu) - (127 + expw);
+  const int dy = (int)((by >> 23) & 0xffu) - (127 + expw);
+  const LogEntryFineF tx = fine[(bx >> 13) & (LOG_TABLE_FINE - 1)];
+  const LogEntryFineF ty = fine[(by >> 13) & (LOG_TABLE_FINE - 1)];
+  const float2 m = make_float2(__uint_as_float((bx & 0x7fffffu) | 0x3f800000u),
+                               __uint_as_float((by & 0x7fffffu) | 0x3f800000u));
+  const float2 inv = make_float2(tx.inv, ty.inv);
+  const float2 thi = make_float2(tx.hi, ty.hi), tlo = make_float2(tx.lo, ty.lo);
+  const float2 pr = mul2(m, inv);
+  const float2 pe = fma2(m, inv, neg2(pr));
+  const float2 pm1 = sub2(pr, bcast2(1.0f));
+  const float2 rp = add2(pm1, pe);
+  const float2 tail = mul2(mul2(rp, rp),
+                           fma2(rp, fma2(rp, bcast2(-0.25f), bcast2(1.0f / 3.0f)), bcast2(-0.5f)));
+  float2 Lh, Le, lo;
+  if constexpr (kUniform) {
+    two_sum2(thi, pm1, Lh, Le);
+    lo = add2(add2(add2(tlo, Le), pe), tail);
+  } else {
+    const float2 Cx = bcast2(C.x), Cy = bcast2(C.y);
+    float2 s1, e1;
+    two_sum2(Cx, thi, s1, e1);
+    two_sum2(s1, pm1, Lh, Le);
+    lo = add2(add2(add2(add2(add2(Cy, tlo), e1), Le), pe), tail);
+  }
+  {  // B1 += f_neq ln(f/w)
+    const float2 tp = mul2(n.hi, Lh);
+    float2 te = fma2(n.hi, Lh, neg2(tp));
+    te = fma2(n.hi, lo, fma2(n.lo, Lh, te));
+    float2 e3;
+    two_sum2(a.bh, tp, a.bh, e3);
+    a.bl = add2(a.bl, add2(e3, te));
+  }
+  {  // sum_q d_q f_neq_q
+    const float2 dd = sub2(make_float2(__int_as_float(0x4B400000 + dx), __int_as_float(0x4B400000 + dy)),
+                           bcast2(12582912.0f));
+    const float2 tp = mul2(n.hi, dd);
+    const float2 te = fma2(n.lo, dd, fma2(n.hi, dd, neg2(tp)));
+    float2 e3;
+    two_sum2(a.eh, tp, a.eh, e3);
+    a.el = add2(a.el, add2(e3, te));
+  }
+  const float2 y0 = make_float2(rcp_sfu(f.x), rcp_sfu(f.y));
+  const float2 ee = fma2(neg2(f), y0, bcast2(1.0f));
+  {  // M2 += f_neq^2 y0 (1 + e)
+    const float2 sq = mul2(n.hi, n.hi);
+    const float2 sqe = fma2(mul2(bcast2(2.0f), n.hi), n.lo, fma2(n.hi, n.hi, neg2(sq)));
+    const float2 tq = mul2(sq, y0);
+    float2 tqe = fma2(sq, y0, neg2(tq));
+    tqe = fma2(tq, ee, fma2(sqe, y0, tqe));
+    float2 e4;
+    two_sum2(a.mh, tq, a.mh, e4);
+    a.ml = add2(a.ml, add2(e4, tqe));
+  }
+  const float2 rf = mul2(n.hi, y0);
+  float2 tt = mul2(n.hi, mul2(rf, rf));  // f r^3
+  if (tierB) {
+    const double nqx = widen_exact(n.hi.x) + widen_exact(n.lo.x);
+    const double nqy = widen_exact(n.hi.y) + widen_exact(n.lo.y);
+    const double gx = nqx * fma(widen_exact(y0.x), widen_exact(ee.x), widen_exact(y0.x));
+    const double gy = nqy * fma(widen_exact(y0.y), widen_exact(ee.y), widen_exact(y0.y));
+    const double p2x = gx * nqx, p2y = gy * nqy;
+    M3 = fma(p2x, gx, M3);
+    M4 = fma(p2x * gx, gx, M4);
+    M3 = fma(p2y, gy, M3);
+    M4 = fma(p2y * gy, gy, M4);
+  } else {
+    a.M3f = add2(a.M3f, tt);
+    a.M4f = fma2(tt, rf, a.M4f);
+  }
+  tt = mul2(tt, mul2(rf, rf));
+  a.M5 = add2(a.M5, tt);  // f r^5
+  tt = mul2(tt, rf);
+  a.M6 = add2(a.M6, tt);
+  tt = mul2(tt, rf);
+  a.M7 = add2(a.M7, tt);
+  tt = mul2(tt, rf);
+  a.M8 = add2(a.M8, tt);
+}
+
+// The moment-series coefficients of an FP32-storage node from f_neq in
+// double-float form, with no FP64 arithmetic in the population loop:
+//   B1 = sum_q f_neq_q ln(f_q/w_q), ln(f/w) = d ln2 - ln(m_q) + ln(1/inv_j)
+//        + log1p(r'), r' = m inv_j - 1 (m the float mantissa of f, exact as
+//        RN(m inv_j) - 1 plus the FMA residual), log1p(r') = r' + r'^2 (r'/3
+//        - 1/2 - r'/4) with the tail in FP32; the d ln2 parts accumulate as
+//        sum_q d_q f_neq_q, and on lattices with one weight significand the
+//        -ln(m_q) parts cancel (sum_q f_neq_q = 0);
+//   M2 = sum_q f_neq_q^2 / f_q with 1/f = y0 (1 + e), y0 the SFU reciprocal,
+//        e = 1 - f y0 from one FMA;
+// both as double-float sums (TwoSum on the running high part), rounded once
+// to FP64 at the end. M3..M8 as in make_entropy_eval (FP32 sums in tier A,
+// M3 and M4 in FP64 in tier B). The pair (q, opposite(q)) of each leader runs
+// in the two lanes of packed FP32x2 instructions (series_terms2), the rest
+// population in lane x ahead of the first pair; the lanes' sums are added at
+// the end (two more double-float additions in the error bound). The error
+// bound is series_error_bound.
 template <int LAT>
 __device__ __forceinline__ HSeries make_series_dfl(const Pulled<LAT, ST_F32>& P, const dfl nd[],
                                                    float nfr[], float rabs,
                                                    const LogEntryFineF* fine,
                                                    const float2* mconst) {
   using L = Lattice<LAT>;
-  constexpr bool kUniform = uniform_weight_significand<LAT>();
   const bool tierB = rabs > kSeriesTierA;
-  float bh = 0.0f, bl = 0.0f;  // B1 without the exponent parts
-  float eh = 0.0f, el = 0.0f;  // sum_q d_q f_neq_q
-  float mh = 0.0f, ml = 0.0f;  // M2
+  SeriesAcc2 a;
+  a.bh = a.bl = a.eh = a.el = a.mh = a.ml = bcast2(0.0f);
+  a.M3f = a.M4f = a.M5 = a.M6 = a.M7 = a.M8 = bcast2(0.0f);
   double M3 = 0.0, M4 = 0.0;
-  float M3f = 0.0f, M4f = 0.0f, M5 = 0.0f, M6 = 0.0f, M7 = 0.0f, M8 = 0.0f;
-#pragma unroll
-  for (int q = 0; q < L::Q; ++q) {
-    const float f = P.v[q];
-    const dfl n = nd[q];
-    nfr[q] = n.hi;
-    // ln(f/w) without d ln2: -ln(m_q) + ln(1/inv_j) + log1p(r')
-    const uint32_t b = __float_as_uint(f);
-    const int d = (int)((b >> 23) & 0xffu) - (127 + exponent_of(L::w(q)));
-    const LogEntryFineF t = fine[(b >> 13) & (LOG_TABLE_FINE - 1)];
-    const float m = __uint_as_float((b & 0x7fffffu) | 0x3f800000u);
-    const float pr = __fmul_rn(m, t.inv);
-    const float pe = __fmaf_rn(m, t.inv, -pr);  // exact residual of the product
-    const float pm1 = __fsub_rn(pr, 1.0f);      // exact (pr within 2^-10 of 1)
-    const float rp = __fadd_rn(pm1, pe);
-    const float tail = __fmul_rn(__fmul_rn(rp, rp),
-                                 __fmaf_rn(rp, __fmaf_rn(rp, -0.25f, 1.0f / 3.0f), -0.5f));
-    float Lh, Le, lo;
-    if constexpr (kUniform) {
-      two_sum(t.hi, pm1, Lh, Le);
-      lo = __fadd_rn(__fadd_rn(__fadd_rn(t.lo, Le), pe), tail);
-    } else {
-      const float2 C = mconst[q];
-      float s1, e1;
-      two_sum(C.x, t.hi, s1, e1);
-      two_sum(s1, pm1, Lh, Le);
-      lo = __fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(C.y, t.lo), e1), Le), pe), tail);
-    }
-    // B1 += f_neq ln(f/w) (double-float product and sum)
-    {
-      const float tp = __fmul_rn(n.hi, Lh);
-      float te = __fmaf_rn(n.hi, Lh, -tp);
-      te = __fmaf_rn(n.hi, lo, __fmaf_rn(n.lo, Lh, te));
-      float e3;
-      two_sum(bh, tp, bh, e3);
-      bl = __fadd_rn(bl, __fadd_rn(e3, te));
-    }
-    // the exponent part: sum_q d_q f_neq_q (d small; the product's residual
-    // by FMA)
-    {
-      const float dd = __fsub_rn(__int_as_float(0x4B400000 + d), 12582912.0f);  // (float)d
-      const float tp = __fmul_rn(n.hi, dd);
-      const float te = __fmaf_rn(n.lo, dd, __fmaf_rn(n.hi, dd, -tp));
-      float e3;
-      two_sum(eh, tp, eh, e3);
-      el = __fadd_rn(el, __fadd_rn(e3, te));
-    }
-    // M2 += f_neq^2 y0 (1 + e)
-    const float y0 = rcp_sfu(f);
-    const float ee = __fmaf_rn(-f, y0, 1.0f);
-    {
-      const float sq = __fmul_rn(n.hi, n.hi);
-      const float sqe = __fmaf_rn(2.0f * n.hi, n.lo, __fmaf_rn(n.hi, n.hi, -sq));
-      const float tq = __fmul_rn(sq, y0);
-      float tqe = __fmaf_rn(sq, y0, -tq);
-      tqe = __fmaf_rn(tq, ee, __fmaf_rn(sqe, y0, tqe));
-      float e4;
-      two_sum(mh, tq, mh, e4);
-      ml = __fadd_rn(ml, __fadd_rn(e4, tqe));
-    }
-    // higher moments
-    const float rf = n.hi * y0;
-    float tt = n.hi * (rf * rf);  // f r^3
-    if (tierB) {
-      const double nq = widen_exact(n.hi) + widen_exact(n.lo);
-      const double y = widen_exact(y0);
-      const double g = nq * fma(y, widen_exact(ee), y);  // r_q
-      const double p2 = g * nq;
-      M3 = fma(p2, g, M3);
-      M4 = fma(p2 * g, g, M4);
-    } else {
-      M3f += tt;
-      M4f = fmaf(tt, rf, M4f);
-    }
-    tt *= rf * rf; M5 += tt;  // f r^5
-    tt *= rf; M6 += tt;
-    tt *= rf; M7 += tt;
-    tt *= rf; M8 += tt;
+  {
+    // the rest population in lane x, a zero term in lane y (f = 1, f_neq = 0:
+    // every product with it is an exact zero)
+    nfr[0] = nd[0].hi;
+    const dfl2 n2 = dfl2_pack(nd[0], dfl{0.0f, 0.0f});
+    series_terms2<LAT>(make_float2(P.v[0], 1.0f), n2, exponent_of(L::w(0)), fine, mconst[0],
+                       tierB, a, M3, M4);
   }
-  // B1 = (bh + bl) + ln2 (eh + el), M2 = mh + ml, each rounded once to FP64
-  dfl B{bh, bl}, E{eh, el}, M{mh, ml};
-  fast_two_sum(B.hi, B.lo, B.hi, B.lo);
-  fast_two_sum(E.hi, E.lo, E.hi, E.lo);
-  fast_two_sum(M.hi, M.lo, M.hi, M.lo);
+#pragma unroll
+  for (int q = 1; q < L::Q; ++q) {
+    if (!is_pair_leader<LAT>(q)) continue;
+    const int qb = opposite<LAT>(q);
+    nfr[q] = nd[q].hi;
+    nfr[qb] = nd[qb].hi;
+    series_terms2<LAT>(make_float2(P.v[q], P.v[qb]), dfl2_pack(nd[q], nd[qb]),
+                       exponent_of(L::w(q)), fine, mconst[q], tierB, a, M3, M4);
+  }
+  // B1 = (bh + bl) + ln2 (eh + el), M2 = mh + ml, over both lanes, each
+  // rounded once to FP64
+  auto lanes = [](float2 h, float2 l) {
+    dfl x{h.x, l.x}, y{h.y, l.y};
+    fast_two_sum(x.hi, x.lo, x.hi, x.lo);
+    fast_two_sum(y.hi, y.lo, y.hi, y.lo);
+    return dfl_add(x, y);
+  };
+  dfl B = lanes(a.bh, a.bl), E = lanes(a.eh, a.el), M = lanes(a.mh, a.ml);
   constexpr float kLn2F = 0x1.62e43p-1f;                  // RN_float(ln 2)
   constexpr float kLn2FLo = -0x1.05c610p-29f;             // ln 2 - kLn2F
   B = dfl_add(B, dfl_mul(E, dfl{kLn2F, kLn2FLo}));
   const double B1 = dfl_to_double(B);
   const double M2 = dfl_to_double(M);
-  if (!tierB) { M3 = widen_exact(M3f); M4 = widen_exact(M4f); }
+  if (!tierB) {
+    M3 = widen_exact(a.M3f.x + a.M3f.y);
+    M4 = widen_exact(a.M4f.x + a.M4f.y);
+  }
+  const float M5 = a.M5.x + a.M5.y, M6 = a.M6.x + a.M6.y, M7 = a.M7.x + a.M7.y,
+              M8 = a.M8.x + a.M8.y;
   return HSeries{B1, M2 * 0.5, M3 * (1.0 / 6.0), M4 * (1.0 / 12.0), M2, M3 * 0.5,
                  M4 * (1.0 / 3.0), M5 * (1.0f / 20.0f), M6 * (1.0f / 30.0f),
                  M7 * (1.0f / 42.0f), M8 * (1.0f / 56.0f), M5 * 0.25f, M6 * 0.2f,
@@ -1112,11 +1161,32 @@ __device__ __forceinline__ void neq_pairs(const Pulled<LAT, ST>& P, double rho, 
   }
 }
 
+// The pair leaders of a lattice in population order (pairs (q, opposite(q))).
+template <int LAT>
+struct PairIndex {
+  static constexpr int count() {
+    int c = 0;
+    for (int q = 1; q < Lattice<LAT>::Q; ++q) c += is_pair_leader<LAT>(q) ? 1 : 0;
+    return c;
+  }
+  static constexpr int leader(int k) {
+    int c = 0;
+    for (int q = 1; q < Lattice<LAT>::Q; ++q) {
+      if (!is_pair_leader<LAT>(q)) continue;
+      if (c == k) return q;
+      ++c;
+    }
+    return 0;
+  }
+};
+
 // f_neq in double-float arithmetic (dfloat.cuh) for FP32 storage: the same
 // pair form as neq_pairs, each operation on (hi, lo) float pairs, the result
 // rounded once to FP64. Error: a few 2^-48 of rho w_q (1 + |P_q|) a
 // population (bounded in series_error_bound), from ~20x fewer FP64-pipe
-// cycles than the FP64 form.
+// cycles than the FP64 form. Two pairs run at a time in packed FP32x2 lanes
+// (dfl2): each lane performs the scalar sequence of operations, so the
+// values are those of the one-pair-at-a-time form.
 template <int LAT>
 __device__ __forceinline__ void neq_pairs_dfl(const Pulled<LAT, ST_F32>& P, double rho,
                                               const double u[3], dfl n[]) {
@@ -1135,33 +1205,57 @@ __device__ __forceinline__ void neq_pairs_dfl(const Pulled<LAT, ST_F32>& P, doub
     const float wl = (float)(L::w(q) - (double)wh);
     return dfl_mul(r, dfl{wh, wl});
   };
+  auto cu_of = [&](int q) {
+    dfl cu{0.0f, 0.0f};
+    bool first = true;
+#pragma unroll
+    for (int k = 0; k < L::D; ++k) {
+      if (L::c(q, k) == 0) continue;
+      const dfl t = L::c(q, k) > 0 ? uv[k] : dfl_neg(uv[k]);
+      cu = first ? t : dfl_add(cu, t);
+      first = false;
+    }
+    return cu;
+  };
   {
     const dfl rw = rw_of(0);
     const dfl feq = dfl_add(rw, dfl_mul(rw, common));
     n[0] = dfl_add_f(dfl_neg(feq), P.v[0]);
   }
+  constexpr int NP = PairIndex<LAT>::count();
+  const dfl2 common2 = dfl2_pack(common, common), A2 = dfl2_pack(A, A), B2 = dfl2_pack(B, B);
 #pragma unroll
-  for (int q = 1; q < L::Q; ++q) {
-    if (is_pair_leader<LAT>(q)) {
-      const int qb = opposite<LAT>(q);
-      dfl cu{0.0f, 0.0f};
-      bool first = true;
-#pragma unroll
-      for (int k = 0; k < L::D; ++k) {
-        if (L::c(q, k) == 0) continue;
-        const dfl t = L::c(q, k) > 0 ? uv[k] : dfl_neg(uv[k]);
-        cu = first ? t : dfl_add(cu, t);
-        first = false;
-      }
-      const dfl c2 = dfl_mul(cu, cu);
-      const dfl E = dfl_add(dfl_mul(c2, dfl_add(dfl_mul_f(c2, 3.375f), A)), common);
-      const dfl O = dfl_mul(cu, dfl_add(dfl_mul_f(c2, 4.5f), B));
-      const dfl rw = rw_of(q);
-      const dfl A1 = dfl_add(rw, dfl_mul(rw, E));  // rho w (1 + E)
-      const dfl B1 = dfl_mul(rw, O);               // rho w O
-      n[q] = dfl_sub(dfl_add_f(dfl_neg(A1), P.v[q]), B1);
-      n[qb] = dfl_add(dfl_add_f(dfl_neg(A1), P.v[qb]), B1);
-    }
+  for (int k = 0; k + 1 < NP; k += 2) {
+    const int qa = PairIndex<LAT>::leader(k), qb = PairIndex<LAT>::leader(k + 1);
+    const dfl2 cu = dfl2_pack(cu_of(qa), cu_of(qb));
+    const dfl2 c2 = dfl2_mul(cu, cu);
+    const dfl2 E = dfl2_add(dfl2_mul(c2, dfl2_add(dfl2_mul_f(c2, bcast2(3.375f)), A2)), common2);
+    const dfl2 O = dfl2_mul(cu, dfl2_add(dfl2_mul_f(c2, bcast2(4.5f)), B2));
+    const dfl2 rw = dfl2_pack(rw_of(qa), rw_of(qb));
+    const dfl2 A1 = dfl2_add(rw, dfl2_mul(rw, E));  // rho w (1 + E)
+    const dfl2 B1 = dfl2_mul(rw, O);                // rho w O
+    const dfl2 nA = dfl2_add_f(dfl2_neg(A1), make_float2(P.v[qa], P.v[qb]));
+    const dfl2 nAb = dfl2_add_f(dfl2_neg(A1),
+                                make_float2(P.v[opposite<LAT>(qa)], P.v[opposite<LAT>(qb)]));
+    const dfl2 np = dfl2_sub(nA, B1);
+    const dfl2 nm = dfl2_add(nAb, B1);
+    n[qa] = dfl2_x(np);
+    n[qb] = dfl2_y(np);
+    n[opposite<LAT>(qa)] = dfl2_x(nm);
+    n[opposite<LAT>(qb)] = dfl2_y(nm);
+  }
+  if constexpr (NP % 2 == 1) {
+    const int q = PairIndex<LAT>::leader(NP - 1);
+    const int qb = opposite<LAT>(q);
+    const dfl cu = cu_of(q);
+    const dfl c2 = dfl_mul(cu, cu);
+    const dfl E = dfl_add(dfl_mul(c2, dfl_add(dfl_mul_f(c2, 3.375f), A)), common);
+    const dfl O = dfl_mul(cu, dfl_add(dfl_mul_f(c2, 4.5f), B));
+    const dfl rw = rw_of(q);
+    const dfl A1 = dfl_add(rw, dfl_mul(rw, E));
+    const dfl B1 = dfl_mul(rw, O);
+    n[q] = dfl_sub(dfl_add_f(dfl_neg(A1), P.v[q]), B1);
+    n[qb] = dfl_add(dfl_add_f(dfl_neg(A1), P.v[qb]), B1);
   }
 }
 
