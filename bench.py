@@ -570,7 +570,9 @@ def run_ours(args):
                 if peak_src == "measured" else "fallback 6.8 TB/s",
                 "bytes_per_node": bpn, "kernel": "elbm_lowp_kernel" if entropic else
                 (("bgk_f64x_kernel" if w.get("fp64Arithmetic") == "fixed" else "bgk_f64_kernel")
-                 if w["storage"] == "f64" else "bgk_lowp_kernel"),
+                 if w["storage"] == "f64" else
+                 ("bgk_f16_pair_kernel" if w["storage"].startswith("f16") and deck_l.shape[2] % 2 == 0
+                  else "bgk_lowp_kernel")),
                 "traffic_source": prof.get("source")}
     if "fp64_inst_per_node" in prof:
         # the kernel's binding roof: GB300's FP64 pipe (no FP64 figure in

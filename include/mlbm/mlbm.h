@@ -115,9 +115,12 @@ enum { MLBM_ALPHA_REFERENCE = 0, MLBM_ALPHA_RESIDUAL = 1 };
  * (the reference, Algorithm.h:103-106), the constant 2, or the learned model
  * installed with mlbm_set_alpha_model. LEARNED runs the model where a node has
  * no solved alpha from the previous step (its stored alpha is exactly 2:
- * after mlbm_init_equilibrium, a restart, or an alpha = 2 fallback) and takes
- * the previous alpha elsewhere; LEARNED_EVERYWHERE runs the model at every
- * solved node. Both need FP32 / FP16 storage. */
+ * after mlbm_init_equilibrium, mlbm_set_alpha, or an alpha = 2 fallback) and
+ * takes the previous alpha elsewhere; an mlbm_step call that starts with no
+ * such node runs kernels without the network (a node that falls back to
+ * alpha = 2 during that call takes the constant 2 until the next call).
+ * LEARNED_EVERYWHERE runs the model at every solved node. Both need FP32 /
+ * FP16 storage. */
 enum { MLBM_GUESS_PREVIOUS = 0, MLBM_GUESS_TWO = 1, MLBM_GUESS_LEARNED = 2,
        MLBM_GUESS_LEARNED_EVERYWHERE = 3 };
 

@@ -73,7 +73,11 @@ struct mlbm_handle {
   int main_blocks = 0;          // blocks of the (first) step kernel
   // entropic FP32/FP16 step: second-pass worklist
   unsigned* defer_list = nullptr;
-  unsigned* defer_count = nullptr;
+  unsigned* defer_count = nullptr;  // [2] worklist lengths, [2] cold-node flags (by parity)
+  // learned guess: nodes without a solved alpha may exist (after init, a
+  // restart, set_alpha, or a step that stored alpha = 2)
+  bool alpha_cold = true;
+  bool learned_now = false;  // the steps being enqueued run the network
   int defer_blocks = 0;
   double* diag_dev = nullptr;
   unsigned long long* counters = nullptr;
@@ -382,6 +386,7 @@ static double host_sin_profile(double amplitude, unsigned i, double lambda) {
 }
 
 static int fill_alpha(mlbm_handle* h, double value) {
+  h->alpha_cold = true;
   cudaError_t e = fill_alpha_field(h->alpha, h->alpha32, h->V, value, h->stream);
   count_launches(1);
   if (e != cudaSuccess) return fail(h, MLBM_ERR_CUDA, "alpha fill: %s", cudaGetErrorString(e));
@@ -514,9 +519,9 @@ extern "C" int mlbm_create(const mlbm_config* cfg, mlbm_handle** out) {
     h->defer_blocks = 2 * sms;
     h->partial_blocks += h->defer_blocks;
     if ((rc = device_alloc(h, (void**)&h->defer_list, sizeof(unsigned) * (size_t)V)) ||
-        (rc = device_alloc(h, (void**)&h->defer_count, 2 * sizeof(unsigned))))
+        (rc = device_alloc(h, (void**)&h->defer_count, 4 * sizeof(unsigned))))
       return bail(rc);
-    cudaMemsetAsync(h->defer_count, 0, 2 * sizeof(unsigned), h->stream);
+    cudaMemsetAsync(h->defer_count, 0, 4 * sizeof(unsigned), h->stream);
   }
   if ((rc = device_alloc(h, (void**)&h->partials,
                          sizeof(double) * DIAG_FIELDS *
@@ -660,6 +665,7 @@ extern "C" int mlbm_create(const mlbm_config* cfg, mlbm_handle** out) {
   p.log_table_fine = h->log_table_fine;
   p.defer_list = h->defer_list;
   p.defer_count = h->defer_count;
+  p.cold_flags = h->defer_count ? h->defer_count + 2 : nullptr;
   p.defer_blocks = h->defer_blocks;
   p.defer_slot0 = h->main_blocks;
 
@@ -749,7 +755,35 @@ extern "C" int mlbm_get_populations(mlbm_handle* h, double* f, int layout) {
 
 static int enqueue_step(mlbm_handle* h, bool last, unsigned int flags, bool in_place);
 
+// MLBM_GUESS_LEARNED: the network runs where a node has no solved alpha from
+// the previous step. Whether any node of the lattice is in that state is
+// known on the host after initialisation and set_alpha, and from the
+// cold-node flag the previous step's kernels set on the device; a call that
+// starts with none runs the kernels without the network (they take the
+// previous alpha everywhere, and a node that falls back to alpha = 2 during
+// the call takes the constant 2 until the next call). LEARNED_EVERYWHERE
+// always runs the network.
+static int choose_learned_kernel(mlbm_handle* h) {
+  h->learned_now = false;
+  if (h->cfg.collision == MLBM_BGK || h->storage == MLBM_STORAGE_F64) return MLBM_OK;
+  if (h->cfg.alpha_guess == MLBM_GUESS_LEARNED_EVERYWHERE) {
+    h->learned_now = true;
+    return MLBM_OK;
+  }
+  if (h->cfg.alpha_guess != MLBM_GUESS_LEARNED) return MLBM_OK;
+  if (!h->alpha_cold && h->steps > 0 && h->defer_count) {
+    unsigned flag = 0;
+    MLBM_CUDA(h, cudaMemcpy(&flag, h->defer_count + 2 + ((h->steps - 1) & 1), sizeof flag,
+                            cudaMemcpyDeviceToHost));
+    h->alpha_cold = flag != 0;
+  }
+  h->learned_now = h->alpha_cold;
+  h->alpha_cold = false;  // the flags of this call's steps report what they store
+  return MLBM_OK;
+}
+
 extern "C" int mlbm_step(mlbm_handle* h, int nsteps, unsigned int flags) {
+  int rc0;
   if (!h) return MLBM_ERR_INVALID;
   if (nsteps < 0) return fail(h, MLBM_ERR_INVALID, "negative step count");
   if (nsteps == 0) return MLBM_OK;
@@ -760,6 +794,7 @@ extern "C" int mlbm_step(mlbm_handle* h, int nsteps, unsigned int flags) {
       h->cfg.collision != MLBM_BGK && !h->have_model)
     return fail(h, MLBM_ERR_STATE, "learned alpha guess without a model (mlbm_set_alpha_model)");
   MLBM_CUDA(h, cudaSetDevice(h->cfg.device));
+  if ((rc0 = choose_learned_kernel(h))) return rc0;
   MLBM_CUDA(h, cudaMemsetAsync(h->counters, 0, sizeof(unsigned long long) * CNT_COUNT, h->stream));
   for (int s = 0; s < nsteps; ++s) {
     int rc = enqueue_step(h, s == nsteps - 1, flags, false);
@@ -777,6 +812,7 @@ static int enqueue_step(mlbm_handle* h, bool last, unsigned int flags, bool in_p
   {
     StepParams p = h->base;
     p.parity = (int)(h->steps & 1);
+    p.learned_kernel = h->learned_now ? 1 : 0;
     p.store = last && (flags & MLBM_STEP_STORE_FIELDS) ? 1 : 0;
     p.diag = last && (flags & MLBM_STEP_DIAGNOSTICS) ? 1 : 0;
     const void* prev = h->f[h->cur];
@@ -835,7 +871,13 @@ static int enqueue_step(mlbm_handle* h, bool last, unsigned int flags, bool in_p
 extern "C" int mlbm_testing_step_in_place(mlbm_handle* h) {
   if (!h) return MLBM_ERR_INVALID;
   MLBM_CUDA(h, cudaSetDevice(h->cfg.device));
-  return enqueue_step(h, true, 0u, true);
+  int rc = choose_learned_kernel(h);
+  if (rc) return rc;
+  rc = enqueue_step(h, true, 0u, true);
+  // its cold-node flag sits at the parity the next step reuses and clears:
+  // the next call decides from the host state instead
+  h->alpha_cold = true;
+  return rc;
 }
 
 extern "C" int mlbm_sync(mlbm_handle* h, int timeout_ms) {
@@ -973,6 +1015,7 @@ extern "C" int mlbm_set_alpha(mlbm_handle* h, const double* alpha, int layout) {
   if (!alpha || !valid_layout(layout)) return fail(h, MLBM_ERR_INVALID, "bad arguments");
   MLBM_CUDA(h, cudaSetDevice(h->cfg.device));
   MLBM_CUDA(h, cudaStreamSynchronize(h->stream));
+  h->alpha_cold = true;  // it may hold alpha = 2
   if (h->alpha) return upload(h, alpha, h->alpha, 1, layout);
   std::vector<double> ad((size_t)h->V);
   if (layout == MLBM_LAYOUT_DENSE) std::memcpy(ad.data(), alpha, sizeof(double) * h->V);

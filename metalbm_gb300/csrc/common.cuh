@@ -92,6 +92,11 @@ struct StepParams {
   unsigned* defer_list;      // [V] node indices
   unsigned* defer_count;     // [2] list lengths, used by alternating steps
   int parity;                // step number & 1
+  // learned guess: 1 when this step launches the kernels with the network;
+  // cold_flags[parity] is set when the step stores a node without a solved
+  // alpha (alpha exactly 2), cold_flags[parity ^ 1] cleared for the next step
+  int learned_kernel;
+  unsigned* cold_flags;
   int defer_blocks;          // grid of the second pass
   int defer_slot0;           // its first block's slot in diag_partials
 };

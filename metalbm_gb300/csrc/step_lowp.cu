@@ -1285,7 +1285,7 @@ __device__ __forceinline__ void elbm_node(const typename Storage<ST>::T* __restr
                                           const LogEntry* s_log, const LogEntryFine* s_fine,
                                           const double* s_lnw, const LogEntryFineF* s_finef,
                                           const float2* s_mconst, unsigned cnt[], bool& defer,
-                                          double& mass,
+                                          bool& cold, double& mass,
                                           double& energy, double& mach, double& amin,
                                           double& amax) {
   using L = Lattice<LAT>;
@@ -1473,6 +1473,7 @@ __device__ __forceinline__ void elbm_node(const typename Storage<ST>::T* __restr
     // absolute, so the previous alpha stays a guess to FP64 accuracy
     const float stored = narrow_rn(alpha - 2.0);
     p.alpha_field_f32[idx] = stored;
+    cold |= stored == 0.0f;
     if (p.diag) {
       const double a = 2.0 + widen_exact(stored);
       if (MODE == ELBM_MAIN) {  // one node a thread: no FP64 compares
@@ -1526,16 +1527,21 @@ __global__ void __launch_bounds__(128, LEARNED ? MLBM_ELBM_MIN_BLOCKS_LEARNED : 
     stage_log_table_fine(s_fine, s_lnw, reinterpret_cast<const LogEntryFine*>(p.log_table_fine));
   // the worklist counter of the next step (its last reader was the previous
   // step's second pass, which has completed)
-  if (blockIdx.x == 0 && threadIdx.x == 0) p.defer_count[p.parity ^ 1] = 0u;
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    p.defer_count[p.parity ^ 1] = 0u;
+    if (p.cold_flags) p.cold_flags[p.parity ^ 1] = 0u;
+  }
   __syncthreads();
   const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const bool active = idx < p.V;
   double mass = 0.0, energy = 0.0, mach = 0.0, amin = 1e300, amax = -1e300;
   unsigned cnt[CNT_COUNT] = {};
-  bool defer = false;
+  bool defer = false, cold = false;
   elbm_node<LAT, FS, ST, LEARNED, ELBM_MAIN>(prev, next, p, active, idx, nullptr, s_fine, s_lnw,
-                                             s_finef, s_mconst, cnt, defer, mass, energy, mach,
-                                             amin, amax);
+                                             s_finef, s_mconst, cnt, defer, cold, mass, energy,
+                                             mach, amin, amax);
+  if (p.cold_flags && __any_sync(0xffffffffu, cold) && (threadIdx.x & 31) == 0)
+    p.cold_flags[p.parity] = 1u;
   // warp-aggregated append to the worklist
   const unsigned m = __ballot_sync(0xffffffffu, defer);
   if (m) {
@@ -1560,6 +1566,7 @@ __global__ void __launch_bounds__(128) elbm_lowp_deferred_kernel(const typename 
   const long long count = (long long)p.defer_count[p.parity];
   double mass = 0.0, energy = 0.0, mach = 0.0, amin = 1e300, amax = -1e300;
   unsigned cnt[CNT_COUNT] = {};
+  bool cold = false;
   for (long long b = (long long)blockIdx.x * blockDim.x; b < count;
        b += (long long)gridDim.x * blockDim.x) {
     const long long i = b + threadIdx.x;
@@ -1567,9 +1574,11 @@ __global__ void __launch_bounds__(128) elbm_lowp_deferred_kernel(const typename 
     const long long idx = active ? (long long)p.defer_list[i] : 0;
     bool defer = false;
     elbm_node<LAT, FS, ST, LEARNED, ELBM_DEFERRED>(prev, next, p, active, idx, s_log, nullptr,
-                                                   nullptr, nullptr, nullptr, cnt, defer, mass,
-                                                   energy, mach, amin, amax);
+                                                   nullptr, nullptr, nullptr, cnt, defer, cold,
+                                                   mass, energy, mach, amin, amax);
   }
+  if (p.cold_flags && __any_sync(0xffffffffu, cold) && (threadIdx.x & 31) == 0)
+    p.cold_flags[p.parity] = 1u;
   add_counters(p.counters, cnt);
   if (p.diag)
     block_reduce_diag(0.0, 0.0, 0.0, amin, amax,
@@ -1787,7 +1796,7 @@ static cudaError_t launch_lowp(int collision, const void* prev, void* next, cons
   } else {
     const int bs = 128;
     const unsigned grid = (unsigned)((p.V + bs - 1) / bs);
-    if (p.guess_mode == GUESS_LEARNED || p.guess_mode == GUESS_LEARNED_EVERYWHERE) {
+    if (p.learned_kernel) {
       elbm_lowp_kernel<LAT, FS, ST, true><<<grid, bs, 0, s>>>((const T*)prev, (T*)next, p);
       elbm_lowp_deferred_kernel<LAT, FS, ST, true><<<p.defer_blocks, bs, 0, s>>>((const T*)prev, (T*)next, p);
     } else {
