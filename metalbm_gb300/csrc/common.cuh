@@ -236,6 +236,20 @@ __device__ __forceinline__ float narrow_rn(double x) {
   return __uint_as_float(bits | (hi & 0x80000000u));
 }
 
+// v 2^-k for an integer v (|v| < 2^63, 0 < k <= 60): one rounding (the
+// conversion), the scaling an exponent subtraction instead of an FP64 multiply.
+__device__ __forceinline__ double ll_scaled(long long v, int k) {
+  const double d = (double)v;
+  return v == 0 ? 0.0 : __longlong_as_double(__double_as_longlong(d) - ((long long)k << 52));
+}
+
+// x / 2 for a positive normal or zero double, exactly, by an exponent step
+// (values below 2^-1021 take the multiply).
+__device__ __forceinline__ double half_exact(double x) {
+  const long long b = __double_as_longlong(x);
+  return ((b >> 52) & 0x7ff) > 1 ? __longlong_as_double(b - (1LL << 52)) : x * 0.5;
+}
+
 // Order-preserving integer key of a double, so that maxima and minima are
 // integer operations (GB300 runs FP64 compares on its narrow FP64 path):
 // non-negative values keep their bit pattern, negative ones are mirrored.

@@ -1058,14 +1058,24 @@ __device__ __forceinline__ HSeries make_series_dfl(const Pulled<LAT, ST_F32>& P,
   B = dfl_add(B, dfl_mul(E, dfl{kLn2F, kLn2FLo}));
   const double B1 = dfl_to_double(B);
   const double M2 = dfl_to_double(M);
+  // the FP32 moments (tier A) scaled in FP32, M2 / 2 by an exponent step:
+  // no FP64 multiply
+  double a3, a4, b3, b4;
   if (!tierB) {
-    M3 = widen_exact(a.M3f.x + a.M3f.y);
-    M4 = widen_exact(a.M4f.x + a.M4f.y);
+    const float m3 = a.M3f.x + a.M3f.y, m4 = a.M4f.x + a.M4f.y;
+    a3 = widen_exact(m3 * (1.0f / 6.0f));
+    a4 = widen_exact(m4 * (1.0f / 12.0f));
+    b3 = widen_exact(m3 * 0.5f);
+    b4 = widen_exact(m4 * (1.0f / 3.0f));
+  } else {
+    a3 = M3 * (1.0 / 6.0);
+    a4 = M4 * (1.0 / 12.0);
+    b3 = M3 * 0.5;
+    b4 = M4 * (1.0 / 3.0);
   }
   const float M5 = a.M5.x + a.M5.y, M6 = a.M6.x + a.M6.y, M7 = a.M7.x + a.M7.y,
               M8 = a.M8.x + a.M8.y;
-  return HSeries{B1, M2 * 0.5, M3 * (1.0 / 6.0), M4 * (1.0 / 12.0), M2, M3 * 0.5,
-                 M4 * (1.0 / 3.0), M5 * (1.0f / 20.0f), M6 * (1.0f / 30.0f),
+  return HSeries{B1, half_exact(M2), a3, a4, M2, b3, b4, M5 * (1.0f / 20.0f), M6 * (1.0f / 30.0f),
                  M7 * (1.0f / 42.0f), M8 * (1.0f / 56.0f), M5 * 0.25f, M6 * 0.2f,
                  M7 * (1.0f / 6.0f), M8 * (1.0f / 7.0f)};
 }
@@ -1102,12 +1112,11 @@ __device__ __forceinline__ void moments_exact(const Pulled<LAT, ST>& P, double& 
     }
   }
   if (!bad) {
-    const double s = 0x1p-60;
-    const double Sd = (double)S * s;
+    const double Sd = ll_scaled(S, 60);
     rho = ST == ST_F32 ? Sd : 1.0 + Sd;
     rhop = ST == ST_F32 ? Sd - 1.0 : Sd;
 #pragma unroll
-    for (int k = 0; k < 3; ++k) j[k] = (double)J[k] * s;
+    for (int k = 0; k < 3; ++k) j[k] = ll_scaled(J[k], 60);
   } else {
     rho = P.f64(0);
     j[0] = j[1] = j[2] = 0.0;
