@@ -633,14 +633,17 @@ extern "C" int mlbm_create(const mlbm_config* cfg, mlbm_handle** out) {
     const double om = p.bgk_b;
     const int a = om < 0.5 ? 0 : (om < 1.5 ? 1 : 2);
     const double r = om - a;
-    p.fx_ok = std::fabs(r) <= 0.5 ? 1 : 0;
+    p.fx_ok = om > 0.0 && om < 2.0 ? 1 : 0;  // |1 - omega| < 1, |omega - a| <= 1/2
     p.fx_omega_a = a;
-    auto halves = [](double v, int out[2]) {
-      const long long x = std::llround(std::ldexp(v, 62));
+    auto split31 = [](long long x, int out[2]) {
       out[0] = (int)(x >> 31);
       out[1] = (int)(x & 0x7fffffffLL);
     };
+    auto halves = [&](double v, int out[2]) { split31(std::llround(std::ldexp(v, 62)), out); };
     halves(p.fx_ok ? r : 0.0, p.fx_omega_s31);
+    // (1 - omega) 2^62 = 2^62 - omega 2^62, exact in integers (omega 2^62 is
+    // an integer for omega >= 2^-9; smaller omega rounds once)
+    split31(p.fx_ok ? (1LL << 62) - std::llround(std::ldexp(om, 62)) : 0LL, p.fx_1mw_s31);
     for (int q = 0; q < h->Q; ++q) {
       const bool in = std::fabs(p.guo_k[q]) < 1.0;
       if (!in && c.forcing_scheme == MLBM_FORCING_GUO) p.fx_ok = 0;

@@ -61,11 +61,12 @@ struct StepParams {
   float guo_kt_f;            // (1 - 1/(2 tau)) 3; S_q = kt w_q [...]
   // FP64 BGK in fixed point (step_f64x.cu): omega = a + (omega - a) with
   // (omega - a) 2^62 as 31-bit halves (high, low), and
-  // ((1 - 1/(2 tau)) w_q inv_cs2) 2^62 likewise; fx_ok = 0 when
-  // |omega - a| > 1/2 or a Guo factor is not below 1 (the kernel's ranges)
+  // ((1 - 1/(2 tau)) w_q inv_cs2) 2^62 likewise; fx_ok = 0 when omega is
+  // outside (0, 2) or a Guo factor is not below 1 (the kernel's ranges)
   int fx_ok;
   int fx_omega_a;
   int fx_omega_s31[2];
+  int fx_1mw_s31[2];         // (1 - omega) 2^62 as 31-bit halves
   int fx_guo_s31[kMaxQ][2];
   // entropic solver
   int alpha_mode, guess_mode;

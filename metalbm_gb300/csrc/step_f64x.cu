@@ -18,9 +18,11 @@
 //     pair (q, -q) sharing the even and odd parts of 3 s + R_q;
 //   * Guo's source ((1 - 1/(2 tau)) w_q 3) [(c_q - u).F + 3 (c_q.u)(c_q.F)]
 //     (ForcingScheme.h:81-118);
-//   * f'_q 2^62 = 4 F_q + a T_q + (omega - a) T_q + S_q (T_q = f_eq_q - f_q,
-//     a the integer nearest omega), rounded once to FP64, to nearest even
-//     (the one FP64-pipe instruction a population).
+//   * f'_q 2^62 = (1 - omega) 4 F_q + Omega_q (1 + E_q +- O_q) + S_q for the
+//     moving populations (Omega_q = omega w_q rho, once per weight), and
+//     4 F_0 + a T_0 + (omega - a) T_0 + S_0 for the rest population (T_0 =
+//     f_eq_0 - f_0, a the integer nearest omega), rounded once to FP64, to
+//     nearest even (the one FP64-pipe instruction a population).
 // Every product is of two values below 2^62 in magnitude held as 31-bit
 // halves, (a_h 2^31 + a_l)(b_h 2^31 + b_l) 2^-62 = a_h b_h + (a_h b_l + a_l b_h)
 // 2^-31 with the product of the low halves dropped: three 32 x 32 -> 64-bit
@@ -228,16 +230,26 @@ __device__ __forceinline__ bool bgk_node_fixed(const double f[], const double F[
   }
   const int oa = p.fx_omega_a;
   const S31 om = S31{p.fx_omega_s31[0], p.fx_omega_s31[1]};
+  const S31 c1mw = S31{p.fx_1mw_s31[0], p.fx_1mw_s31[1]};
   bool out_bad = false;
-  // new population q from T = (f_eq_q - f_q) 2^62 and the source S (2^62)
-  auto update = [&](int q, long long T, long long S) {
-    // (f + omega T + S) 2^62, summed modulo 2^64: a value outside (-2, 2)
-    // wraps to one that fails the range check
-    const long long X = (long long)((Fq[q] << 2) + (unsigned long long)(oa * T) +
-                                    (unsigned long long)mul62(split(T), om) +
-                                    (unsigned long long)S);
+  auto store = [&](int q, long long X) {
     const double r = fixed62_to_double(X, out_bad);
     if (active) pop(next, p.V, q)[(uint32_t)idx] = r;
+  };
+  // new population q from T = (f_eq_q - f_q) 2^62 and the source S (2^62):
+  // (f + omega T + S) 2^62, summed modulo 2^64 (a value outside (-2, 2) wraps
+  // to one that fails the range check)
+  auto update = [&](int q, long long T, long long S) {
+    store(q, (long long)((Fq[q] << 2) + (unsigned long long)(oa * T) +
+                         (unsigned long long)mul62(split(T), om) + (unsigned long long)S));
+  };
+  // the moving populations as (1 - omega) f + omega w rho (1 + E +- O) + S,
+  // Omega = omega w rho per weight (< 1/2 for the moving weights, rho < 2):
+  // two products a population instead of three
+  auto update_moving = [&](int q, S31 Omega_s, long long Omega, long long EO, long long S) {
+    store(q, (long long)((unsigned long long)mul62(split((long long)(Fq[q] << 2)), c1mw) +
+                         (unsigned long long)Omega + (unsigned long long)mul62(Omega_s, split(EO)) +
+                         (unsigned long long)S));
   };
   // rest population: s = 0, R_0 = -1.5 u^2 + 1.125 u^4
   {
@@ -265,9 +277,8 @@ __device__ __forceinline__ bool bgk_node_fixed(const double f[], const double F[
     const long long E = ((9 * s2) >> 1) + P0 + mul62(s2s, split((27 * s2 - 54 * u2) >> 3));
     const long long O = 3 * s + ((9 * mul62(ss, split(s2 - u2))) >> 1);
     const long long wrv = mul62(rho61, csplit(K::W63(q)));  // w_q rho 2^62 (w_q = w_-q)
-    const S31 wr = split(wrv);
-    const long long Tp = wrv - (long long)(Fq[q] << 2) + mul62(wr, split(E + O));
-    const long long Tm = wrv - (long long)(Fq[qb] << 2) + mul62(wr, split(E - O));
+    const long long Omega = oa * wrv + mul62(split(wrv), om);  // omega w_q rho 2^62
+    const S31 Omega_s = split(Omega);
     long long Sp = 0, Sm = 0;
     if (FS == FS_GUO) {
       // ((c - u) + 3 (c.u) c).F = c.F - u.F + 3 s c.F
@@ -275,8 +286,8 @@ __device__ __forceinline__ bool bgk_node_fixed(const double f[], const double F[
       Sp = mul62(split(cF - uF + e3), S31{p.fx_guo_s31[q][0], p.fx_guo_s31[q][1]});
       Sm = mul62(split(-cF - uF + e3), S31{p.fx_guo_s31[qb][0], p.fx_guo_s31[qb][1]});
     }
-    update(q, Tp, Sp);
-    update(qb, Tm, Sm);
+    update_moving(q, Omega_s, Omega, E + O, Sp);
+    update_moving(qb, Omega_s, Omega, E - O, Sm);
   }
   if (__any_sync(0xffffffffu, out_bad)) return false;
   // stored fields and diagnostics (store / diagnostics steps only): FP64

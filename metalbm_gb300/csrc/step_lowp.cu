@@ -1418,7 +1418,9 @@ __device__ __forceinline__ void elbm_node(const typename Storage<ST>::T* __restr
   }
   if (!defer) {
     // update in FP32: f - alpha beta f_neq + S (Collision.h:243-258)
-    const float ab = narrow_rn(alpha * p.beta);
+    // alpha beta in FP32 (2 beta = bgk_b_f exactly halved): its rounding
+    // scales f_neq, a small part of the FP32-rounded update
+    const float ab = narrow_rn(alpha) * (0.5f * p.bgk_b_f);
     float uf[3] = {0.0f, 0.0f, 0.0f}, Ff[3] = {0.0f, 0.0f, 0.0f}, rf = 1.0f, uF = 0.0f;
     PolyNode nu{0.0f, 0.0f}, nv{0.0f, 0.0f};
     float vf[3] = {0.0f, 0.0f, 0.0f};
@@ -1495,7 +1497,10 @@ __device__ __forceinline__ void elbm_node(const typename Storage<ST>::T* __restr
     }
   }
   if (MODE == ELBM_MAIN) {
-    if (!(rho > 0.0) || !isfinite(rho)) atomicOr(p.err_word, ERR_NONFINITE);
+    {  // rho positive and finite, tested on its bits (no FP64 compare)
+      const long long rb = __double_as_longlong(rho);
+      if (rb <= 0 || rb >= 0x7ff0000000000000LL) atomicOr(p.err_word, ERR_NONFINITE);
+    }
     if (p.store || p.diag) {
       // rho, u_hydro and F of every node; alpha by the kernel that solves it
       mass = rho;

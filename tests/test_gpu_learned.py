@@ -130,6 +130,49 @@ def test_zero_model_equals_constant_two_guess():
 
 
 @pytest.mark.gpu
+def test_learned_kernel_only_where_a_node_lacks_a_solved_alpha():
+    """MLBM_GUESS_LEARNED with a zero-weight model (its guess is exactly 2):
+    the first call after initialisation runs the network (learned_nodes > 0)
+    and matches the previous-alpha guess bit for bit; a later call starts with
+    every alpha solved and runs the kernels without the network
+    (learned_nodes = 0), still bit for bit; after mlbm_set_alpha with nodes
+    at alpha = 2 the next call runs the network on those (the solved ones of
+    them)."""
+    from metalbm_gb300 import InputDeck, Lattice, MlpModel, fields
+    z = MlpModel.init(27, np.ones(27, np.float32), 0.05, seed=0)
+    z.w1[:] = 0; z.w2[:] = 0; z.w3[:] = 0; z.b3 = 0.0
+    shape = (16, 12, 10)
+    rho, u = fields.taylor_green(shape, u0=0.08)
+    out = {}
+    for guess in ("learned", "previous"):
+        deck = InputDeck(latticeT="D3Q27", collisionT="ELBM", relaxationTime=0.50025,
+                         globalLength=shape, storage="f32", alphaSolver="residual",
+                         alphaGuess=guess, newtonTolerance=1e-12, deviationThreshold=0.0)
+        with Lattice(deck) as L:
+            if guess == "learned":
+                L.set_alpha_model(z)
+            L.init_equilibrium(rho, u)
+            L.step(2)
+            d1 = L.diagnostics()
+            L.step(3, store=True)
+            d2 = L.diagnostics()
+            f2 = L.fields()
+            a = f2["alpha"].copy()
+            a[:100] = 2.0  # 100 nodes without a solved alpha
+            L.set_alpha(a)
+            L.step(1)
+            d3 = L.diagnostics()
+            out[guess] = (d1, d2, f2, d3, L.populations())
+    dl, dp = out["learned"], out["previous"]
+    assert dl[0]["learned_nodes"] > 0 and dp[0]["learned_nodes"] == 0
+    assert dl[1]["learned_nodes"] == 0
+    assert dl[1]["newton_iterations"] == dp[1]["newton_iterations"]
+    assert np.array_equal(dl[2]["alpha"], dp[2]["alpha"]) and np.array_equal(dl[2]["u"], dp[2]["u"])
+    assert 0 < dl[3]["learned_nodes"] <= 100 and dp[3]["learned_nodes"] == 0
+    assert np.array_equal(dl[4], dp[4])
+
+
+@pytest.mark.gpu
 def test_learned_guess_at_equal_residual():
     """Train on samples of a plain run (the library's sample logger and GPU
     training kernels), then start from the initial state, where no node has a
