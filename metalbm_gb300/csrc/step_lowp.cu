@@ -475,7 +475,11 @@ __device__ __forceinline__ void bgk_node2(const StepParams& p, uint32_t x, uint3
     }
   }
   const float2 rho = add2(bcast2(1.0f), rhop);
-  const float2 irho = make_float2(1.0f / rho.x, 1.0f / rho.y);
+  // SFU reciprocals (within 1 ulp; u feeds FP16-rounded populations)
+  float ix, iy;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(ix) : "f"(rho.x));
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(iy) : "f"(rho.y));
+  const float2 irho = make_float2(ix, iy);
 #pragma unroll
   for (int k = 0; k < 3; ++k) u[k] = mul2(j[k], irho);
   float2 F[3] = {bcast2(0.0f), bcast2(0.0f), bcast2(0.0f)};
@@ -486,7 +490,10 @@ __device__ __forceinline__ void bgk_node2(const StepParams& p, uint32_t x, uint3
   const float2 common = mul2(u2, fma2(bcast2(1.125f), u2, bcast2(-1.5f)));
   const float2 A = fma2(bcast2(-6.75f), u2, bcast2(4.5f));
   const float2 B = fma2(bcast2(-4.5f), u2, bcast2(3.0f));
-  const float2 b = bcast2(p.bgk_b_f);
+  // d' = d + b (d_eq - d) as (1 - b) d + b w_q (rho' + rho P_q): b w_q rho'
+  // and b w_q rho once a weight
+  const float bs = p.bgk_b_f;
+  const float2 c1b = bcast2(1.0f - bs);
   float2 uF = bcast2(0.0f), v[3] = {bcast2(0.0f), bcast2(0.0f), bcast2(0.0f)};
   float2 commonv = common, Av = A, Bv = B;
   if (FS == FS_GUO) {
@@ -506,8 +513,8 @@ __device__ __forceinline__ void bgk_node2(const StepParams& p, uint32_t x, uint3
   }
   {  // rest population
     const float ws = (float)L::w(0) * S::template scale<LAT>(0);
-    const float2 deq = mul2(bcast2(ws), fma2(rho, common, rhop));
-    float2 r = fma2(b, sub2(deq, d[0]), d[0]);
+    const float2 bw = bcast2(ws * bs);
+    float2 r = fma2(mul2(bw, rho), common, fma2(c1b, d[0], mul2(bw, rhop)));
     if (FS == FS_GUO) r = fma2(bcast2(-(p.guo_kt_f * ws)), uF, r);
     if (FS == FS_EDM) r = fma2(mul2(bcast2(ws), rho), sub2(commonv, common), r);
     d[0] = r;
@@ -520,10 +527,10 @@ __device__ __forceinline__ void bgk_node2(const StepParams& p, uint32_t x, uint3
       const float2 cu = cdotf2<LAT>(q, u);
       float2 E, O;
       poly_pair2(cu, A, B, common, E, O);
-      const float2 dq = mul2(bcast2(ws), fma2(rho, add2(E, O), rhop));
-      const float2 dqb = mul2(bcast2(ws), fma2(rho, sub2(E, O), rhop));
-      float2 rq = fma2(b, sub2(dq, d[q]), d[q]);
-      float2 rqb = fma2(b, sub2(dqb, d[qb]), d[qb]);
+      const float2 bw = bcast2(ws * bs);
+      const float2 bwr = mul2(bw, rho), bwp = mul2(bw, rhop);
+      float2 rq = fma2(bwr, add2(E, O), fma2(c1b, d[q], bwp));
+      float2 rqb = fma2(bwr, sub2(E, O), fma2(c1b, d[qb], bwp));
       if (FS == FS_GUO) {
         const float2 cF = cdotf2<LAT>(q, F);
         const float2 Es = fma2(mul2(bcast2(3.0f), cu), cF, neg2(uF));
