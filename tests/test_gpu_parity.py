@@ -466,6 +466,35 @@ def test_f64_fixed_point_falls_back_out_of_range():
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("shape", [(9, 7, 24), (5, 3, 8), (33, 5, 16), (4, 6, 512), (3, 4, 88),
+                                   (6, 5, 7)])
+@pytest.mark.parametrize("lattice,forcing,force", [("D3Q19", "Guo", "Kolmogorov"),
+                                                   ("D3Q27", "None", "None")])
+def test_f16_tracks_f64_on_more_shapes(shape, lattice, forcing, force):
+    """FP16-shifted storage on lines of 8 to 512 nodes and on an odd Lz (the
+    one-node kernel), a force varying along y, against the FP64 kernel, to
+    the FP16 storage tolerance, with the diagnostics."""
+    from metalbm_gb300 import InputDeck, Lattice, fields
+    rho, u = fields.perturbed_rest(shape, 3, 0.02, seed=9, rho_amplitude=0.005)
+    out = {}
+    for st in ("f64", "f16_shifted"):
+        with Lattice(InputDeck(latticeT=lattice, forcingSchemeT=forcing, forceT=force,
+                               relaxationTime=0.6, forceAmplitude=(1e-4, 0.0, 0.0),
+                               forceWaveLength=(float(shape[1]), 1.0, 1.0), kolmogorovAxis=1,
+                               globalLength=shape, storage=st)) as lat:
+            lat.init_equilibrium(rho, u)
+            lat.step(20, store=True, diagnostics=True)
+            out[st] = lat.fields()
+            out[st + "_d"] = lat.diagnostics()
+    assert rel(out["f16_shifted"]["u"], out["f64"]["u"]) <= 5e-3
+    assert rel(out["f16_shifted"]["rho"], out["f64"]["rho"]) <= 5e-5
+    d16, d64 = out["f16_shifted_d"], out["f64_d"]
+    assert abs(d16["energy"] - d64["energy"]) <= 2e-2 * d64["energy"]
+    assert abs(d16["mass"] - d64["mass"]) <= 1e-6 * d64["mass"]
+    assert d16["error_word"] == 0
+
+
+@pytest.mark.gpu
 @pytest.mark.parametrize("lattice", ["D3Q19", "D3Q27", "D3Q15"])
 @pytest.mark.parametrize("forcing,force", [("Guo", "Kolmogorov"), ("ExactDifferenceMethod", "Sinusoidal")])
 def test_f16_two_nodes_packed_tracks_f64(lattice, forcing, force):
