@@ -1099,9 +1099,20 @@ __device__ __forceinline__ long long fixed60(float v, bool& bad) {
   return (b >> 31) ? -a : a;
 }
 
+// f 2^32 as an exact integer for a float f in [2^-9, 1): the significand
+// with its leading one shifted left by e - 118 in [0, 8]; `bad` outside that
+// range.
+__device__ __forceinline__ long long fixed32(float v, bool& bad) {
+  const uint32_t b = __float_as_uint(v);
+  bad |= b - 0x3b000000u >= 0x04800000u;
+  return (long long)(((b & 0x7fffffu) | 0x800000u) << (((b >> 23) - 118u) & 31u));
+}
+
 // rho (or rho - 1 for F16 storage, whose stored deviations sum to it) and
-// the momentum as exact fixed-point sums of the stored values, each rounded
-// once to FP64; FP64 sums where a value is out of the fixed-point range.
+// the momentum as exact fixed-point sums of the stored values (2^-32 units
+// for FP32 populations in [2^-9, 1), 2^-60 for the FP16 deviations), each
+// rounded once to FP64; FP64 sums where a value is out of the fixed-point
+// range.
 template <int LAT, int ST>
 __device__ __forceinline__ void moments_exact(const Pulled<LAT, ST>& P, double& rho, double& rhop,
                                               double j[3]) {
@@ -1110,7 +1121,7 @@ __device__ __forceinline__ void moments_exact(const Pulled<LAT, ST>& P, double& 
   bool bad = false;
 #pragma unroll
   for (int q = 0; q < L::Q; ++q) {
-    const long long a = fixed60(P.v[q], bad);
+    const long long a = ST == ST_F32 ? fixed32(P.v[q], bad) : fixed60(P.v[q], bad);
     S += a;
 #pragma unroll
     for (int k = 0; k < L::D; ++k) {
@@ -1119,11 +1130,12 @@ __device__ __forceinline__ void moments_exact(const Pulled<LAT, ST>& P, double& 
     }
   }
   if (!bad) {
-    const double Sd = ll_scaled(S, 60);
+    constexpr int kScale = ST == ST_F32 ? 32 : 60;
+    const double Sd = ll_scaled(S, kScale);
     rho = ST == ST_F32 ? Sd : 1.0 + Sd;
     rhop = ST == ST_F32 ? Sd - 1.0 : Sd;
 #pragma unroll
-    for (int k = 0; k < 3; ++k) j[k] = ll_scaled(J[k], 60);
+    for (int k = 0; k < 3; ++k) j[k] = ll_scaled(J[k], kScale);
   } else {
     rho = P.f64(0);
     j[0] = j[1] = j[2] = 0.0;
