@@ -922,8 +922,7 @@ struct SeriesAcc2 {
 
 template <int LAT>
 __device__ __forceinline__ void series_terms2(float2 f, dfl2 n, int expw, const LogEntryFineF* fine,
-                                              float2 C, bool tierB, SeriesAcc2& a, double& M3,
-                                              double& M4) {
+                                              float2 C, SeriesAcc2& a) {
   constexpr bool kUniform = uniform_weight_significand<LAT>();
   const uint32_t bx = __float_as_uint(f.x), by = __float_as_uint(f.y);
   const int dx = (int)((bx >> 23) & 0xffu) - (127 + expw);
@@ -982,20 +981,8 @@ __device__ __forceinline__ void series_terms2(float2 f, dfl2 n, int expw, const 
   }
   const float2 rf = mul2(n.hi, y0);
   float2 tt = mul2(n.hi, mul2(rf, rf));  // f r^3
-  if (tierB) {
-    const double nqx = widen_exact(n.hi.x) + widen_exact(n.lo.x);
-    const double nqy = widen_exact(n.hi.y) + widen_exact(n.lo.y);
-    const double gx = nqx * fma(widen_exact(y0.x), widen_exact(ee.x), widen_exact(y0.x));
-    const double gy = nqy * fma(widen_exact(y0.y), widen_exact(ee.y), widen_exact(y0.y));
-    const double p2x = gx * nqx, p2y = gy * nqy;
-    M3 = fma(p2x, gx, M3);
-    M4 = fma(p2x * gx, gx, M4);
-    M3 = fma(p2y, gy, M3);
-    M4 = fma(p2y * gy, gy, M4);
-  } else {
-    a.M3f = add2(a.M3f, tt);
-    a.M4f = fma2(tt, rf, a.M4f);
-  }
+  a.M3f = add2(a.M3f, tt);  // tier A (tier B: make_series_dfl's FP64 pass)
+  a.M4f = fma2(tt, rf, a.M4f);
   tt = mul2(tt, mul2(rf, rf));
   a.M5 = add2(a.M5, tt);  // f r^5
   tt = mul2(tt, rf);
@@ -1039,8 +1026,7 @@ __device__ __forceinline__ HSeries make_series_dfl(const Pulled<LAT, ST_F32>& P,
     // every product with it is an exact zero)
     nfr[0] = nd[0].hi;
     const dfl2 n2 = dfl2_pack(nd[0], dfl{0.0f, 0.0f});
-    series_terms2<LAT>(make_float2(P.v[0], 1.0f), n2, exponent_of(L::w(0)), fine, mconst[0],
-                       tierB, a, M3, M4);
+    series_terms2<LAT>(make_float2(P.v[0], 1.0f), n2, exponent_of(L::w(0)), fine, mconst[0], a);
   }
 #pragma unroll
   for (int q = 1; q < L::Q; ++q) {
@@ -1049,7 +1035,27 @@ __device__ __forceinline__ HSeries make_series_dfl(const Pulled<LAT, ST_F32>& P,
     nfr[q] = nd[q].hi;
     nfr[qb] = nd[qb].hi;
     series_terms2<LAT>(make_float2(P.v[q], P.v[qb]), dfl2_pack(nd[q], nd[qb]),
-                       exponent_of(L::w(q)), fine, mconst[q], tierB, a, M3, M4);
+                       exponent_of(L::w(q)), fine, mconst[q], a);
+  }
+  // tier B: M3 and M4 in FP64 in a pass of their own (kept out of the packed
+  // loop's code), the populations in the packed loop's order
+  if (tierB) {
+    auto fp64_terms = [&](float f, dfl n) {
+      const float y0 = rcp_sfu(f);
+      const float ee = fmaf(-f, y0, 1.0f);
+      const double nq = widen_exact(n.hi) + widen_exact(n.lo);
+      const double g = nq * fma(widen_exact(y0), widen_exact(ee), widen_exact(y0));  // r_q
+      const double p2 = g * nq;
+      M3 = fma(p2, g, M3);
+      M4 = fma(p2 * g, g, M4);
+    };
+    fp64_terms(P.v[0], nd[0]);
+#pragma unroll
+    for (int q = 1; q < L::Q; ++q) {
+      if (!is_pair_leader<LAT>(q)) continue;
+      fp64_terms(P.v[q], nd[q]);
+      fp64_terms(P.v[opposite<LAT>(q)], nd[opposite<LAT>(q)]);
+    }
   }
   // B1 = (bh + bl) + ln2 (eh + el), M2 = mh + ml, over both lanes, each
   // rounded once to FP64
