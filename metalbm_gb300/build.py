@@ -32,17 +32,20 @@ PER_FILE = {"step_f64.cu": ["-fmad=false"], "step_f64x.cu": ["-fmad=false"]}
 
 def units() -> list[tuple[Path, list[str], str]]:
     """(source, extra flags, object stem): the step kernels are compiled once
-    per lattice (and storage format) so the units build in parallel."""
+    per lattice (and storage format, and for the low-precision step forcing
+    scheme) so the units build in parallel."""
     out = []
     for src in sorted(CSRC.glob("*.cu")):
         extra = PER_FILE.get(src.name, [])
-        if src.name == "step_f64.cu":
-            out += [(src, extra + [f"-DMLBM_LAT={l}"], f"{src.stem}_L{l}") for l in range(6)]
+        if src.name == "step_f64.cu":  # six lattices; one forcing scheme a unit
+            out += [(src, extra + [f"-DMLBM_LAT={l}", f"-DMLBM_FS={fs}"], f"{src.stem}_L{l}_F{fs}")
+                    for l in range(6) for fs in range(4)]
         elif src.name == "step_f64x.cu":  # D2Q9, D3Q19, D3Q27, D3Q15
             out += [(src, extra + [f"-DMLBM_LAT={l}"], f"{src.stem}_L{l}") for l in range(4)]
-        elif src.name == "step_lowp.cu":
-            out += [(src, extra + [f"-DMLBM_LAT={l}", f"-DMLBM_ST={st}"], f"{src.stem}_L{l}_S{st}")
-                    for l in range(4) for st in (1, 2)]  # D2Q9, D3Q19, D3Q27, D3Q15
+        elif src.name == "step_lowp.cu":  # D2Q9, D3Q19, D3Q27, D3Q15; one forcing scheme a unit
+            out += [(src, extra + [f"-DMLBM_LAT={l}", f"-DMLBM_ST={st}", f"-DMLBM_FS={fs}"],
+                     f"{src.stem}_L{l}_S{st}_F{fs}")
+                    for l in range(4) for st in (1, 2) for fs in range(4)]
         else:
             out.append((src, extra, src.stem))
     return out
@@ -98,8 +101,16 @@ def build(force: bool = False, verbose: bool = False) -> Path:
         return LIB
     BUILD.mkdir(exist_ok=True)
     todo = units()
-    # longest units first
-    todo.sort(key=lambda u: 0 if u[0].name.startswith("step_") else 1)
+    # longest units first: the D3Q27 low-precision steps (the entropic
+    # kernels) and the D3Q33 / D3Q27 FP64 steps, then the other steps, the rest
+    def cost(u):
+        src, extra, _ = u
+        if src.name == "step_lowp.cu":
+            return (0 if "-DMLBM_LAT=2" in extra else 1, "-DMLBM_ST=2" in extra)
+        if src.name == "step_f64.cu":
+            return (0 if ("-DMLBM_LAT=5" in extra or "-DMLBM_LAT=2" in extra) else 1, True)
+        return (2 if src.name.startswith("step_") else 3, False)
+    todo.sort(key=cost)
     with cf.ThreadPoolExecutor(max(1, min(len(todo), os.cpu_count() or 1))) as ex:
         results = list(ex.map(_compile, todo))
     (BUILD / "ptxas.log").write_text("\n".join(log for _, log in results))

@@ -250,38 +250,46 @@ static cudaError_t launch_elbm(const double* prev, double* next, const StepParam
   return cudaGetLastError();
 }
 
-template <int LAT>
-static cudaError_t dispatch_fs(int collision, int fs, const double* prev, double* next,
-                               const StepParams& p, cudaStream_t s) {
-  if (collision == 0) {
-    switch (fs) {
-      case FS_NONE: return launch_bgk<LAT, FS_NONE>(prev, next, p, s);
-      case FS_GUO: return launch_bgk<LAT, FS_GUO>(prev, next, p, s);
-      case FS_SHANCHEN: return launch_bgk<LAT, FS_SHANCHEN>(prev, next, p, s);
-      case FS_EDM: return launch_bgk<LAT, FS_EDM>(prev, next, p, s);
-    }
-  } else {
-    switch (fs) {
-      case FS_NONE: return launch_elbm<LAT, FS_NONE>(prev, next, p, s);
-      case FS_GUO: return launch_elbm<LAT, FS_GUO>(prev, next, p, s);
-      case FS_SHANCHEN: return launch_elbm<LAT, FS_SHANCHEN>(prev, next, p, s);
-      case FS_EDM: return launch_elbm<LAT, FS_EDM>(prev, next, p, s);
-    }
-  }
-  return cudaErrorInvalidValue;
-}
-
-// This file is compiled once per lattice (MLBM_LAT = 0..5) so the six sets
-// of kernels build in parallel; misc.cu dispatches on the lattice.
-#ifndef MLBM_LAT
-#error "compile step_f64.cu with -DMLBM_LAT=<0..5>"
+// This file is compiled once per (lattice, forcing scheme) pair (MLBM_LAT =
+// 0..5, MLBM_FS = 0..3: None, Guo, Shan-Chen, EDM) so the units build in
+// parallel. Each unit holds the step kernels of its forcing scheme; the FS_NONE
+// unit also holds the lattice's dispatcher and the kernels that do not depend
+// on the forcing scheme. misc.cu dispatches on the lattice.
+#if !defined(MLBM_LAT) || !defined(MLBM_FS)
+#error "compile step_f64.cu with -DMLBM_LAT=<0..5> -DMLBM_FS=<0..3>"
 #endif
 #define MLBM_CAT2(a, b) a##b
 #define MLBM_CAT(a, b) MLBM_CAT2(a, b)
+#define MLBM_FN_FS(fs) MLBM_CAT(MLBM_CAT(MLBM_CAT(step_f64_L, MLBM_LAT), _F), fs)
 
+// one forcing scheme's step launches (collision 0 BGK, otherwise entropic)
+cudaError_t MLBM_FN_FS(0)(int collision, const double* prev, double* next, const StepParams& p,
+                          cudaStream_t s);
+cudaError_t MLBM_FN_FS(1)(int collision, const double* prev, double* next, const StepParams& p,
+                          cudaStream_t s);
+cudaError_t MLBM_FN_FS(2)(int collision, const double* prev, double* next, const StepParams& p,
+                          cudaStream_t s);
+cudaError_t MLBM_FN_FS(3)(int collision, const double* prev, double* next, const StepParams& p,
+                          cudaStream_t s);
+
+cudaError_t MLBM_FN_FS(MLBM_FS)(int collision, const double* prev, double* next,
+                                const StepParams& p, cudaStream_t s) {
+  if (collision == 0) return launch_bgk<MLBM_LAT, MLBM_FS>(prev, next, p, s);
+  return launch_elbm<MLBM_LAT, MLBM_FS>(prev, next, p, s);
+}
+
+#if MLBM_FS == 0
 cudaError_t MLBM_CAT(step_f64_L, MLBM_LAT)(int collision, int forcing, const double* prev,
                                              double* next, const StepParams& p, cudaStream_t s) {
-  return dispatch_fs<MLBM_LAT>(collision, forcing, prev, next, p, s);
+  static_assert(FS_NONE == 0 && FS_GUO == 1 && FS_SHANCHEN == 2 && FS_EDM == 3,
+                "the units are numbered by the forcing scheme's value");
+  switch (forcing) {
+    case FS_NONE: return MLBM_FN_FS(0)(collision, prev, next, p, s);
+    case FS_GUO: return MLBM_FN_FS(1)(collision, prev, next, p, s);
+    case FS_SHANCHEN: return MLBM_FN_FS(2)(collision, prev, next, p, s);
+    case FS_EDM: return MLBM_FN_FS(3)(collision, prev, next, p, s);
+  }
+  return cudaErrorInvalidValue;
 }
 
 cudaError_t MLBM_CAT(init_f64_L, MLBM_LAT)(const double* rho, const double* u, double* f,
@@ -308,5 +316,6 @@ cudaError_t MLBM_CAT(log_samples_f64_L, MLBM_LAT)(const double* prev, const Step
   samples_f64_kernel<MLBM_LAT><<<grid, 128, 0, s>>>(prev, p, nodes, n, features, alpha, solved);
   return cudaGetLastError();
 }
+#endif  // MLBM_FS == 0
 
 }  // namespace mlbm

@@ -1846,25 +1846,48 @@ static cudaError_t launch_lowp(int collision, const void* prev, void* next, cons
   return cudaGetLastError();
 }
 
-// This file is compiled once per (lattice, storage) pair (MLBM_LAT = 0..3:
-// D2Q9, D3Q19, D3Q27, D3Q15 -- the lattices of reach 1 with inv_cs2 = 3 and a
-// conserving equilibrium, which this file's pair algebra and series form
-// assume; MLBM_ST = 1 F32 or 2 F16-shifted); misc.cu dispatches.
-#if !defined(MLBM_LAT) || !defined(MLBM_ST)
-#error "compile step_lowp.cu with -DMLBM_LAT=<0..3> -DMLBM_ST=<1|2>"
+// This file is compiled once per (lattice, storage, forcing scheme) triple
+// (MLBM_LAT = 0..3: D2Q9, D3Q19, D3Q27, D3Q15 -- the lattices of reach 1 with
+// inv_cs2 = 3 and a conserving equilibrium, which this file's pair algebra and
+// series form assume; MLBM_ST = 1 F32 or 2 F16-shifted; MLBM_FS = 0..3: None,
+// Guo, Shan-Chen, EDM), so that the units build in parallel. Each unit holds
+// the step kernels of its forcing scheme; the FS_NONE unit also holds the
+// (lattice, storage) pair's dispatcher and the kernels that do not depend on
+// the forcing scheme. misc.cu dispatches on the lattice and storage.
+#if !defined(MLBM_LAT) || !defined(MLBM_ST) || !defined(MLBM_FS)
+#error "compile step_lowp.cu with -DMLBM_LAT=<0..3> -DMLBM_ST=<1|2> -DMLBM_FS=<0..3>"
 #endif
 #define MLBM_CAT2(a, b, c, d) a##b##c##d
 #define MLBM_CAT(a, b, c, d) MLBM_CAT2(a, b, c, d)
 #define MLBM_FN(name) MLBM_CAT(name, MLBM_LAT, _S, MLBM_ST)
+#define MLBM_FN_FS(fs) MLBM_CAT(MLBM_FN(step_lowp_L), _F, fs, )
 using StT = typename Storage<MLBM_ST>::T;
 
+// one forcing scheme's step launches
+cudaError_t MLBM_FN_FS(0)(int collision, const void* prev, void* next, const StepParams& p,
+                          cudaStream_t s);
+cudaError_t MLBM_FN_FS(1)(int collision, const void* prev, void* next, const StepParams& p,
+                          cudaStream_t s);
+cudaError_t MLBM_FN_FS(2)(int collision, const void* prev, void* next, const StepParams& p,
+                          cudaStream_t s);
+cudaError_t MLBM_FN_FS(3)(int collision, const void* prev, void* next, const StepParams& p,
+                          cudaStream_t s);
+
+cudaError_t MLBM_FN_FS(MLBM_FS)(int collision, const void* prev, void* next, const StepParams& p,
+                                cudaStream_t s) {
+  return launch_lowp<MLBM_LAT, MLBM_FS, MLBM_ST>(collision, prev, next, p, s);
+}
+
+#if MLBM_FS == 0
 cudaError_t MLBM_FN(step_lowp_L)(int collision, int fs, const void* prev, void* next,
                                  const StepParams& p, cudaStream_t s) {
+  static_assert(FS_NONE == 0 && FS_GUO == 1 && FS_SHANCHEN == 2 && FS_EDM == 3,
+                "the units are numbered by the forcing scheme's value");
   switch (fs) {
-    case FS_NONE: return launch_lowp<MLBM_LAT, FS_NONE, MLBM_ST>(collision, prev, next, p, s);
-    case FS_GUO: return launch_lowp<MLBM_LAT, FS_GUO, MLBM_ST>(collision, prev, next, p, s);
-    case FS_SHANCHEN: return launch_lowp<MLBM_LAT, FS_SHANCHEN, MLBM_ST>(collision, prev, next, p, s);
-    case FS_EDM: return launch_lowp<MLBM_LAT, FS_EDM, MLBM_ST>(collision, prev, next, p, s);
+    case FS_NONE: return MLBM_FN_FS(0)(collision, prev, next, p, s);
+    case FS_GUO: return MLBM_FN_FS(1)(collision, prev, next, p, s);
+    case FS_SHANCHEN: return MLBM_FN_FS(2)(collision, prev, next, p, s);
+    case FS_EDM: return MLBM_FN_FS(3)(collision, prev, next, p, s);
   }
   return cudaErrorInvalidValue;
 }
@@ -1911,5 +1934,6 @@ cudaError_t MLBM_FN(log_samples_lowp_L)(const void* prev, const StepParams& p,
       (const StT*)prev, p, nodes, n, features, alpha, solved);
   return cudaGetLastError();
 }
+#endif  // MLBM_FS == 0
 
 }  // namespace mlbm
