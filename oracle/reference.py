@@ -1,8 +1,8 @@
 """Runner for the reference metaLBM binaries built by oracle/build_ref.py.
 
 Test infrastructure only; usable where the reference sources exist (the
-golden-vector generator and the CPU timing in this container). Nothing that
-runs on a GPU machine needs it.
+golden-vector generator and the CPU timing on the machine that holds them).
+Nothing the GPU tests, smoke() or bench.py run needs it.
 """
 from __future__ import annotations
 
