@@ -5,11 +5,11 @@ transparent-huge-page size (hpage_pmd_size: 2 MiB with 4 KiB base pages,
 512 MiB with the 64 KiB base pages of GB300 hosts), asks for transparent huge
 pages (madvise MADV_HUGEPAGE) and registers the range with CUDA
 (cudaHostRegister). Without the alignment a mapping gets few or no huge pages
-of that size. On GB300 machines with 64 KiB pages the transfers of the 4.3 GB
+of that size. On GB300 hosts with 64 KiB pages the transfers of the 4.3 GB
 field arrays of a 512^3 lattice were bound by the translation of the host
 pages: the copy engines uploaded them in 300-450 ms, a copy kernel over the
 host link in ~30 ms with warm translations and ~300 ms with cold ones (those
-boxes granted no 512 MiB transparent huge page, aligned or not).
+hosts granted no 512 MiB transparent huge page, aligned or not).
 """
 from __future__ import annotations
 
